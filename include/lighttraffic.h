@@ -1,0 +1,213 @@
+/*
+ * lighttraffic.h -- C ABI of the GB300 random-walk engine.
+ *
+ * The reference (LightTraffic) has no FFI: its boundary is a compile-time
+ * template plugin (struct Walker / App / AppManager, app/ppr.cu:11-94) driven
+ * by LightTraffic<AppManager,App,Walker>::start (src/LightTraffic.h:11-44) and
+ * configured from the command line by Config (src/Config.h:38-89).  Each entry
+ * point below names the reference interface it replaces.
+ *
+ * Conventions
+ *  - Every function returns lt_status; nothing calls exit() (the reference's
+ *    gpuCall does, src/utils/GPUCall.h:3-11).  lt_last_error() gives a message
+ *    for the most recent failure on the calling thread.
+ *  - Output buffers are owned by the caller.  "host" buffers are ordinary or
+ *    pinned host memory; "device" buffers are device pointers on the engine's
+ *    GPU.
+ *  - One engine per host thread; an engine is not re-entrant (the reference
+ *    keeps static state in its scheduler too, src/Scheduler.h:394).
+ *  - Types follow src/Type.h:5-8: vertex ids u32, edge offsets u64.  Visit
+ *    counts are u64 (the reference's u32 counters overflow on hubs,
+ *    app/pagerank.cu:133-135).
+ *  - Randomness is Philox4x32-10 keyed by (seed, run, walker index, step
+ *    value), never by thread or schedule, so results are bit-identical for
+ *    every device cache size, scheduler and launch shape.
+ */
+#ifndef LIGHTTRAFFIC_H
+#define LIGHTTRAFFIC_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum lt_status {
+    LT_OK = 0,
+    LT_ERR_INVALID = 1,     /* bad argument */
+    LT_ERR_IO = 2,          /* file cannot be opened / read / written */
+    LT_ERR_FORMAT = 3,      /* truncated or inconsistent bcsr / .part file */
+    LT_ERR_NOMEM = 4,       /* host or device allocation failed */
+    LT_ERR_CUDA = 5,        /* a CUDA call failed */
+    LT_ERR_PARTITION = 6,   /* one vertex does not fit the partition size */
+    LT_ERR_TIMEOUT = 7,     /* a bounded device-side wait gave up */
+    LT_ERR_CAPACITY = 8,    /* a device queue or buffer limit was exceeded */
+    LT_ERR_UNSUPPORTED = 9  /* configuration not supported by this build */
+} lt_status;
+
+typedef enum lt_app { LT_APP_PPR = 0, LT_APP_PAGERANK = 1, LT_APP_WALK = 2 } lt_app;
+
+/* Where walkers start.  SOURCE: all at one vertex (src/walk/SingleSource.h:6-20);
+ * UNIFORM: a seeded uniform vertex each (src/walk/NodeSampler.h:5-15);
+ * PER_VERTEX: walker i starts at vertex i mod V. */
+typedef enum lt_start { LT_START_SOURCE = 0, LT_START_UNIFORM = 1, LT_START_PER_VERTEX = 2 } lt_start;
+
+typedef enum lt_sched { LT_SCHED_PLAIN = 0, LT_SCHED_FIFO = 1, LT_SCHED_LEARNED = 2 } lt_sched;
+
+typedef struct lt_graph lt_graph;
+typedef struct lt_engine lt_engine;
+
+typedef struct lt_graph_info {
+    uint32_t num_nodes;          /* V */
+    uint64_t num_edges;          /* E */
+    uint32_t num_partitions;     /* P */
+    uint64_t partition_bytes;    /* -s in bytes */
+    uint32_t max_nodes_in_partition;
+    uint64_t max_edges_in_partition;
+} lt_graph_info;
+
+typedef struct lt_engine_cfg {
+    int device;                      /* CUDA device ordinal (the reference fixes 0, app/ppr.cu:101) */
+    uint32_t num_device_partitions;  /* -p: partitions cached on the device (0 = all) */
+    uint64_t num_device_walkers;     /* -b: walkers held on the device (0 = all) */
+    int sched;                       /* lt_sched */
+    int pipeline;                    /* overlap partition loads with stepping (1 = on) */
+    uint64_t zerocopy_threshold;     /* walkers below which a cold partition is read zero-copy;
+                                        UINT64_MAX = default partitionSize/128/2 (src/Scheduler.h:295) */
+    uint64_t seed;                   /* Philox key */
+    int block_size;                  /* threads per CTA of the step kernel (0 = tuned default) */
+    int ctas_per_sm;                 /* resident CTAs per SM (0 = occupancy maximum) */
+} lt_engine_cfg;
+
+typedef struct lt_stats {
+    uint64_t updates;        /* App::update calls */
+    uint64_t moves;          /* hops along an edge */
+    uint64_t teleports;      /* PageRank jumps */
+    uint64_t iterations;     /* scheduler iterations (src/Scheduler.h:314) */
+    uint64_t explicit_iterations;
+    uint64_t h2d_graph_bytes;
+    uint64_t h2d_walker_bytes;
+    uint64_t d2h_walker_bytes;
+    uint64_t zerocopy_bytes;  /* estimate: 32 B per zero-copy access */
+    uint64_t partition_loads;
+    uint64_t kernel_launches;
+    double running_ms;        /* host wall time of the run ("Running Time") */
+    double graph_loading_ms;  /* event timers of src/Scheduler.h:284-288 */
+    double computing_ms;
+    double zerocopy_ms;
+    double walker_loading_ms;
+    double walker_evicting_ms;
+    uint64_t graph_loading_calls;
+    uint64_t computing_calls;
+    uint64_t zerocopy_calls;
+    uint64_t walker_loading_calls;
+    uint64_t walker_evicting_calls;
+    double step_kernel_ms;    /* CUDA-event time of the step kernels of the last run */
+} lt_stats;
+
+const char *lt_strerror(lt_status s);
+const char *lt_last_error(void);
+/* Library version string. */
+const char *lt_version(void);
+
+/* ------------------------------------------------------------------ graphs */
+
+/* Open a .bcsr graph (src/GraphLoader.h:30-48) and its partition table.
+ * materialize != 0: partition greedily with part_mb MiB partitions and write
+ * <path>.part (Config -m, src/Config.h:63-66 + EqualSizeStrategy,
+ * src/partition/PartitionStrategy.h:189-253,325-337); otherwise read
+ * <path>.part (MaterializedStrategy, :76-97).  The graph is held in pinned
+ * host memory (CPUGraph + cudaHostRegister, src/GraphLoader.h:115-157). */
+lt_status lt_graph_open(const char *bcsr_path, int materialize, uint64_t part_mb, lt_graph **out);
+
+/* Build a graph from caller CSR arrays (copied) and partition it with
+ * part_bytes-byte partitions (EqualSizeStrategy(CPUBuffer&, maxSize),
+ * src/partition/PartitionStrategy.h:239-241). */
+lt_status lt_graph_from_csr(uint32_t num_nodes, uint64_t num_edges, const uint64_t *rowptr,
+                            const uint32_t *col, uint64_t part_bytes, lt_graph **out);
+
+/* Generate a seeded RMAT graph on the GPU (no counterpart in the reference,
+ * whose datasets come from tools/convert_from_txt.cc): 2^scale raw vertices,
+ * num_edges directed edges, quadrant probabilities a,b,c,d quantised to 2^-16;
+ * isolated vertices removed keeping order (tools/rm_isolated_vertices.cc:70-87).
+ * Self-loops and duplicate edges are kept. */
+lt_status lt_graph_generate_rmat(int device, uint32_t scale, uint64_t num_edges, double a, double b,
+                                 double c, double d, uint64_t seed, uint64_t part_bytes,
+                                 lt_graph **out);
+
+lt_status lt_graph_info_get(const lt_graph *g, lt_graph_info *out);
+/* Copy the partition table: node_off[P+1], edge_off[P+1] (either may be NULL). */
+lt_status lt_graph_partitions(const lt_graph *g, uint32_t *node_off, uint64_t *edge_off);
+/* Host views of the CSR arrays (owned by the graph). */
+lt_status lt_graph_csr(const lt_graph *g, const uint64_t **rowptr, const uint32_t **col);
+lt_status lt_graph_write_bcsr(const lt_graph *g, const char *path);
+/* Write <bcsr_path>.part for the graph's partition table (materialize, :325-337). */
+lt_status lt_graph_write_part(const lt_graph *g, const char *bcsr_path);
+void lt_graph_close(lt_graph *g);
+
+/* Greedy partitioner on caller arrays (EqualSizeStrategy::init,
+ * src/partition/PartitionStrategy.h:193-218).  node_off/edge_off hold cap
+ * entries; on success *num_parts = P and entries [0, P] are written. */
+lt_status lt_partition_equal_size(const uint64_t *rowptr, uint32_t num_nodes, uint64_t max_bytes,
+                                  uint32_t *node_off, uint64_t *edge_off, uint32_t cap,
+                                  uint32_t *num_parts);
+
+/* ----------------------------------------------------------------- engines */
+
+void lt_engine_cfg_default(lt_engine_cfg *cfg);
+/* Replaces LightTraffic(Config&, AppManager&) + GPU/CPU device setup
+ * (src/LightTraffic.h:19-31, src/Device.h:13-43). */
+lt_status lt_engine_create(lt_graph *g, const lt_engine_cfg *cfg, lt_engine **out);
+void lt_engine_destroy(lt_engine *e);
+/* Drop every cached partition so the next run reloads them from the host. */
+lt_status lt_engine_drop_cache(lt_engine *e);
+
+/* PPR from one source (app/ppr.cu main + AppManager, :45-113): num_walkers
+ * walks with stop probability prob; counts_out (host, u64[V], may be NULL)
+ * receives per-vertex endpoint counts (AppManager::reduce, :65-67). */
+lt_status lt_run_ppr(lt_engine *e, uint32_t source, uint64_t num_walkers, float prob,
+                     uint64_t *counts_out);
+
+/* Walk-based PageRank (app/pagerank.cu:160-219): runs epochs of num_walkers
+ * walks of `length` updates each, teleport when U > alpha (alpha = 0.85 in the
+ * reference, app/pagerank.cu:6); counts_out (host, u64[V], may be NULL). */
+lt_status lt_run_pagerank(lt_engine *e, uint64_t num_walkers, uint32_t length, uint32_t runs,
+                          float alpha, int start_mode, uint64_t *counts_out);
+
+/* Fixed-length generic walk (app/genericwalk.cu:286-335) for run index `run`:
+ * endpoints_out (host, u32[W]) and paths_out (host, u32[W*(length+1)],
+ * INVALID 0xFFFFFFFF after a stop at a vertex without out-edges); either may
+ * be NULL. */
+lt_status lt_run_walk(lt_engine *e, uint64_t num_walkers, uint32_t length, uint32_t run,
+                      int start_mode, uint32_t *endpoints_out, uint32_t *paths_out);
+
+/* Statistics and phase timers of the last run (Scheduler::timing,
+ * src/Scheduler.h:440-453). */
+lt_status lt_engine_stats(const lt_engine *e, lt_stats *out);
+
+/* ------------------------------------------------- device-resident kernels */
+
+/* One pass of an app over a graph already resident in device memory, all
+ * pointers on the current device, launched on `stream` (cudaStream_t, NULL =
+ * legacy default stream).  This is the step kernel of randomWalkKernel
+ * (src/WalkManager.h:229-246) over the whole graph at once.
+ *   d_counts   : u64[V], added to (PPR / PageRank), may be NULL for LT_APP_WALK
+ *   d_endpoints: u32[W] or NULL; d_paths: u32[W*(length+1)] or NULL (walk only)
+ *   d_scratch  : device scratch of lt_walk_scratch_bytes() bytes; the call
+ *                clears it on `stream` before the kernel.
+ *   d_stats    : u64[3] or NULL: {updates, moves, teleports}, added to
+ * prob is the PPR stop probability or the PageRank alpha.  Returns without
+ * waiting for the kernel. */
+size_t lt_walk_scratch_bytes(void);
+lt_status lt_walk_device(int app, int start_mode, const uint64_t *d_rowptr, const uint32_t *d_col,
+                         uint32_t num_nodes, uint32_t source, uint64_t num_walkers,
+                         uint32_t length, float prob, uint32_t run, uint64_t seed,
+                         uint64_t *d_counts, uint32_t *d_endpoints, uint32_t *d_paths,
+                         void *d_scratch, uint64_t *d_stats, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* LIGHTTRAFFIC_H */

@@ -1,0 +1,275 @@
+"""lighttraffic_gb300 -- Python view of the GB300 random-walk engine.
+
+Every call goes through the C ABI of ``include/lighttraffic.h`` in the in-tree
+``liblighttraffic.so`` (built by ``lighttraffic_gb300.build``).  There is no
+Python or CPU implementation of the walks here: if the library is missing,
+importing the package raises.
+
+The names mirror the reference's app surface (app/ppr.cu, app/pagerank.cu,
+app/genericwalk.cu and src/Config.h):
+
+    g = Graph.open("G.bcsr", materialize=True, part_mb=32)      # -f G.bcsr -m -s 32
+    eng = Engine(g, partitions=0, batch=0, seed=1)              # -p / -b
+    counts = eng.ppr(source=0, walkers=2 * g.num_nodes, prob=0.15)
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(PKG, "liblighttraffic.so")
+BIN_DIR = os.path.join(PKG, "bin")
+
+APP_PPR, APP_PAGERANK, APP_WALK = 0, 1, 2
+START_SOURCE, START_UNIFORM, START_PER_VERTEX = 0, 1, 2
+SCHED_PLAIN, SCHED_FIFO, SCHED_LEARNED = 0, 1, 2
+INVALID_NODE = 0xFFFFFFFF
+
+STATUS = {0: "LT_OK", 1: "LT_ERR_INVALID", 2: "LT_ERR_IO", 3: "LT_ERR_FORMAT", 4: "LT_ERR_NOMEM",
+          5: "LT_ERR_CUDA", 6: "LT_ERR_PARTITION", 7: "LT_ERR_TIMEOUT", 8: "LT_ERR_CAPACITY",
+          9: "LT_ERR_UNSUPPORTED"}
+
+
+class LTError(RuntimeError):
+    def __init__(self, status: int, message: str):
+        super().__init__(f"{STATUS.get(status, status)}: {message}")
+        self.status = status
+
+
+class GraphInfo(C.Structure):
+    _fields_ = [("num_nodes", C.c_uint32), ("num_edges", C.c_uint64), ("num_partitions", C.c_uint32),
+                ("partition_bytes", C.c_uint64), ("max_nodes_in_partition", C.c_uint32),
+                ("max_edges_in_partition", C.c_uint64)]
+
+
+class EngineCfg(C.Structure):
+    _fields_ = [("device", C.c_int), ("num_device_partitions", C.c_uint32),
+                ("num_device_walkers", C.c_uint64), ("sched", C.c_int), ("pipeline", C.c_int),
+                ("zerocopy_threshold", C.c_uint64), ("seed", C.c_uint64), ("block_size", C.c_int),
+                ("ctas_per_sm", C.c_int)]
+
+
+class Stats(C.Structure):
+    _fields_ = [("updates", C.c_uint64), ("moves", C.c_uint64), ("teleports", C.c_uint64),
+                ("iterations", C.c_uint64), ("explicit_iterations", C.c_uint64),
+                ("h2d_graph_bytes", C.c_uint64), ("h2d_walker_bytes", C.c_uint64),
+                ("d2h_walker_bytes", C.c_uint64), ("zerocopy_bytes", C.c_uint64),
+                ("partition_loads", C.c_uint64), ("kernel_launches", C.c_uint64),
+                ("running_ms", C.c_double), ("graph_loading_ms", C.c_double),
+                ("computing_ms", C.c_double), ("zerocopy_ms", C.c_double),
+                ("walker_loading_ms", C.c_double), ("walker_evicting_ms", C.c_double),
+                ("graph_loading_calls", C.c_uint64), ("computing_calls", C.c_uint64),
+                ("zerocopy_calls", C.c_uint64), ("walker_loading_calls", C.c_uint64),
+                ("walker_evicting_calls", C.c_uint64), ("step_kernel_ms", C.c_double)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+def _load():
+    if not os.path.exists(LIB_PATH):
+        raise ImportError(f"{LIB_PATH} is missing: run `python -m lighttraffic_gb300.build` "
+                          "(the engine has no fallback implementation)")
+    L = C.CDLL(LIB_PATH)
+    vp, u64p, u32p = C.c_void_p, C.POINTER(C.c_uint64), C.POINTER(C.c_uint32)
+    sig = {
+        "lt_strerror": ([C.c_int], C.c_char_p),
+        "lt_last_error": ([], C.c_char_p),
+        "lt_version": ([], C.c_char_p),
+        "lt_graph_open": ([C.c_char_p, C.c_int, C.c_uint64, C.POINTER(vp)], C.c_int),
+        "lt_graph_from_csr": ([C.c_uint32, C.c_uint64, u64p, u32p, C.c_uint64, C.POINTER(vp)], C.c_int),
+        "lt_graph_generate_rmat": ([C.c_int, C.c_uint32, C.c_uint64, C.c_double, C.c_double, C.c_double,
+                                    C.c_double, C.c_uint64, C.c_uint64, C.POINTER(vp)], C.c_int),
+        "lt_graph_info_get": ([vp, C.POINTER(GraphInfo)], C.c_int),
+        "lt_graph_partitions": ([vp, u32p, u64p], C.c_int),
+        "lt_graph_csr": ([vp, C.POINTER(u64p), C.POINTER(u32p)], C.c_int),
+        "lt_graph_write_bcsr": ([vp, C.c_char_p], C.c_int),
+        "lt_graph_write_part": ([vp, C.c_char_p], C.c_int),
+        "lt_graph_close": ([vp], None),
+        "lt_partition_equal_size": ([u64p, C.c_uint32, C.c_uint64, u32p, u64p, C.c_uint32, u32p], C.c_int),
+        "lt_engine_cfg_default": ([C.POINTER(EngineCfg)], None),
+        "lt_engine_create": ([vp, C.POINTER(EngineCfg), C.POINTER(vp)], C.c_int),
+        "lt_engine_destroy": ([vp], None),
+        "lt_engine_drop_cache": ([vp], C.c_int),
+        "lt_run_ppr": ([vp, C.c_uint32, C.c_uint64, C.c_float, u64p], C.c_int),
+        "lt_run_pagerank": ([vp, C.c_uint64, C.c_uint32, C.c_uint32, C.c_float, C.c_int, u64p], C.c_int),
+        "lt_run_walk": ([vp, C.c_uint64, C.c_uint32, C.c_uint32, C.c_int, u32p, u32p], C.c_int),
+        "lt_engine_stats": ([vp, C.POINTER(Stats)], C.c_int),
+        "lt_walk_scratch_bytes": ([], C.c_size_t),
+        "lt_walk_device": ([C.c_int, C.c_int, vp, vp, C.c_uint32, C.c_uint32, C.c_uint64, C.c_uint32,
+                            C.c_float, C.c_uint32, C.c_uint64, vp, vp, vp, vp, vp, vp], C.c_int),
+    }
+    for name, (args, res) in sig.items():
+        f = getattr(L, name)
+        f.argtypes = args
+        f.restype = res
+    return L
+
+
+lib = _load()
+
+
+def check(status: int):
+    if status != 0:
+        raise LTError(status, lib.lt_last_error().decode(errors="replace"))
+
+
+def _ptr(a, ctype):
+    return None if a is None else a.ctypes.data_as(C.POINTER(ctype))
+
+
+def partition_equal_size(rowptr, max_bytes: int):
+    """EqualSizeStrategy::init (src/partition/PartitionStrategy.h:193-218) on caller arrays."""
+    rowptr = np.ascontiguousarray(rowptr, dtype=np.uint64)
+    V = len(rowptr) - 1
+    cap = V + 2
+    no = np.zeros(cap, dtype=np.uint32)
+    eo = np.zeros(cap, dtype=np.uint64)
+    P = C.c_uint32(0)
+    check(lib.lt_partition_equal_size(_ptr(rowptr, C.c_uint64), V, max_bytes, _ptr(no, C.c_uint32),
+                                      _ptr(eo, C.c_uint64), cap, C.byref(P)))
+    return no[: P.value + 1].copy(), eo[: P.value + 1].copy()
+
+
+class Graph:
+    """A bcsr graph in pinned host memory with its partition table."""
+
+    def __init__(self, handle):
+        self._h = C.c_void_p(handle) if not isinstance(handle, C.c_void_p) else handle
+        info = GraphInfo()
+        check(lib.lt_graph_info_get(self._h, C.byref(info)))
+        self.info = info
+
+    @classmethod
+    def open(cls, path: str, materialize: bool = False, part_mb: int = 32) -> "Graph":
+        h = C.c_void_p()
+        check(lib.lt_graph_open(path.encode(), int(materialize), part_mb, C.byref(h)))
+        return cls(h)
+
+    @classmethod
+    def from_csr(cls, rowptr, col, part_bytes: int) -> "Graph":
+        rowptr = np.ascontiguousarray(rowptr, dtype=np.uint64)
+        col = np.ascontiguousarray(col, dtype=np.uint32)
+        h = C.c_void_p()
+        check(lib.lt_graph_from_csr(len(rowptr) - 1, len(col), _ptr(rowptr, C.c_uint64),
+                                    _ptr(col, C.c_uint32), part_bytes, C.byref(h)))
+        return cls(h)
+
+    @classmethod
+    def rmat(cls, scale: int, edges: int, seed: int = 1, part_bytes: int = 32 << 20,
+             a=0.57, b=0.19, c=0.19, d=0.05, device: int = 0) -> "Graph":
+        h = C.c_void_p()
+        check(lib.lt_graph_generate_rmat(device, scale, edges, a, b, c, d, seed, part_bytes,
+                                         C.byref(h)))
+        return cls(h)
+
+    @property
+    def num_nodes(self) -> int:
+        return self.info.num_nodes
+
+    @property
+    def num_edges(self) -> int:
+        return self.info.num_edges
+
+    @property
+    def num_partitions(self) -> int:
+        return self.info.num_partitions
+
+    def partitions(self):
+        P = self.info.num_partitions
+        no = np.zeros(P + 1, dtype=np.uint32)
+        eo = np.zeros(P + 1, dtype=np.uint64)
+        check(lib.lt_graph_partitions(self._h, _ptr(no, C.c_uint32), _ptr(eo, C.c_uint64)))
+        return no, eo
+
+    def csr(self):
+        """Copies of (rowptr, col)."""
+        rp, cl = C.POINTER(C.c_uint64)(), C.POINTER(C.c_uint32)()
+        check(lib.lt_graph_csr(self._h, C.byref(rp), C.byref(cl)))
+        V, E = self.num_nodes, self.num_edges
+        rowptr = np.ctypeslib.as_array(rp, shape=(V + 1,)).copy()
+        col = np.ctypeslib.as_array(cl, shape=(E,)).copy() if E else np.zeros(0, np.uint32)
+        return rowptr, col
+
+    def write_bcsr(self, path: str):
+        check(lib.lt_graph_write_bcsr(self._h, path.encode()))
+
+    def write_part(self, bcsr_path: str):
+        check(lib.lt_graph_write_part(self._h, bcsr_path.encode()))
+
+    def close(self):
+        if self._h:
+            lib.lt_graph_close(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Engine:
+    """One engine = the reference's LightTraffic<AppManager,App,Walker> object."""
+
+    def __init__(self, graph: Graph, partitions: int = 0, batch: int = 0, seed: int = 0x5EED5EED,
+                 sched: int = SCHED_PLAIN, pipeline: bool = True, zerocopy_threshold=None,
+                 device: int = 0, ctas_per_sm: int = 0):
+        cfg = EngineCfg()
+        lib.lt_engine_cfg_default(C.byref(cfg))
+        cfg.device = device
+        cfg.num_device_partitions = partitions
+        cfg.num_device_walkers = batch
+        cfg.seed = seed
+        cfg.sched = sched
+        cfg.pipeline = int(pipeline)
+        if zerocopy_threshold is not None:
+            cfg.zerocopy_threshold = zerocopy_threshold
+        cfg.ctas_per_sm = ctas_per_sm
+        self.graph = graph
+        self._h = C.c_void_p()
+        check(lib.lt_engine_create(graph._h, C.byref(cfg), C.byref(self._h)))
+
+    def ppr(self, source: int, walkers: int, prob: float = 0.15, out=None):
+        V = self.graph.num_nodes
+        counts = out if out is not None else np.zeros(V, dtype=np.uint64)
+        check(lib.lt_run_ppr(self._h, source, walkers, prob, _ptr(counts, C.c_uint64)))
+        return counts
+
+    def pagerank(self, walkers: int, length: int = 10, runs: int = 1, alpha: float = 0.85,
+                 start: int = START_UNIFORM, out=None):
+        V = self.graph.num_nodes
+        counts = out if out is not None else np.zeros(V, dtype=np.uint64)
+        check(lib.lt_run_pagerank(self._h, walkers, length, runs, alpha, start,
+                                  _ptr(counts, C.c_uint64)))
+        return counts
+
+    def walk(self, walkers: int, length: int = 10, run: int = 0, start: int = START_UNIFORM,
+             paths: bool = False):
+        ep = np.zeros(walkers, dtype=np.uint32)
+        pa = np.zeros(walkers * (length + 1), dtype=np.uint32) if paths else None
+        check(lib.lt_run_walk(self._h, walkers, length, run, start, _ptr(ep, C.c_uint32),
+                              _ptr(pa, C.c_uint32)))
+        return ep, pa
+
+    def drop_cache(self):
+        check(lib.lt_engine_drop_cache(self._h))
+
+    def stats(self) -> dict:
+        s = Stats()
+        check(lib.lt_engine_stats(self._h, C.byref(s)))
+        return s.as_dict()
+
+    def close(self):
+        if self._h:
+            lib.lt_engine_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -1,0 +1,247 @@
+// capi.cpp -- extern "C" entry points declared in include/lighttraffic.h.
+#include <cstring>
+#include <new>
+
+#include "engine.h"
+
+using namespace lt;
+
+extern "C" {
+
+const char *lt_strerror(lt_status s)
+{
+    switch (s) {
+    case LT_OK: return "ok";
+    case LT_ERR_INVALID: return "invalid argument";
+    case LT_ERR_IO: return "i/o error";
+    case LT_ERR_FORMAT: return "malformed file";
+    case LT_ERR_NOMEM: return "out of memory";
+    case LT_ERR_CUDA: return "CUDA error";
+    case LT_ERR_PARTITION: return "vertex does not fit the partition size";
+    case LT_ERR_TIMEOUT: return "bounded device wait expired";
+    case LT_ERR_CAPACITY: return "capacity exceeded";
+    case LT_ERR_UNSUPPORTED: return "unsupported configuration";
+    }
+    return "unknown status";
+}
+
+const char *lt_last_error(void) { return last_error(); }
+const char *lt_version(void) { return "lighttraffic-gb300 0.1 (sm_103a)"; }
+
+lt_status lt_partition_equal_size(const uint64_t *rowptr, uint32_t num_nodes, uint64_t max_bytes, uint32_t *node_off,
+                                  uint64_t *edge_off, uint32_t cap, uint32_t *num_parts)
+{
+    if (!rowptr || !node_off || !edge_off || !num_parts) return fail(LT_ERR_INVALID, "null argument");
+    std::vector<uint32_t> no;
+    std::vector<uint64_t> eo;
+    LT_TRY(partition_equal_size(rowptr, num_nodes, max_bytes, no, eo));
+    if (no.size() > cap) return fail(LT_ERR_CAPACITY, "%zu partitions exceed the output capacity %u", no.size() - 1, cap);
+    std::memcpy(node_off, no.data(), 4 * no.size());
+    std::memcpy(edge_off, eo.data(), 8 * eo.size());
+    *num_parts = (uint32_t)no.size() - 1;
+    return LT_OK;
+}
+
+lt_status lt_graph_open(const char *bcsr_path, int materialize, uint64_t part_mb, lt_graph **out)
+{
+    if (!bcsr_path || !out) return fail(LT_ERR_INVALID, "null argument");
+    lt_graph *g = new (std::nothrow) lt_graph();
+    if (!g) return fail(LT_ERR_NOMEM, "graph allocation failed");
+    lt_status s = read_bcsr(bcsr_path, *g);
+    if (s == LT_OK) {
+        if (materialize) {
+            g->part_bytes = part_mb * 1024ull * 1024ull;
+            s = partition_equal_size(g->rowptr(), g->V, g->part_bytes, g->node_off, g->edge_off);
+            if (s == LT_OK) s = finish_partitions(*g);
+            if (s == LT_OK) s = write_part(*g, bcsr_path);
+        } else {
+            s = read_part(bcsr_path, *g);
+            if (s == LT_OK && g->node_off.back() != g->V)
+                s = fail(LT_ERR_FORMAT, "partition file does not match the graph");
+        }
+    }
+    if (s != LT_OK) {
+        graph_free(*g);
+        delete g;
+        return s;
+    }
+    *out = g;
+    return LT_OK;
+}
+
+lt_status lt_graph_from_csr(uint32_t num_nodes, uint64_t num_edges, const uint64_t *rowptr, const uint32_t *col,
+                            uint64_t part_bytes, lt_graph **out)
+{
+    if (!rowptr || (!col && num_edges) || !out || num_nodes == 0) return fail(LT_ERR_INVALID, "null or empty argument");
+    if (rowptr[0] != 0 || rowptr[num_nodes] != num_edges) return fail(LT_ERR_FORMAT, "rowptr does not span [0, E]");
+    lt_graph *g = new (std::nothrow) lt_graph();
+    if (!g) return fail(LT_ERR_NOMEM, "graph allocation failed");
+    g->V = num_nodes;
+    g->E = num_edges;
+    lt_status s = host_alloc(g->rowptr_buf, 8ull * ((uint64_t)num_nodes + 1), true);
+    if (s == LT_OK) s = host_alloc(g->col_buf, 4ull * num_edges, true);
+    if (s == LT_OK) {
+        std::memcpy(g->rowptr_mut(), rowptr, 8ull * ((uint64_t)num_nodes + 1));
+        if (num_edges) std::memcpy(g->col_mut(), col, 4ull * num_edges);
+        for (uint64_t v = 0; v < num_nodes && s == LT_OK; v++)
+            if (rowptr[v + 1] < rowptr[v]) s = fail(LT_ERR_FORMAT, "rowptr decreases at %llu", (unsigned long long)v);
+        for (uint64_t k = 0; k < num_edges && s == LT_OK; k++)
+            if (col[k] >= num_nodes) s = fail(LT_ERR_FORMAT, "col[%llu] out of range", (unsigned long long)k);
+    }
+    if (s == LT_OK) {
+        g->part_bytes = part_bytes;
+        s = partition_equal_size(g->rowptr(), g->V, part_bytes, g->node_off, g->edge_off);
+    }
+    if (s == LT_OK) s = finish_partitions(*g);
+    if (s != LT_OK) {
+        graph_free(*g);
+        delete g;
+        return s;
+    }
+    *out = g;
+    return LT_OK;
+}
+
+lt_status lt_graph_generate_rmat(int device, uint32_t scale, uint64_t num_edges, double a, double b, double c, double d,
+                                 uint64_t seed, uint64_t part_bytes, lt_graph **out)
+{
+    if (!out) return fail(LT_ERR_INVALID, "null output");
+    lt_graph *g = new (std::nothrow) lt_graph();
+    if (!g) return fail(LT_ERR_NOMEM, "graph allocation failed");
+    lt_status s = generate_rmat(device, scale, num_edges, a, b, c, d, seed, *g);
+    if (s == LT_OK) {
+        g->part_bytes = part_bytes;
+        s = partition_equal_size(g->rowptr(), g->V, part_bytes, g->node_off, g->edge_off);
+    }
+    if (s == LT_OK) s = finish_partitions(*g);
+    if (s != LT_OK) {
+        graph_free(*g);
+        delete g;
+        return s;
+    }
+    *out = g;
+    return LT_OK;
+}
+
+lt_status lt_graph_info_get(const lt_graph *g, lt_graph_info *out)
+{
+    if (!g || !out) return fail(LT_ERR_INVALID, "null argument");
+    out->num_nodes = g->V;
+    out->num_edges = g->E;
+    out->num_partitions = g->P();
+    out->partition_bytes = g->part_bytes;
+    out->max_nodes_in_partition = g->max_nodes;
+    out->max_edges_in_partition = g->max_edges;
+    return LT_OK;
+}
+
+lt_status lt_graph_partitions(const lt_graph *g, uint32_t *node_off, uint64_t *edge_off)
+{
+    if (!g) return fail(LT_ERR_INVALID, "null graph");
+    if (node_off) std::memcpy(node_off, g->node_off.data(), 4 * g->node_off.size());
+    if (edge_off) std::memcpy(edge_off, g->edge_off.data(), 8 * g->edge_off.size());
+    return LT_OK;
+}
+
+lt_status lt_graph_csr(const lt_graph *g, const uint64_t **rowptr, const uint32_t **col)
+{
+    if (!g) return fail(LT_ERR_INVALID, "null graph");
+    if (rowptr) *rowptr = g->rowptr();
+    if (col) *col = g->col();
+    return LT_OK;
+}
+
+lt_status lt_graph_write_bcsr(const lt_graph *g, const char *path)
+{
+    if (!g || !path) return fail(LT_ERR_INVALID, "null argument");
+    return write_bcsr(*g, path);
+}
+
+lt_status lt_graph_write_part(const lt_graph *g, const char *bcsr_path)
+{
+    if (!g || !bcsr_path) return fail(LT_ERR_INVALID, "null argument");
+    return write_part(*g, bcsr_path);
+}
+
+void lt_graph_close(lt_graph *g)
+{
+    if (!g) return;
+    graph_free(*g);
+    delete g;
+}
+
+void lt_engine_cfg_default(lt_engine_cfg *cfg)
+{
+    if (!cfg) return;
+    std::memset(cfg, 0, sizeof *cfg);
+    cfg->device = 0;
+    cfg->num_device_partitions = 0;
+    cfg->num_device_walkers = 0;
+    cfg->sched = LT_SCHED_PLAIN;
+    cfg->pipeline = 1;
+    cfg->zerocopy_threshold = UINT64_MAX;
+    cfg->seed = 0x5EED5EEDull;
+    cfg->block_size = 0;
+    cfg->ctas_per_sm = 0;
+}
+
+lt_status lt_engine_create(lt_graph *g, const lt_engine_cfg *cfg, lt_engine **out)
+{
+    lt_engine_cfg c;
+    lt_engine_cfg_default(&c);
+    if (cfg) c = *cfg;
+    return engine_create(g, c, out);
+}
+
+void lt_engine_destroy(lt_engine *e) { engine_destroy(e); }
+
+lt_status lt_engine_drop_cache(lt_engine *e)
+{
+    if (!e) return fail(LT_ERR_INVALID, "null engine");
+    return engine_drop_cache(e);
+}
+
+lt_status lt_run_ppr(lt_engine *e, uint32_t source, uint64_t num_walkers, float prob, uint64_t *counts_out)
+{
+    if (!e) return fail(LT_ERR_INVALID, "null engine");
+    if (!(prob > 0.0f && prob <= 1.0f)) return fail(LT_ERR_INVALID, "PPR stop probability must be in (0, 1]");
+    return engine_run(e, LT_APP_PPR, LT_START_SOURCE, source, num_walkers, 0, 1, 0, prob, counts_out, nullptr, nullptr);
+}
+
+lt_status lt_run_pagerank(lt_engine *e, uint64_t num_walkers, uint32_t length, uint32_t runs, float alpha,
+                          int start_mode, uint64_t *counts_out)
+{
+    if (!e) return fail(LT_ERR_INVALID, "null engine");
+    if (length == 0) return fail(LT_ERR_INVALID, "walk length must be positive");
+    if (start_mode == LT_START_SOURCE) return fail(LT_ERR_INVALID, "PageRank walkers start uniformly or per vertex");
+    return engine_run(e, LT_APP_PAGERANK, start_mode, 0, num_walkers, length, runs, 0, alpha, counts_out, nullptr, nullptr);
+}
+
+lt_status lt_run_walk(lt_engine *e, uint64_t num_walkers, uint32_t length, uint32_t run, int start_mode,
+                      uint32_t *endpoints_out, uint32_t *paths_out)
+{
+    if (!e) return fail(LT_ERR_INVALID, "null engine");
+    if (length == 0) return fail(LT_ERR_INVALID, "walk length must be positive");
+    if (start_mode == LT_START_SOURCE) return fail(LT_ERR_INVALID, "generic walkers start uniformly or per vertex");
+    return engine_run(e, LT_APP_WALK, start_mode, 0, num_walkers, length, 1, run, 0.0f, nullptr, endpoints_out, paths_out);
+}
+
+lt_status lt_engine_stats(const lt_engine *e, lt_stats *out)
+{
+    if (!e || !out) return fail(LT_ERR_INVALID, "null argument");
+    *out = e->stats;
+    return LT_OK;
+}
+
+size_t lt_walk_scratch_bytes(void) { return walk_scratch_bytes(); }
+
+lt_status lt_walk_device(int app, int start_mode, const uint64_t *d_rowptr, const uint32_t *d_col, uint32_t num_nodes,
+                         uint32_t source, uint64_t num_walkers, uint32_t length, float prob, uint32_t run,
+                         uint64_t seed, uint64_t *d_counts, uint32_t *d_endpoints, uint32_t *d_paths,
+                         void *d_scratch, uint64_t *d_stats, void *stream)
+{
+    return walk_device(app, start_mode, d_rowptr, d_col, num_nodes, source, num_walkers, length, prob, run, seed,
+                       d_counts, d_endpoints, d_paths, d_scratch, d_stats, (cudaStream_t)stream, 0);
+}
+
+}  // extern "C"

@@ -1,0 +1,212 @@
+// walk_whole.cu -- persistent step kernel for a graph resident in HBM.
+//
+// Replaces randomWalkKernel / randomWalkInsidePool[AllBatch]
+// (src/WalkManager.h:229-274) for the case where every partition is cached on
+// the device: walkers never need re-bucketing, so each one is stepped from
+// creation to termination without leaving the SM.
+//
+// Design (GB300-first):
+//  * Persistent grid: SMs x resident CTAs; each lane owns one walker at a time.
+//  * Lazy walker creation: walker i is created from its index alone (start
+//    vertex and, for PPR, its geometric length are pure functions of
+//    (seed, run, i)), so no walker array is ever materialised.  A lane whose
+//    walker ends takes the next index from a warp-aggregated atomic counter
+//    (one atomic per warp refill), keeping every lane busy despite the
+//    geometric length spread of PPR walks.
+//  * Graph reads: rowptr[cur], rowptr[cur+1] (16 B) and col[e] (4 B) through
+//    the read-only path; counters are u64 atomics resolved in L2.
+#include "lt_core.cuh"
+#include "walk_whole.h"
+
+namespace lt {
+
+namespace {
+
+constexpr unsigned kFull = 0xFFFFFFFFu;
+
+__device__ __forceinline__ uint64_t ldg_u64(const uint64_t *p) { return __ldg((const unsigned long long *)p); }
+__device__ __forceinline__ uint32_t ldg_u32(const uint32_t *p) { return __ldg(p); }
+
+template <int APP, int START>
+__global__ void __launch_bounds__(kWholeBlock) walk_whole_kernel(WholeArgs a)
+{
+    const int lane = threadIdx.x & 31;
+    const unsigned lt_mask = (1u << lane) - 1u;
+
+    uint32_t cur = 0, step = 0;
+    uint64_t idx = 0;
+    bool active = false;
+    bool exhausted = false;
+    uint32_t hop = 0;  // hops taken (walk app path position)
+    uint64_t n_upd = 0, n_mov = 0, n_tel = 0;
+
+    while (true) {
+        const unsigned idle = __ballot_sync(kFull, !active);
+        if (idle != 0u && !exhausted) {
+            const int leader = __ffs(idle) - 1;
+            unsigned long long base = 0;
+            if (lane == leader) base = atomicAdd((unsigned long long *)a.next, (unsigned long long)__popc(idle));
+            base = __shfl_sync(kFull, base, leader);
+            if (base + __popc(idle) >= a.W) exhausted = true;
+            if (!active) {
+                const uint64_t my = base + __popc(idle & lt_mask);
+                if (my < a.W) {
+                    idx = my;
+                    cur = start_vertex(START, a.source, a.V, a.seed, a.run, idx);
+                    if (APP == kPPR) {
+                        step = ppr_length(a.seed, a.run, idx, a.thr);
+                    } else {
+                        step = a.length;
+                    }
+                    hop = 0;
+                    if (APP == kWalk && a.paths) a.paths[idx * (uint64_t)(a.length + 1)] = cur;
+                    active = true;
+                }
+            }
+        }
+        if (__ballot_sync(kFull, active) == 0u) {
+            if (exhausted) break;
+            continue;
+        }
+        if (!active) continue;
+
+        const uint32_t s = step;
+        n_upd++;
+        if (APP == kPPR) {
+            // app/ppr.cu:22-42
+            if (s == 1) {
+                atomicAdd((unsigned long long *)&a.counts[cur], 1ull);
+                active = false;
+            } else {
+                step = s - 1;
+                const uint64_t first = ldg_u64(a.rowptr + cur);
+                const uint64_t deg = ldg_u64(a.rowptr + cur + 1) - first;
+                if (deg > 0) {
+                    const Rand4 r = walk_draw(a.seed, s, kTagStep, a.run, idx);
+                    cur = ldg_u32(a.col + first + mod_u64(r64_of(r), deg));
+                    n_mov++;
+                } else {
+                    atomicAdd((unsigned long long *)&a.counts[cur], 1ull);
+                    active = false;
+                }
+            }
+        } else if (APP == kPageRank) {
+            // app/pagerank.cu:26-44; a vertex without out-edges teleports.
+            atomicAdd((unsigned long long *)&a.counts[cur], 1ull);
+            if (s == 1) {
+                active = false;
+            } else {
+                step = s - 1;
+                const Rand4 r = walk_draw(a.seed, s, kTagStep, a.run, idx);
+                const uint64_t r64 = r64_of(r);
+                bool tele = m53_of(r) >= a.thr;
+                if (!tele) {
+                    const uint64_t first = ldg_u64(a.rowptr + cur);
+                    const uint64_t deg = ldg_u64(a.rowptr + cur + 1) - first;
+                    if (deg > 0) {
+                        cur = ldg_u32(a.col + first + mod_u64(r64, deg));
+                        n_mov++;
+                    } else {
+                        tele = true;
+                    }
+                }
+                if (tele) {
+                    cur = (uint32_t)mod_u64(r64, a.V);
+                    n_tel++;
+                }
+            }
+        } else {
+            // app/genericwalk.cu:22-32
+            const uint64_t first = ldg_u64(a.rowptr + cur);
+            const uint64_t deg = ldg_u64(a.rowptr + cur + 1) - first;
+            uint32_t *path = a.paths ? a.paths + idx * (uint64_t)(a.length + 1) : nullptr;
+            if (deg > 0) {
+                const Rand4 r = walk_draw(a.seed, s, kTagStep, a.run, idx);
+                cur = ldg_u32(a.col + first + mod_u64(r64_of(r), deg));
+                n_mov++;
+                hop++;
+                if (path) path[hop] = cur;
+                step = s - 1;
+            } else {
+                if (path) {
+                    for (uint32_t h = hop + 1; h <= a.length; h++) path[h] = kInvalidNode;
+                }
+                step = 0;
+            }
+            if (step == 0) active = false;
+        }
+        if (!active && a.endpoints) a.endpoints[idx] = cur;
+    }
+
+    // Warp-reduce the statistics, one atomic per warp.
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        n_upd += __shfl_down_sync(kFull, n_upd, o);
+        n_mov += __shfl_down_sync(kFull, n_mov, o);
+        n_tel += __shfl_down_sync(kFull, n_tel, o);
+    }
+    if (lane == 0 && a.stats) {
+        atomicAdd((unsigned long long *)&a.stats[0], (unsigned long long)n_upd);
+        atomicAdd((unsigned long long *)&a.stats[1], (unsigned long long)n_mov);
+        atomicAdd((unsigned long long *)&a.stats[2], (unsigned long long)n_tel);
+    }
+}
+
+template <int APP, int START>
+cudaError_t launch_t(const WholeArgs &a, int grid, cudaStream_t st)
+{
+    walk_whole_kernel<APP, START><<<grid, kWholeBlock, 0, st>>>(a);
+    return cudaGetLastError();
+}
+
+template <int APP>
+cudaError_t launch_app(const WholeArgs &a, int start, int grid, cudaStream_t st)
+{
+    switch (start) {
+    case kStartSource: return launch_t<APP, kStartSource>(a, grid, st);
+    case kStartUniform: return launch_t<APP, kStartUniform>(a, grid, st);
+    default: return launch_t<APP, kStartPerVertex>(a, grid, st);
+    }
+}
+
+template <int APP, int START>
+int occupancy_t()
+{
+    int n = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, walk_whole_kernel<APP, START>, kWholeBlock, 0);
+    return n;
+}
+
+}  // namespace
+
+int whole_grid(int app, int start, int device, int ctas_per_sm)
+{
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+    int occ = 0;
+    switch (app * 3 + start) {
+    case 0: occ = occupancy_t<kPPR, kStartSource>(); break;
+    case 1: occ = occupancy_t<kPPR, kStartUniform>(); break;
+    case 2: occ = occupancy_t<kPPR, kStartPerVertex>(); break;
+    case 3: occ = occupancy_t<kPageRank, kStartSource>(); break;
+    case 4: occ = occupancy_t<kPageRank, kStartUniform>(); break;
+    case 5: occ = occupancy_t<kPageRank, kStartPerVertex>(); break;
+    case 6: occ = occupancy_t<kWalk, kStartSource>(); break;
+    case 7: occ = occupancy_t<kWalk, kStartUniform>(); break;
+    default: occ = occupancy_t<kWalk, kStartPerVertex>(); break;
+    }
+    if (occ < 1) occ = 1;
+    if (ctas_per_sm > 0 && ctas_per_sm < occ) occ = ctas_per_sm;
+    return sms * occ;
+}
+
+cudaError_t launch_walk_whole(const WholeArgs &a, int app, int start, int grid, cudaStream_t st)
+{
+    switch (app) {
+    case kPPR: return launch_app<kPPR>(a, start, grid, st);
+    case kPageRank: return launch_app<kPageRank>(a, start, grid, st);
+    default: return launch_app<kWalk>(a, start, grid, st);
+    }
+}
+
+}  // namespace lt

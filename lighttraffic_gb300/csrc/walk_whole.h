@@ -1,0 +1,32 @@
+// walk_whole.h -- launcher of the resident-graph step kernel.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace lt {
+
+constexpr int kWholeBlock = 256;
+
+struct WholeArgs {
+    const uint64_t *rowptr;  // u64[V+1], global edge offsets
+    const uint32_t *col;     // u32[E]
+    uint32_t V;
+    uint32_t source;
+    uint64_t W;              // walkers in this pass
+    uint32_t length;         // PageRank / walk length
+    uint32_t run;            // epoch index (random stream selector)
+    uint64_t seed;
+    uint64_t thr;            // floor(p 2^53): PPR stop prob or PageRank alpha
+    uint64_t *counts;        // u64[V] or null (walk app)
+    uint32_t *endpoints;     // u32[W] or null
+    uint32_t *paths;         // u32[W*(length+1)] or null (walk app)
+    uint64_t *next;          // scratch: next walker index (zeroed before launch)
+    uint64_t *stats;         // u64[3] or null: updates, moves, teleports
+};
+
+// Persistent grid size: SMs x resident CTAs (capped by ctas_per_sm when > 0).
+int whole_grid(int app, int start, int device, int ctas_per_sm);
+cudaError_t launch_walk_whole(const WholeArgs &a, int app, int start, int grid, cudaStream_t st);
+
+}  // namespace lt

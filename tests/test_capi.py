@@ -1,0 +1,57 @@
+"""The C-ABI library loads and exports every function include/*.h declares;
+host-side error paths work without a GPU."""
+import ctypes
+import glob
+import os
+import re
+import subprocess
+
+import numpy as np
+import pytest
+
+from conftest import ROOT, gpu_available
+
+
+def _declared():
+    names = set()
+    for h in glob.glob(os.path.join(ROOT, "include", "*.h")):
+        src = open(h).read()
+        src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+        for m in re.finditer(r"\b(lt_\w+)\s*\(", src):
+            names.add(m.group(1))
+    return sorted(names)
+
+
+def test_header_declares_entry_points():
+    names = _declared()
+    assert "lt_run_ppr" in names and "lt_walk_device" in names and len(names) >= 20
+
+
+@pytest.mark.parametrize("name", _declared())
+def test_symbol_exported(lt, name):
+    lib = ctypes.CDLL(lt.LIB_PATH)
+    assert hasattr(lib, name), f"{name} declared in include/ but not exported"
+
+
+def test_strerror_and_version(lt):
+    assert lt.lib.lt_strerror(0) == b"ok"
+    assert b"sm_103a" in lt.lib.lt_version()
+
+
+def test_engine_without_gpu_fails_loudly(lt):
+    if gpu_available():
+        pytest.skip("a GPU is visible")
+    rp = np.array([0, 1, 2], np.uint64)
+    col = np.array([1, 0], np.uint32)
+    g = lt.Graph.from_csr(rp, col, 1 << 20)
+    with pytest.raises(lt.LTError) as ei:
+        lt.Engine(g)
+    assert ei.value.status == 5                      # LT_ERR_CUDA, no silent fallback
+
+
+def test_cli_requires_file(lt):
+    exe = os.path.join(lt.BIN_DIR, "ppr")
+    r = subprocess.run([exe], capture_output=True, text=True)
+    assert r.returncode == 2 and "-f option must be given" in r.stderr
+    r = subprocess.run([exe, "-f", "/nonexistent.bcsr", "-m"], capture_output=True, text=True)
+    assert r.returncode == 1 and "cannot open" in r.stderr

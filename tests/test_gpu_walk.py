@@ -1,0 +1,163 @@
+"""GPU parity: the CUDA step kernels against the CPU oracle, bit-exact.
+
+Every comparison is on the same seeded inputs; the RNG is keyed by walker and
+step, so visit counts, endpoints and paths must match exactly -- across
+graphs, apps, start modes, runs and launch shapes.
+"""
+import os
+
+import numpy as np
+import pytest
+
+import oracle
+from conftest import GOLDEN
+
+pytestmark = pytest.mark.gpu
+
+
+def _golden(name):
+    return oracle.read_bcsr(os.path.join(GOLDEN, "graphs", f"{name}.bcsr"))
+
+
+SMALL = ["path4", "hub10", "gaps8", "rmat10", "rmat12"]
+
+
+@pytest.fixture(scope="module")
+def rmat16():
+    return oracle.rmat(16, 1 << 20, seed=21)
+
+
+def _engine(lt, rp, col, **kw):
+    g = lt.Graph.from_csr(rp, col, 1 << 30)
+    return g, lt.Engine(g, **kw)
+
+
+@pytest.mark.parametrize("name", SMALL)
+@pytest.mark.parametrize("seed", [1, 0xDEADBEEF12345])
+def test_ppr_small(lt, require_gpu, name, seed):
+    rp, col = _golden(name)
+    g, e = _engine(lt, rp, col, seed=seed)
+    for prob in (0.15, 0.5, 1.0):
+        want, _, st = oracle.ppr(rp, col, 0, 7777, prob=prob, seed=seed)
+        got = e.ppr(0, 7777, prob)
+        assert (got == want).all(), (name, prob)
+        s = e.stats()
+        assert s["moves"] == st[1]
+
+
+@pytest.mark.parametrize("name", SMALL)
+@pytest.mark.parametrize("start", [1, 2])
+def test_pagerank_small(lt, require_gpu, name, start):
+    rp, col = _golden(name)
+    V = len(rp) - 1
+    g, e = _engine(lt, rp, col, seed=77)
+    want, st = oracle.pagerank(rp, col, 3 * V + 5, length=9, runs=3, seed=77, start_mode=start)
+    got = e.pagerank(3 * V + 5, length=9, runs=3, start=start)
+    assert (got == want).all()
+    s = e.stats()
+    assert (s["updates"], s["moves"], s["teleports"]) == tuple(int(x) for x in st)
+
+
+@pytest.mark.parametrize("name", SMALL)
+@pytest.mark.parametrize("start", [1, 2])
+def test_walk_small(lt, require_gpu, name, start):
+    rp, col = _golden(name)
+    V = len(rp) - 1
+    g, e = _engine(lt, rp, col, seed=5)
+    for run in (0, 3):
+        ep, pa, _ = oracle.generic_walk(rp, col, 4 * V + 3, length=7, start_mode=start, run=run, seed=5,
+                                        paths=True)
+        gep, gpa = e.walk(4 * V + 3, length=7, run=run, start=start, paths=True)
+        assert (gep == ep).all() and (gpa == pa).all()
+
+
+def test_launch_shape_does_not_change_results(lt, require_gpu, rmat16):
+    rp, col = rmat16
+    V = len(rp) - 1
+    ref = None
+    for ctas in (1, 2, 0):
+        g, e = _engine(lt, rp, col, seed=3, ctas_per_sm=ctas)
+        c = e.pagerank(2 * V, length=10, start=2)
+        p = e.ppr(5, 100000, 0.15)
+        if ref is None:
+            ref = (c, p)
+        assert (c == ref[0]).all() and (p == ref[1]).all()
+    want, _ = oracle.pagerank(rp, col, 2 * V, length=10, seed=3, start_mode=2)
+    assert (ref[0] == want).all()
+    wp, _, _ = oracle.ppr(rp, col, 5, 100000, prob=0.15, seed=3)
+    assert (ref[1] == wp).all()
+
+
+def test_ppr_sources_and_zero_walkers(lt, require_gpu, rmat16):
+    rp, col = rmat16
+    V = len(rp) - 1
+    g, e = _engine(lt, rp, col, seed=8)
+    for src in (0, 1, V // 2, V - 1):
+        want, _, _ = oracle.ppr(rp, col, src, 20000, prob=0.2, seed=8)
+        assert (e.ppr(src, 20000, 0.2) == want).all()
+    assert e.ppr(0, 0, 0.15).sum() == 0
+    with pytest.raises(lt.LTError):
+        e.ppr(V, 10, 0.15)                  # source out of range
+    with pytest.raises(lt.LTError):
+        e.ppr(0, 10, 0.0)                   # would never terminate
+
+
+def test_gpu_rmat_matches_oracle(lt, require_gpu):
+    for scale, edges, seed in [(10, 1 << 13, 7), (12, 1 << 15, 3), (16, 1 << 20, 21)]:
+        g = lt.Graph.rmat(scale, edges, seed=seed, part_bytes=1 << 30)
+        rp, col = g.csr()
+        wr, wc = oracle.rmat(scale, edges, seed=seed)
+        assert (rp == wr).all() and (col == wc).all(), scale
+
+
+def test_c0_ppr_full_size(lt, require_gpu):
+    """c0: RMAT(2^20, 2^24), 32 MB partitions all cached, PPR from 0, W = 2V, p = 0.15."""
+    g = lt.Graph.rmat(20, 1 << 24, seed=1, part_bytes=32 << 20)
+    rp, col = g.csr()
+    V = g.num_nodes
+    assert g.num_partitions >= 3
+    e = lt.Engine(g, seed=1)
+    got = e.ppr(0, 2 * V, 0.15)
+    want, _, st = oracle.ppr(rp, col, 0, 2 * V, prob=0.15, seed=1)
+    assert (got == want).all()
+    assert got.sum() == 2 * V
+    assert e.stats()["moves"] == st[1]
+
+
+def test_c1_pagerank_and_walk_full_size(lt, require_gpu):
+    """c1: RMAT(2^23, 2^27), 2V walkers one per vertex, PageRank l=10 teleport 0.15,
+    generic walk l=10 -- bit-exact against the oracle."""
+    g = lt.Graph.rmat(23, 1 << 27, seed=1, part_bytes=32 << 20)
+    rp, col = g.csr()
+    V = g.num_nodes
+    assert g.num_partitions >= 18
+    e = lt.Engine(g, seed=1)
+    got = e.pagerank(2 * V, length=10, start=2)
+    assert got.sum() == 2 * V * 10
+    want, _ = oracle.pagerank(rp, col, 2 * V, length=10, seed=1, start_mode=2)
+    assert (got == want).all()
+    gep, _ = e.walk(2 * V, length=10, start=2)
+    wep, _, _ = oracle.generic_walk(rp, col, 2 * V, length=10, start_mode=2, seed=1)
+    assert (gep == wep).all()
+
+
+def test_device_entry_point(lt, require_gpu, rmat16):
+    """lt_walk_device on caller device buffers (torch allocations as plumbing)."""
+    import ctypes
+    import torch
+    rp, col = rmat16
+    V = len(rp) - 1
+    d_rp = torch.from_numpy(rp.view(np.int64)).cuda()
+    d_col = torch.from_numpy(col.view(np.int32)).cuda()
+    d_cnt = torch.zeros(V, dtype=torch.int64, device="cuda")
+    d_scr = torch.zeros(lt.lib.lt_walk_scratch_bytes() // 8, dtype=torch.int64, device="cuda")
+    d_st = torch.zeros(3, dtype=torch.int64, device="cuda")
+    stream = torch.cuda.current_stream()
+    for rep in range(2):
+        d_cnt.zero_()
+        lt.check(lt.lib.lt_walk_device(0, 0, d_rp.data_ptr(), d_col.data_ptr(), V, 3, 50000, 0,
+                                       ctypes.c_float(0.15), 0, 99, d_cnt.data_ptr(), None, None,
+                                       d_scr.data_ptr(), d_st.data_ptr(), stream.cuda_stream))
+        torch.cuda.synchronize()
+        want, _, _ = oracle.ppr(rp, col, 3, 50000, prob=0.15, seed=99)
+        assert (d_cnt.cpu().numpy().view(np.uint64) == want).all()
