@@ -71,7 +71,7 @@ class Stats(C.Structure):
 
 def _load():
     if not os.path.exists(LIB_PATH):
-        raise ImportError(f"{LIB_PATH} is missing: run `python -m lighttraffic_gb300.build` "
+        raise ImportError(f"{LIB_PATH} is missing: run `python lighttraffic_gb300/build.py` "
                           "(the engine has no fallback implementation)")
     L = C.CDLL(LIB_PATH)
     vp, u64p, u32p = C.c_void_p, C.POINTER(C.c_uint64), C.POINTER(C.c_uint32)

@@ -1,6 +1,6 @@
 """In-tree build of the native library and the CLI binaries.
 
-    python -m lighttraffic_gb300.build          # or lighttraffic_gb300.build.build()
+    python lighttraffic_gb300/build.py
 
 Produces
   lighttraffic_gb300/liblighttraffic.so   (C ABI of include/lighttraffic.h)
