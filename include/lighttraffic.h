@@ -206,6 +206,21 @@ lt_status lt_walk_device(int app, int start_mode, const uint64_t *d_rowptr, cons
                          uint64_t *d_counts, uint32_t *d_endpoints, uint32_t *d_paths,
                          void *d_scratch, uint64_t *d_stats, void *stream);
 
+/* lt_walk_device without the scratch argument, for callers that cannot
+ * allocate device memory (inside a stream capture, or when a host framework
+ * owns every device allocation and hands over only inputs and outputs).  No
+ * counterpart in the reference.  It allocates nothing: its scratch is a
+ * 256-byte static device array shared by every call in the process; the call
+ * clears it on `stream` first, calls that overlap on the GPU race (order them
+ * on one stream), and a scratch need above 256 bytes is rejected with
+ * LT_ERR_CAPACITY.  The first call on each device looks up the array's device
+ * address (cudaGetSymbolAddress); make it before any stream capture. */
+lt_status lt_walk_device_noalloc(int app, int start_mode, const uint64_t *d_rowptr, const uint32_t *d_col,
+                                 uint32_t num_nodes, uint32_t source, uint64_t num_walkers,
+                                 uint32_t length, float prob, uint32_t run, uint64_t seed,
+                                 uint64_t *d_counts, uint32_t *d_endpoints, uint32_t *d_paths,
+                                 uint64_t *d_stats, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

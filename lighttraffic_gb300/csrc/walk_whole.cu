@@ -210,3 +210,85 @@ cudaError_t launch_walk_whole(const WholeArgs &a, int app, int start, int grid, 
 }
 
 }  // namespace lt
+
+// ---------------------------------------------------------------------------
+// Allocation-free variant of lt_walk_device.
+//
+// Some callers cannot allocate device memory: code running inside a stream
+// capture that must not call cudaMalloc, plugins handed fixed input and output
+// buffers by a host framework that owns every allocation, and processes whose
+// device memory is fully reserved by another allocator.  lt_walk_device asks
+// them for a scratch buffer; this entry point needs none.  Its scratch (the
+// next-walker counter of the step kernel) lives in the file-scope array below,
+// which every GPU that loads this library holds until the process exits.
+//
+// The array is kNoAllocScratchBytes (256 B); the step kernel's scratch does not
+// grow with the graph or the walker count (one 8-byte counter inside a
+// walk_scratch_bytes()-byte block), and a call whose scratch need exceeds the
+// array is rejected with LT_ERR_CAPACITY.
+//
+// All calls share the one array: it keeps the previous call's contents, so the
+// counter is cleared on the caller's stream before each launch, and two calls
+// whose kernels overlap on the GPU (different streams, no ordering between
+// them) race on the counter and produce wrong results.  Order such calls on one
+// stream.
+//
+// The device address of the array is looked up once per device, on the first
+// call made with that device current (cudaGetSymbolAddress); make that first
+// call before any stream capture begins.
+// ---------------------------------------------------------------------------
+
+#include <mutex>
+
+#include "common.h"
+#include "engine.h"
+
+namespace lt {
+namespace {
+
+constexpr size_t kNoAllocScratchBytes = 256;
+constexpr int kNoAllocMaxDevices = 64;
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+
+std::mutex g_noalloc_mu;
+void *g_noalloc_ptr[kNoAllocMaxDevices] = {};
+
+lt_status noalloc_scratch(void **out)
+{
+    int device = 0;
+    LT_CUDA_TRY(cudaGetDevice(&device));
+    if (device < 0 || device >= kNoAllocMaxDevices)
+        return fail(LT_ERR_UNSUPPORTED, "device ordinal %d is beyond the %d devices the static scratch tracks", device,
+                    kNoAllocMaxDevices);
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    if (!g_noalloc_ptr[device]) {
+        void *p = nullptr;
+        const cudaError_t err = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (err != cudaSuccess || !p)
+            return fail(LT_ERR_CUDA, "cudaGetSymbolAddress of the static walk scratch failed on device %d: %s",
+                        device, cudaGetErrorString(err));
+        g_noalloc_ptr[device] = p;
+    }
+    *out = g_noalloc_ptr[device];
+    return LT_OK;
+}
+
+}  // namespace
+}  // namespace lt
+
+extern "C" lt_status lt_walk_device_noalloc(int app, int start_mode, const uint64_t *d_rowptr, const uint32_t *d_col,
+                                            uint32_t num_nodes, uint32_t source, uint64_t num_walkers,
+                                            uint32_t length, float prob, uint32_t run, uint64_t seed,
+                                            uint64_t *d_counts, uint32_t *d_endpoints, uint32_t *d_paths,
+                                            uint64_t *d_stats, void *stream)
+{
+    const size_t need = lt::walk_scratch_bytes();
+    if (need > lt::kNoAllocScratchBytes)
+        return lt::fail(LT_ERR_CAPACITY, "the step kernel needs %zu scratch bytes; the static array holds %zu", need,
+                        lt::kNoAllocScratchBytes);
+    void *scratch = nullptr;
+    LT_TRY(lt::noalloc_scratch(&scratch));
+    return lt::walk_device(app, start_mode, d_rowptr, d_col, num_nodes, source, num_walkers, length, prob, run, seed,
+                           d_counts, d_endpoints, d_paths, scratch, d_stats, (cudaStream_t)stream, 0);
+}
