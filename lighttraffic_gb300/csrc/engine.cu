@@ -102,21 +102,22 @@ lt_status engine_create(lt_graph *g, const lt_engine_cfg &cfg, lt_engine **out)
     const uint32_t P = g->P();
     const uint32_t cache = cfg.num_device_partitions == 0 ? P : std::min(cfg.num_device_partitions, P);
     e->resident = cache >= P;
-    if (!e->resident)
-        return bail(fail(LT_ERR_UNSUPPORTED, "out-of-core runs (-p %u < %u partitions) are not available in this build",
-                         cache, P));
     if (cudaStreamCreateWithFlags(&e->s_compute, cudaStreamNonBlocking) != cudaSuccess ||
         cudaStreamCreateWithFlags(&e->s_copy, cudaStreamNonBlocking) != cudaSuccess ||
         cudaStreamCreateWithFlags(&e->s_copyback, cudaStreamNonBlocking) != cudaSuccess ||
         cudaEventCreate(&e->ev_k0) != cudaSuccess || cudaEventCreate(&e->ev_k1) != cudaSuccess)
         return bail(fail(LT_ERR_CUDA, "stream / event creation failed"));
-    if (cudaMalloc(&e->d_rowptr, 8ull * ((uint64_t)g->V + 1)) != cudaSuccess ||
-        cudaMalloc(&e->d_col, 4ull * (g->E ? g->E : 1)) != cudaSuccess ||
+    if ((e->resident && (cudaMalloc(&e->d_rowptr, 8ull * ((uint64_t)g->V + 1)) != cudaSuccess ||
+                         cudaMalloc(&e->d_col, 4ull * (g->E ? g->E : 1)) != cudaSuccess)) ||
         cudaMalloc(&e->d_counts, 8ull * g->V) != cudaSuccess ||
         cudaMalloc(&e->d_scratch, walk_scratch_bytes()) != cudaSuccess ||
         cudaMalloc(&e->d_stats, 64) != cudaSuccess) {
         cudaGetLastError();
         return bail(fail(LT_ERR_NOMEM, "device allocation for the resident graph failed"));
+    }
+    if (!e->resident) {
+        lt_status s = ooc_create(e, &e->ooc);
+        if (s != LT_OK) return bail(s);
     }
     *out = e;
     return LT_OK;
@@ -127,6 +128,7 @@ void engine_destroy(lt_engine *e)
     if (!e) return;
     cudaSetDevice(e->device);
     if (e->s_compute) cudaStreamSynchronize(e->s_compute);
+    if (e->ooc) ooc_destroy(e->ooc);
     for (void *p : {(void *)e->d_rowptr, (void *)e->d_col, (void *)e->d_counts, e->d_scratch, (void *)e->d_stats,
                     (void *)e->d_endpoints, (void *)e->d_paths})
         if (p) cudaFree(p);
@@ -140,6 +142,7 @@ void engine_destroy(lt_engine *e)
 lt_status engine_drop_cache(lt_engine *e)
 {
     e->loaded = false;
+    if (e->ooc) return ooc_drop_cache(e->ooc);
     return LT_OK;
 }
 
@@ -189,6 +192,8 @@ lt_status engine_run(lt_engine *e, int app, int start, uint32_t source, uint64_t
     if (app == kPPR && source >= g.V) return fail(LT_ERR_INVALID, "source %u out of range (V=%u)", source, g.V);
     if (runs == 0) runs = 1;
     LT_CUDA_TRY(cudaSetDevice(e->device));
+    if (!e->resident)
+        return ooc_run(e, app, start, source, W, length, runs, run_base, prob, counts_out, endpoints_out, paths_out);
     e->stats = lt_stats{};
     const double t0 = now_ms();
     LT_TRY(load_all(e));

@@ -7,6 +7,7 @@
 
 #include "common.h"
 #include "graph.h"
+#include "ooc.h"
 
 namespace lt {
 lt_status generate_rmat(int device, uint32_t scale, uint64_t E, double a, double b, double c, double d, uint64_t seed,
@@ -35,6 +36,8 @@ struct lt_engine {
     uint64_t endpoints_cap = 0;
     uint32_t *d_paths = nullptr;
     uint64_t paths_cap = 0;
+
+    lt::Ooc *ooc = nullptr;  // out-of-core state when not every partition is cached
 
     lt_stats stats{};
 };

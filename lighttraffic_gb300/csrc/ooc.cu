@@ -1,0 +1,732 @@
+// ooc.cu -- out-of-core run loop.
+//
+// One iteration (GPUScheduler::run, src/Scheduler.h:311-330):
+//   1. the policy picks partition p;
+//   2. p is made readable: loaded into a cache slot (evicting the policy's
+//      victim) or, below the zero-copy threshold, mapped from pinned host
+//      memory (zeroCopyCompute, :254-273);
+//   3. p's spilled walkers come back from the host (walkerLoadingPhase,
+//      :215-233), evicting other partitions' walkers to the host if the
+//      device pool is short (handleWalkerPoolOverflow, :59-82);
+//   4. one step-kernel launch drains p's queue (and creates the walkers that
+//      start in p), walking every walker through all readable partitions;
+//   5. walkers that leave for an unreadable partition are bucketed into their
+//      destination queues by the scatter kernel, into chunks allocated here.
+// Queue bookkeeping lives on the host (exact counts, no per-decision D2H of
+// queue metadata as in src/buffer/Pool.h:604-606); per iteration one small
+// D2H (the destination histogram) and one small H2D (the chunk plan) cross
+// the link.
+#include "ooc.h"
+
+#include <algorithm>
+#include <chrono>
+#include <cstring>
+
+#include "engine.h"
+#include "lt_core.cuh"
+#include "walk_part.h"
+
+namespace lt {
+
+uint64_t Queue::dev_count() const
+{
+    return dev_chunks.empty() ? 0 : (uint64_t)(dev_chunks.size() - 1) * kChunk + tail_fill;
+}
+uint64_t Queue::host_count() const { return (uint64_t)host_chunks.size() * kChunk; }
+
+namespace {
+
+constexpr uint32_t kHostSlabChunks = 32;  // chunks per pinned host slab (3 MiB)
+
+double now_ms()
+{
+    using namespace std::chrono;
+    return duration<double, std::milli>(steady_clock::now().time_since_epoch()).count();
+}
+
+template <typename T>
+lt_status dalloc(T **p, uint64_t count)
+{
+    if (cudaMalloc((void **)p, sizeof(T) * (count ? count : 1)) != cudaSuccess) {
+        cudaGetLastError();
+        return fail(LT_ERR_NOMEM, "cudaMalloc of %llu bytes failed", (unsigned long long)(sizeof(T) * count));
+    }
+    return LT_OK;
+}
+
+struct EvPair {
+    cudaEvent_t a = nullptr, b = nullptr;
+};
+
+}  // namespace
+
+struct Ooc {
+    lt_engine *e = nullptr;
+    lt_graph *g = nullptr;
+    uint32_t P = 0, K = 0;
+    uint64_t slot_stride = 0;
+    uint8_t *d_slots = nullptr;
+    std::vector<int32_t> slot_of, part_in_slot;
+    std::vector<uint64_t> last_used;
+    std::vector<unsigned long long> h_rp, h_col;
+    std::vector<uint8_t> h_mapped;
+
+    uint32_t *d_node_off = nullptr;
+    uint64_t *d_edge_off = nullptr;
+    unsigned long long *d_rp = nullptr, *d_col = nullptr;
+    uint8_t *d_mapped = nullptr;
+
+    uint8_t *d_arena = nullptr;
+    uint32_t n_chunks = 0;
+    std::vector<uint32_t> free_chunks;
+
+    std::vector<HostBuf> host_slabs;
+    std::vector<uint32_t> host_free;
+
+    uint64_t staging_cap = 0;
+    uint32_t *d_out = nullptr;  // 4 arrays of staging_cap
+    unsigned long long *d_out_n = nullptr;
+    uint32_t *d_hist = nullptr;
+    uint32_t *d_cursor = nullptr, *d_win_off = nullptr;
+    uint32_t *d_plan = nullptr;
+    uint64_t plan_cap = 0;
+    uint32_t *d_work = nullptr;
+    uint64_t work_cap = 0;
+    unsigned long long *d_next = nullptr, *d_stats = nullptr;
+
+    HostBuf h_hist;  // pinned: P u32 hist + out_n
+    std::vector<uint32_t> h_cursor, h_win_off, h_plan, h_work;
+    std::vector<uint32_t> arrivals;
+    std::vector<uint64_t> waiting;
+
+    std::vector<Queue> q;
+    std::unique_ptr<Policy> policy;
+    int32_t prev_loaded = -1, prev_computed = -1;
+    uint64_t iteration = 0;
+    uint64_t zc_threshold = 0;
+    int grid[3] = {0, 0, 0};
+
+    uint8_t *host_chunk(uint32_t id) { return (uint8_t *)host_slabs[id / kHostSlabChunks].ptr + (uint64_t)(id % kHostSlabChunks) * kChunkBytes; }
+};
+
+namespace {
+
+__global__ void set_entry_kernel(unsigned long long *rp, unsigned long long *col, uint8_t *mapped, uint32_t p,
+                                 unsigned long long rv, unsigned long long cv, uint8_t mv)
+{
+    rp[p] = rv;
+    col[p] = cv;
+    mapped[p] = mv;
+}
+
+// Table updates travel as kernel arguments, so they are ordered on `st` with
+// the kernels that read the table and capture the values at call time.
+lt_status set_entry(Ooc &o, uint32_t p, cudaStream_t st)
+{
+    set_entry_kernel<<<1, 1, 0, st>>>(o.d_rp, o.d_col, o.d_mapped, p, o.h_rp[p], o.h_col[p], o.h_mapped[p]);
+    LT_CUDA_TRY(cudaGetLastError());
+    return LT_OK;
+}
+
+SchedView view(Ooc &o)
+{
+    for (uint32_t p = 0; p < o.P; p++) o.waiting[p] = o.q[p].total();
+    SchedView v;
+    v.P = o.P;
+    v.waiting = o.waiting.data();
+    v.slot_of = o.slot_of.data();
+    v.last_used = o.last_used.data();
+    v.arrivals = o.arrivals.data();
+    v.iteration = o.iteration;
+    return v;
+}
+
+lt_status evict_partition(Ooc &o, uint32_t v)
+{
+    lt_engine &e = *o.e;
+    const int32_t s = o.slot_of[v];
+    o.slot_of[v] = -1;
+    o.part_in_slot[s] = -1;
+    o.h_rp[v] = 0;
+    o.h_col[v] = 0;
+    LT_TRY(set_entry(o, v, e.s_compute));
+    return LT_OK;
+}
+
+// GPUGraph::loadAsync (src/GraphLoader.h:193-214): rowptr slice, then col
+// slice at the next 16-byte boundary of the slot.
+lt_status load_partition(Ooc &o, uint32_t p)
+{
+    lt_engine &e = *o.e;
+    lt_graph &g = *o.g;
+    if (o.slot_of[p] >= 0) return LT_OK;
+    int32_t slot = -1;
+    for (uint32_t s = 0; s < o.K; s++)
+        if (o.part_in_slot[s] < 0) {
+            slot = (int32_t)s;
+            break;
+        }
+    if (slot < 0) {
+        SchedView v = view(o);
+        const int32_t victim = o.policy->victim(v, o.prev_loaded, p);
+        if (victim < 0) return fail(LT_ERR_CAPACITY, "no cached partition can be evicted");
+        slot = o.slot_of[victim];
+        LT_TRY(evict_partition(o, (uint32_t)victim));
+    }
+    // the slot's previous occupant may still be read by queued compute work
+    cudaEvent_t free_ev;
+    LT_CUDA_TRY(cudaEventCreateWithFlags(&free_ev, cudaEventDisableTiming));
+    LT_CUDA_TRY(cudaEventRecord(free_ev, e.s_compute));
+    LT_CUDA_TRY(cudaStreamWaitEvent(e.s_copy, free_ev, 0));
+    cudaEventDestroy(free_ev);
+
+    const uint64_t n0 = g.node_off[p], n1 = g.node_off[p + 1];
+    const uint64_t e0 = g.edge_off[p], e1 = g.edge_off[p + 1];
+    uint8_t *base = o.d_slots + (uint64_t)slot * o.slot_stride;
+    const uint64_t rp_bytes = 8 * (n1 - n0 + 1);
+    const uint64_t col_off = (rp_bytes + 15) & ~15ull;
+    EvPair t;
+    cudaEventCreate(&t.a);
+    cudaEventCreate(&t.b);
+    LT_CUDA_TRY(cudaEventRecord(t.a, e.s_copy));
+    LT_CUDA_TRY(cudaMemcpyAsync(base, g.rowptr() + n0, rp_bytes, cudaMemcpyHostToDevice, e.s_copy));
+    if (e1 > e0) LT_CUDA_TRY(cudaMemcpyAsync(base + col_off, g.col() + e0, 4 * (e1 - e0), cudaMemcpyHostToDevice, e.s_copy));
+    LT_CUDA_TRY(cudaEventRecord(t.b, e.s_copy));
+    // publish the slot to kernels once its data is in place
+    LT_CUDA_TRY(cudaStreamWaitEvent(e.s_compute, t.b, 0));
+    o.h_rp[p] = (unsigned long long)(uintptr_t)base;
+    o.h_col[p] = (unsigned long long)(uintptr_t)(base + col_off);
+    o.h_mapped[p] = 0;
+    LT_TRY(set_entry(o, p, e.s_compute));
+    o.slot_of[p] = slot;
+    o.part_in_slot[slot] = (int32_t)p;
+    LT_CUDA_TRY(cudaEventSynchronize(t.b));
+    float ms = 0;
+    cudaEventElapsedTime(&ms, t.a, t.b);
+    cudaEventDestroy(t.a);
+    cudaEventDestroy(t.b);
+    e.stats.graph_loading_ms += ms;
+    e.stats.graph_loading_calls++;
+    e.stats.h2d_graph_bytes += rp_bytes + 4 * (e1 - e0);
+    e.stats.partition_loads++;
+    return LT_OK;
+}
+
+lt_status host_chunk_alloc(Ooc &o, uint32_t &id)
+{
+    if (o.host_free.empty()) {
+        HostBuf b;
+        LT_TRY(host_alloc(b, kHostSlabChunks * kChunkBytes, true));
+        const uint32_t slab = (uint32_t)o.host_slabs.size();
+        o.host_slabs.push_back(b);
+        for (uint32_t i = kHostSlabChunks; i-- > 0;) o.host_free.push_back(slab * kHostSlabChunks + i);
+    }
+    id = o.host_free.back();
+    o.host_free.pop_back();
+    return LT_OK;
+}
+
+// Move full device chunks of other partitions to the host until `need` device
+// chunks are free (setEvictedWalker / getEvictedPartition, src/Scheduler.h:53-57,
+// :130-147: the partition with the fewest walkers among those holding a full
+// page on the device).
+lt_status spill_until(Ooc &o, uint64_t need, int32_t except)
+{
+    lt_engine &e = *o.e;
+    double t0 = -1;
+    while (o.free_chunks.size() < need) {
+        int32_t best = -1;
+        for (uint32_t i = 0; i < o.P; i++) {
+            if ((int32_t)i == except) continue;
+            const Queue &qi = o.q[i];
+            const size_t full = qi.dev_chunks.size() - (qi.dev_chunks.empty() || qi.tail_fill == kChunk ? 0 : 1);
+            if (qi.dev_chunks.empty() || full == 0) continue;
+            if (best < 0 || qi.total() < o.q[best].total()) best = (int32_t)i;
+        }
+        if (best < 0)
+            return fail(LT_ERR_CAPACITY, "walker pool of %u chunks cannot hold the walkers in flight (-b too small)",
+                        o.n_chunks);
+        if (t0 < 0) {
+            LT_CUDA_TRY(cudaStreamSynchronize(e.s_compute));
+            t0 = now_ms();
+        }
+        Queue &qb = o.q[best];
+        // spill full chunks from the front; the partially filled tail stays
+        const size_t full = qb.dev_chunks.size() - (qb.tail_fill == kChunk ? 0 : 1);
+        size_t moved = 0;
+        for (size_t k = 0; k < full && o.free_chunks.size() + moved < need; k++) {
+            uint32_t hid;
+            LT_TRY(host_chunk_alloc(o, hid));
+            const uint32_t dc = qb.dev_chunks[k];
+            LT_CUDA_TRY(cudaMemcpyAsync(o.host_chunk(hid), o.d_arena + (uint64_t)dc * kChunkBytes, kChunkBytes,
+                                        cudaMemcpyDeviceToHost, e.s_copyback));
+            qb.host_chunks.push_back(hid);
+            o.free_chunks.push_back(dc);
+            moved++;
+            e.stats.d2h_walker_bytes += kChunkBytes;
+        }
+        qb.dev_chunks.erase(qb.dev_chunks.begin(), qb.dev_chunks.begin() + moved);
+        if (qb.dev_chunks.empty()) qb.tail_fill = 0;
+        e.stats.walker_evicting_calls++;
+    }
+    if (t0 >= 0) {
+        LT_CUDA_TRY(cudaStreamSynchronize(e.s_copyback));
+        e.stats.walker_evicting_ms += now_ms() - t0;
+    }
+    return LT_OK;
+}
+
+// Bring up to `max_chunks` of p's spilled chunks back to the device
+// (walkerLoadingPhase); they go in front of p's device chunks.
+lt_status unspill(Ooc &o, uint32_t p, uint64_t max_chunks)
+{
+    lt_engine &e = *o.e;
+    Queue &qp = o.q[p];
+    const uint64_t n = std::min<uint64_t>(max_chunks, qp.host_chunks.size());
+    if (n == 0) return LT_OK;
+    const double t0 = now_ms();
+    std::vector<uint32_t> fresh;
+    for (uint64_t k = 0; k < n; k++) {
+        const uint32_t hid = qp.host_chunks.back();
+        qp.host_chunks.pop_back();
+        const uint32_t dc = o.free_chunks.back();
+        o.free_chunks.pop_back();
+        LT_CUDA_TRY(cudaMemcpyAsync(o.d_arena + (uint64_t)dc * kChunkBytes, o.host_chunk(hid), kChunkBytes,
+                                    cudaMemcpyHostToDevice, e.s_copy));
+        o.host_free.push_back(hid);
+        fresh.push_back(dc);
+        e.stats.h2d_walker_bytes += kChunkBytes;
+    }
+    if (qp.dev_chunks.empty()) qp.tail_fill = kChunk;
+    qp.dev_chunks.insert(qp.dev_chunks.begin(), fresh.begin(), fresh.end());
+    LT_CUDA_TRY(cudaStreamSynchronize(e.s_copy));
+    e.stats.walker_loading_ms += now_ms() - t0;
+    e.stats.walker_loading_calls++;
+    return LT_OK;
+}
+
+
+struct RunParams {
+    int app, start;
+    uint32_t source, length, run;
+    uint64_t W, thr;
+    uint64_t *counts;
+    uint32_t *endpoints, *paths;
+};
+
+// Launch the step kernel over p's device chunks plus G lazily created walkers
+// (ordinals lazy_begin..), then bucket the walkers that left.  p < 0: the
+// lazily created walkers have uniform random starts and belong to no
+// partition yet (the reference's createWalkers / insert, src/WalkManager.h:341-360).
+lt_status step_and_bucket(Ooc &o, const RunParams &rp, int32_t p, uint64_t lazy_begin, uint64_t G, bool zero_copy)
+{
+    lt_engine &e = *o.e;
+    lt_graph &g = *o.g;
+    Queue *qp = p >= 0 ? &o.q[p] : nullptr;
+    const uint64_t n_chunk_walkers = qp ? qp->dev_count() : 0;
+    if (n_chunk_walkers + G == 0) return LT_OK;
+    if (n_chunk_walkers + G > o.staging_cap) return fail(LT_ERR_CAPACITY, "staging area too small");
+    o.h_work.clear();
+    if (qp) o.h_work.assign(qp->dev_chunks.begin(), qp->dev_chunks.end());
+    if (o.h_work.size() > o.work_cap) return fail(LT_ERR_CAPACITY, "work list too small");
+    if (!o.h_work.empty())
+        LT_CUDA_TRY(cudaMemcpyAsync(o.d_work, o.h_work.data(), 4 * o.h_work.size(), cudaMemcpyHostToDevice, e.s_compute));
+    LT_CUDA_TRY(cudaMemsetAsync(o.d_next, 0, 8, e.s_compute));
+    LT_CUDA_TRY(cudaMemsetAsync(o.d_out_n, 0, 8, e.s_compute));
+    LT_CUDA_TRY(cudaMemsetAsync(o.d_hist, 0, 4ull * o.P, e.s_compute));
+
+    StepArgs a{};
+    a.t = PartTable{o.d_node_off, o.d_edge_off, o.d_rp, o.d_col, o.d_mapped, o.P};
+    a.arena = o.d_arena;
+    a.work_chunks = o.d_work;
+    a.n_chunk_walkers = n_chunk_walkers;
+    a.lazy_begin = lazy_begin;
+    a.lazy_count = G;
+    a.lazy_part = p >= 0 ? (uint32_t)p : 0;
+    a.lazy_mode = p < 0 ? kStartUniform : (rp.start == kStartPerVertex ? kStartPerVertex : kStartSource);
+    a.W = rp.W;
+    a.V = g.V;
+    a.source = rp.source;
+    a.length = rp.length;
+    a.run = rp.run;
+    a.seed = e.cfg.seed;
+    a.thr = rp.thr;
+    a.counts = rp.counts;
+    a.endpoints = rp.endpoints;
+    a.paths = rp.paths;
+    a.out_cur = o.d_out;
+    a.out_step = o.d_out + o.staging_cap;
+    a.out_idx = o.d_out + 2 * o.staging_cap;
+    a.out_dest = o.d_out + 3 * o.staging_cap;
+    a.out_n = o.d_out_n;
+    a.hist = o.d_hist;
+    a.next = o.d_next;
+    a.stats = o.d_stats;
+
+    EvPair t;
+    cudaEventCreate(&t.a);
+    cudaEventCreate(&t.b);
+    LT_CUDA_TRY(cudaEventRecord(t.a, e.s_compute));
+    LT_CUDA_TRY(launch_walk_part(a, rp.app, o.grid[rp.app], e.s_compute));
+    LT_CUDA_TRY(cudaEventRecord(t.b, e.s_compute));
+    e.stats.kernel_launches++;
+    uint32_t *h_hist = (uint32_t *)o.h_hist.ptr;
+    unsigned long long *h_n = (unsigned long long *)(h_hist + o.P + (o.P & 1));
+    LT_CUDA_TRY(cudaMemcpyAsync(h_hist, o.d_hist, 4ull * o.P, cudaMemcpyDeviceToHost, e.s_compute));
+    LT_CUDA_TRY(cudaMemcpyAsync(h_n, o.d_out_n, 8, cudaMemcpyDeviceToHost, e.s_compute));
+    LT_CUDA_TRY(cudaStreamSynchronize(e.s_compute));
+    float ms = 0;
+    cudaEventElapsedTime(&ms, t.a, t.b);
+    cudaEventDestroy(t.a);
+    cudaEventDestroy(t.b);
+    e.stats.step_kernel_ms += ms;
+    if (zero_copy) {
+        e.stats.zerocopy_ms += ms;
+        e.stats.zerocopy_calls++;
+    } else {
+        e.stats.computing_ms += ms;
+        e.stats.computing_calls++;
+    }
+    // p's queue is drained: its chunks return to the pool.
+    if (qp) {
+        for (uint32_t c : qp->dev_chunks) o.free_chunks.push_back(c);
+        qp->dev_chunks.clear();
+        qp->tail_fill = 0;
+        qp->lazy_next += G;
+    }
+    const uint64_t staged = *h_n;
+    for (uint32_t d = 0; d < o.P; d++) o.arrivals[d] = h_hist[d];
+    if (staged == 0) return LT_OK;
+
+    // Plan the append of h_hist[d] walkers to each destination queue.
+    uint64_t need = 0;
+    for (uint32_t d = 0; d < o.P; d++) {
+        if (!h_hist[d]) continue;
+        const Queue &qd = o.q[d];
+        const bool open_tail = !qd.dev_chunks.empty() && qd.tail_fill < kChunk;
+        const uint64_t fill = open_tail ? qd.tail_fill : 0;
+        need += (fill + h_hist[d] + kChunk - 1) / kChunk - (open_tail ? 1 : 0);
+    }
+    if (need > o.free_chunks.size()) LT_TRY(spill_until(o, need, -1));
+    if (need > o.free_chunks.size()) return fail(LT_ERR_CAPACITY, "walker pool exhausted");
+    o.h_plan.clear();
+    for (uint32_t d = 0; d < o.P; d++) {
+        o.h_cursor[d] = 0;
+        o.h_win_off[d] = 0;
+        if (!h_hist[d]) continue;
+        Queue &qd = o.q[d];
+        if (qd.dev_chunks.empty() || qd.tail_fill == kChunk) {
+            qd.dev_chunks.push_back(o.free_chunks.back());
+            o.free_chunks.pop_back();
+            qd.tail_fill = 0;
+        }
+        o.h_win_off[d] = (uint32_t)o.h_plan.size();
+        o.h_cursor[d] = qd.tail_fill;
+        o.h_plan.push_back(qd.dev_chunks.back());
+        const uint64_t tot = (uint64_t)qd.tail_fill + h_hist[d];
+        const uint64_t extra = (tot + kChunk - 1) / kChunk - 1;
+        for (uint64_t k = 0; k < extra; k++) {
+            const uint32_t c = o.free_chunks.back();
+            o.free_chunks.pop_back();
+            qd.dev_chunks.push_back(c);
+            o.h_plan.push_back(c);
+        }
+        qd.tail_fill = (uint32_t)(tot - extra * kChunk);
+    }
+    if (o.h_plan.size() > o.plan_cap) return fail(LT_ERR_CAPACITY, "plan buffer too small");
+    LT_CUDA_TRY(cudaMemcpyAsync(o.d_cursor, o.h_cursor.data(), 4ull * o.P, cudaMemcpyHostToDevice, e.s_compute));
+    LT_CUDA_TRY(cudaMemcpyAsync(o.d_win_off, o.h_win_off.data(), 4ull * o.P, cudaMemcpyHostToDevice, e.s_compute));
+    LT_CUDA_TRY(cudaMemcpyAsync(o.d_plan, o.h_plan.data(), 4ull * o.h_plan.size(), cudaMemcpyHostToDevice, e.s_compute));
+    ScatterArgs sa{};
+    sa.in_cur = a.out_cur;
+    sa.in_step = a.out_step;
+    sa.in_idx = a.out_idx;
+    sa.in_dest = a.out_dest;
+    sa.n = staged;
+    sa.arena = o.d_arena;
+    sa.cursor = o.d_cursor;
+    sa.win_off = o.d_win_off;
+    sa.plan_chunks = o.d_plan;
+    sa.P = o.P;
+    LT_CUDA_TRY(launch_scatter(sa, e.device, e.s_compute));
+    e.stats.kernel_launches++;
+    return LT_OK;
+}
+
+// Walkers that can be created in this pass without overflowing the pool:
+// after p's own chunks are released, every staged walker must fit, plus one
+// partially filled tail chunk per destination.
+uint64_t lazy_budget(Ooc &o, int32_t p, uint64_t left)
+{
+    const uint64_t own_chunks = p >= 0 ? o.q[p].dev_chunks.size() : 0;
+    const uint64_t own = p >= 0 ? o.q[p].dev_count() : 0;
+    const uint64_t avail = o.free_chunks.size() + own_chunks;
+    if (avail <= (uint64_t)o.P + 1) return 0;
+    uint64_t g = (avail - o.P - 1) * kChunk;
+    g = g > own ? g - own : 0;
+    if (g + own > o.staging_cap) g = o.staging_cap > own ? o.staging_cap - own : 0;
+    return std::min(g, left);
+}
+
+lt_status ensure_pool(Ooc &o, uint64_t W)
+{
+    lt_engine &e = *o.e;
+    uint64_t B = e.cfg.num_device_walkers ? e.cfg.num_device_walkers : W;
+    if (B > W) B = W;
+    if (B < kChunk) B = kChunk;
+    const uint64_t want = (B + kChunk - 1) / kChunk + 2ull * o.P + 2;
+    if (want > 0xFFFFFFF0ull) return fail(LT_ERR_CAPACITY, "walker pool too large");
+    if (o.d_arena && o.n_chunks == want) return LT_OK;
+    for (void *p : {(void *)o.d_arena, (void *)o.d_out, (void *)o.d_plan, (void *)o.d_work})
+        if (p) cudaFree(p);
+    o.d_arena = nullptr;
+    o.d_out = o.d_plan = o.d_work = nullptr;
+    o.n_chunks = (uint32_t)want;
+    o.staging_cap = (uint64_t)o.n_chunks * kChunk;
+    o.plan_cap = o.n_chunks + (uint64_t)o.P;
+    o.work_cap = o.n_chunks;
+    LT_TRY(dalloc(&o.d_arena, (uint64_t)o.n_chunks * kChunkBytes));
+    LT_TRY(dalloc(&o.d_out, 4 * o.staging_cap));
+    LT_TRY(dalloc(&o.d_plan, o.plan_cap));
+    LT_TRY(dalloc(&o.d_work, o.work_cap));
+    return LT_OK;
+}
+
+void reset_queues(Ooc &o)
+{
+    o.free_chunks.clear();
+    for (uint32_t c = o.n_chunks; c-- > 0;) o.free_chunks.push_back(c);
+    for (Queue &qq : o.q) {
+        for (uint32_t h : qq.host_chunks) o.host_free.push_back(h);
+        qq = Queue{};
+    }
+}
+
+// One iteration for partition p (GPUScheduler::run).
+lt_status process(Ooc &o, const RunParams &rp, uint32_t p)
+{
+    lt_engine &e = *o.e;
+    o.iteration++;
+    e.stats.iterations++;
+    o.last_used[p] = o.iteration;
+    o.prev_computed = (int32_t)p;
+    Queue &qp = o.q[p];
+    const bool zero_copy = o.slot_of[p] < 0 && qp.total() < o.zc_threshold;
+    if (zero_copy) {
+        lt_graph &g = *o.g;
+        void *rp_dev = nullptr, *col_dev = nullptr;
+        LT_CUDA_TRY(cudaHostGetDevicePointer(&rp_dev, (void *)(g.rowptr() + g.node_off[p]), 0));
+        LT_CUDA_TRY(cudaHostGetDevicePointer(&col_dev, (void *)(g.col() + g.edge_off[p]), 0));
+        o.h_rp[p] = (unsigned long long)(uintptr_t)rp_dev;
+        o.h_col[p] = (unsigned long long)(uintptr_t)col_dev;
+        o.h_mapped[p] = 1;
+        LT_TRY(set_entry(o, p, e.s_compute));
+    } else {
+        e.stats.explicit_iterations++;
+        LT_TRY(load_partition(o, p));
+        o.prev_loaded = (int32_t)p;
+    }
+    // walkerLoadingPhase: bring spilled walkers back, keeping room to make progress
+    if (!qp.host_chunks.empty()) {
+        const uint64_t want = qp.host_chunks.size();
+        const uint64_t reserve = (uint64_t)o.P + 2;
+        if (o.free_chunks.size() < want + reserve) {
+            const uint64_t target = std::min<uint64_t>(want + reserve, o.n_chunks - qp.dev_chunks.size());
+            lt_status s = spill_until(o, target, (int32_t)p);
+            if (s != LT_OK && o.free_chunks.size() <= reserve) return s;
+            clear_error();
+        }
+        const uint64_t room = o.free_chunks.size() > reserve ? o.free_chunks.size() - reserve : 0;
+        LT_TRY(unspill(o, p, std::min<uint64_t>(want, room)));
+    }
+    uint64_t G = lazy_budget(o, (int32_t)p, qp.lazy_left());
+    if (G == 0 && qp.lazy_left() > 0 && qp.dev_count() == 0) {
+        LT_TRY(spill_until(o, (uint64_t)o.P + 2 + 1, (int32_t)p));
+        G = lazy_budget(o, (int32_t)p, qp.lazy_left());
+    }
+    LT_TRY(step_and_bucket(o, rp, (int32_t)p, qp.lazy_next, G, zero_copy));
+    if (zero_copy) {
+        o.h_rp[p] = 0;
+        o.h_col[p] = 0;
+        o.h_mapped[p] = 0;
+        LT_TRY(set_entry(o, p, e.s_compute));
+    }
+    SchedView v = view(o);
+    o.policy->observe(v);
+    return LT_OK;
+}
+
+}  // namespace
+
+lt_status ooc_create(lt_engine *e, Ooc **out)
+{
+    Ooc *o = new Ooc();
+    o->e = e;
+    o->g = e->g;
+    lt_graph &g = *e->g;
+    o->P = g.P();
+    o->K = std::min<uint32_t>(e->cfg.num_device_partitions, o->P);
+    if (o->K < 1) o->K = 1;
+    o->slot_stride = (g.part_bytes + 16 + 255) & ~255ull;
+    uint64_t max_slot = 0;
+    for (uint32_t p = 0; p < o->P; p++) max_slot = std::max<uint64_t>(max_slot, g.slot_bytes(p) + 16);
+    if (max_slot > o->slot_stride) o->slot_stride = (max_slot + 255) & ~255ull;
+    auto bail = [&](lt_status s) {
+        ooc_destroy(o);
+        return s;
+    };
+    lt_status s = dalloc(&o->d_slots, (uint64_t)o->K * o->slot_stride);
+    if (s == LT_OK) s = dalloc(&o->d_node_off, o->P + 1);
+    if (s == LT_OK) s = dalloc(&o->d_edge_off, o->P + 1);
+    if (s == LT_OK) s = dalloc(&o->d_rp, o->P);
+    if (s == LT_OK) s = dalloc(&o->d_col, o->P);
+    if (s == LT_OK) s = dalloc(&o->d_mapped, o->P);
+    if (s == LT_OK) s = dalloc(&o->d_out_n, 1);
+    if (s == LT_OK) s = dalloc(&o->d_hist, o->P);
+    if (s == LT_OK) s = dalloc(&o->d_cursor, o->P);
+    if (s == LT_OK) s = dalloc(&o->d_win_off, o->P);
+    if (s == LT_OK) s = dalloc(&o->d_next, 1);
+    if (s == LT_OK) s = dalloc(&o->d_stats, 8);
+    if (s == LT_OK) s = host_alloc(o->h_hist, 4ull * o->P + 16, true);
+    if (s != LT_OK) return bail(s);
+    if (cudaMemcpy(o->d_node_off, g.node_off.data(), 4ull * (o->P + 1), cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy(o->d_edge_off, g.edge_off.data(), 8ull * (o->P + 1), cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemset(o->d_rp, 0, 8ull * o->P) != cudaSuccess || cudaMemset(o->d_col, 0, 8ull * o->P) != cudaSuccess ||
+        cudaMemset(o->d_mapped, 0, o->P) != cudaSuccess)
+        return bail(fail(LT_ERR_CUDA, "partition table upload failed"));
+    o->slot_of.assign(o->P, -1);
+    o->part_in_slot.assign(o->K, -1);
+    o->last_used.assign(o->P, 0);
+    o->h_rp.assign(o->P, 0);
+    o->h_col.assign(o->P, 0);
+    o->h_mapped.assign(o->P, 0);
+    o->h_cursor.assign(o->P, 0);
+    o->h_win_off.assign(o->P, 0);
+    o->arrivals.assign(o->P, 0);
+    o->waiting.assign(o->P, 0);
+    o->q.assign(o->P, Queue{});
+    if (e->cfg.sched == LT_SCHED_FIFO)
+        o->policy.reset(new FifoPolicy());
+    else
+        o->policy.reset(new Policy());
+    o->zc_threshold = e->cfg.zerocopy_threshold == UINT64_MAX ? g.part_bytes / 128 / 2 : e->cfg.zerocopy_threshold;
+    const size_t smem = part_smem(o->P);
+    if (smem > 48 * 1024) return bail(fail(LT_ERR_UNSUPPORTED, "partition count %u needs %zu bytes of shared memory", o->P, smem));
+    for (int app = 0; app < 3; app++) o->grid[app] = part_grid(app, 0, e->device, smem);
+    *out = o;
+    return LT_OK;
+}
+
+void ooc_destroy(Ooc *o)
+{
+    if (!o) return;
+    for (void *p : {(void *)o->d_slots, (void *)o->d_node_off, (void *)o->d_edge_off, (void *)o->d_rp, (void *)o->d_col,
+                    (void *)o->d_mapped, (void *)o->d_arena, (void *)o->d_out, (void *)o->d_out_n, (void *)o->d_hist,
+                    (void *)o->d_cursor, (void *)o->d_win_off, (void *)o->d_plan, (void *)o->d_work, (void *)o->d_next,
+                    (void *)o->d_stats})
+        if (p) cudaFree(p);
+    for (HostBuf &b : o->host_slabs) host_free(b);
+    host_free(o->h_hist);
+    delete o;
+}
+
+lt_status ooc_drop_cache(Ooc *o)
+{
+    lt_engine &e = *o->e;
+    LT_CUDA_TRY(cudaStreamSynchronize(e.s_compute));
+    for (uint32_t p = 0; p < o->P; p++)
+        if (o->slot_of[p] >= 0) LT_TRY(evict_partition(*o, p));
+    LT_CUDA_TRY(cudaStreamSynchronize(e.s_compute));
+    return LT_OK;
+}
+
+lt_status ooc_run(lt_engine *e, int app, int start, uint32_t source, uint64_t W, uint32_t length, uint32_t runs,
+                  uint32_t run_base, float prob, uint64_t *counts_out, uint32_t *endpoints_out, uint32_t *paths_out)
+{
+    Ooc &o = *e->ooc;
+    lt_graph &g = *e->g;
+    if (W >= (1ull << 32)) return fail(LT_ERR_INVALID, "out-of-core runs take fewer than 2^32 walkers per run");
+    if (runs == 0) runs = 1;
+    LT_TRY(ensure_pool(o, W));
+    e->stats = lt_stats{};
+    const double t0 = now_ms();
+    cudaStream_t st = e->s_compute;
+    if (app != kWalk) LT_CUDA_TRY(cudaMemsetAsync(e->d_counts, 0, 8ull * g.V, st));
+    LT_CUDA_TRY(cudaMemsetAsync(o.d_stats, 0, 64, st));
+    if (endpoints_out) {
+        LT_CUDA_TRY(cudaFree(e->d_endpoints));
+        e->d_endpoints = nullptr;
+        LT_TRY(dalloc(&e->d_endpoints, W));
+    }
+    if (paths_out) {
+        LT_CUDA_TRY(cudaFree(e->d_paths));
+        e->d_paths = nullptr;
+        LT_TRY(dalloc(&e->d_paths, W * ((uint64_t)length + 1)));
+    }
+    RunParams rp{};
+    rp.app = app;
+    rp.start = start;
+    rp.source = source;
+    rp.length = length;
+    rp.W = W;
+    rp.thr = app == kWalk ? 0 : threshold53(prob);
+    rp.counts = app == kWalk ? nullptr : e->d_counts;
+    rp.endpoints = endpoints_out ? e->d_endpoints : nullptr;
+    rp.paths = paths_out ? e->d_paths : nullptr;
+    for (uint32_t r = 0; r < runs; r++) {
+        rp.run = run_base + r;
+        reset_queues(o);
+        o.prev_computed = -1;
+        if (start == kStartSource) {
+            o.q[g.find_partition(source)].lazy_total = W;
+        } else if (start == kStartPerVertex) {
+            const uint64_t wraps = W / g.V, rem = W % g.V;
+            for (uint32_t p = 0; p < o.P; p++) {
+                const uint64_t nb = g.node_off[p], n = g.node_off[p + 1] - nb;
+                const uint64_t tail = rem > nb ? std::min<uint64_t>(rem - nb, n) : 0;
+                o.q[p].lazy_total = wraps * n + tail;
+            }
+        } else {
+            // uniform starts: create and bucket them first (createWalkers)
+            uint64_t made = 0;
+            while (made < W) {
+                uint64_t G = lazy_budget(o, -1, W - made);
+                if (G == 0) {
+                    LT_TRY(spill_until(o, (uint64_t)o.P + 2 + 1, -1));
+                    G = lazy_budget(o, -1, W - made);
+                    if (G == 0) return fail(LT_ERR_CAPACITY, "walker pool too small to create walkers");
+                }
+                LT_TRY(step_and_bucket(o, rp, -1, made, G, false));
+                made += G;
+            }
+        }
+        // Scheduler::start (src/Scheduler.h:425-438)
+        bool sync = false;
+        uint32_t p = 0;
+        SchedView v = view(o);
+        while (o.policy->next(v, o.prev_computed, sync, p)) {
+            sync = false;
+            do {
+                LT_TRY(process(o, rp, p));
+                v = view(o);
+            } while (o.policy->next(v, o.prev_computed, false, p));
+            sync = true;
+            v = view(o);
+        }
+    }
+    unsigned long long hs[8];
+    LT_CUDA_TRY(cudaMemcpyAsync(hs, o.d_stats, sizeof hs, cudaMemcpyDeviceToHost, st));
+    if (counts_out) LT_CUDA_TRY(cudaMemcpyAsync(counts_out, e->d_counts, 8ull * g.V, cudaMemcpyDeviceToHost, st));
+    if (endpoints_out) LT_CUDA_TRY(cudaMemcpyAsync(endpoints_out, e->d_endpoints, 4 * W, cudaMemcpyDeviceToHost, st));
+    if (paths_out)
+        LT_CUDA_TRY(cudaMemcpyAsync(paths_out, e->d_paths, 4 * W * ((uint64_t)length + 1), cudaMemcpyDeviceToHost, st));
+    LT_CUDA_TRY(cudaStreamSynchronize(st));
+    e->stats.updates = hs[0];
+    e->stats.moves = hs[1];
+    e->stats.teleports = hs[2];
+    e->stats.zerocopy_bytes = hs[3] * 256;  // two 128-byte host lines per zero-copy hop
+    e->stats.running_ms = now_ms() - t0;
+    return LT_OK;
+}
+
+}  // namespace lt

@@ -1,0 +1,40 @@
+// ooc.h -- out-of-core run loop: partition cache, walker queues and scheduler.
+//
+// Replaces GPUScheduler / Scheduler (src/Scheduler.h:13-454), GPUGraph
+// (src/GraphLoader.h:160-240), GPUListPool / ListPool (src/buffer/Pool.h:90-646)
+// and GPUWalkManager (src/WalkManager.h:284-421) for graphs whose partitions
+// do not all fit the device cache (-p smaller than the partition count).
+#pragma once
+
+#include <cstdint>
+#include <memory>
+#include <vector>
+
+#include "common.h"
+#include "sched.h"
+
+struct lt_engine;
+
+namespace lt {
+
+struct Queue {
+    std::vector<uint32_t> dev_chunks;   // all full except the last
+    uint32_t tail_fill = 0;             // walkers in the last device chunk
+    std::vector<uint32_t> host_chunks;  // spilled full chunks
+    uint64_t lazy_next = 0;             // walkers created so far (lazy ordinals)
+    uint64_t lazy_total = 0;
+
+    uint64_t dev_count() const;
+    uint64_t host_count() const;
+    uint64_t lazy_left() const { return lazy_total - lazy_next; }
+    uint64_t total() const { return dev_count() + host_count() + lazy_left(); }
+};
+
+struct Ooc;
+lt_status ooc_create(lt_engine *e, Ooc **out);
+void ooc_destroy(Ooc *o);
+lt_status ooc_drop_cache(Ooc *o);
+lt_status ooc_run(lt_engine *e, int app, int start, uint32_t source, uint64_t W, uint32_t length, uint32_t runs,
+                  uint32_t run_base, float prob, uint64_t *counts_out, uint32_t *endpoints_out, uint32_t *paths_out);
+
+}  // namespace lt

@@ -1,0 +1,73 @@
+// sched.cpp -- the plain (reference) and FIFO scheduling policies.
+#include "sched.h"
+
+#include <algorithm>
+
+namespace lt {
+
+bool Policy::next(const SchedView &v, int32_t prev_computed, bool sync, uint32_t &choice)
+{
+    uint64_t best = 0;
+    bool picked = false;
+    for (uint32_t i = 0; i < v.P; i++) {
+        if ((int32_t)i == prev_computed && !sync) continue;
+        if (v.waiting[i] > best) {
+            best = v.waiting[i];
+            choice = i;
+            picked = true;
+        }
+    }
+    return picked;
+}
+
+int32_t Policy::victim(const SchedView &v, int32_t except, uint32_t /*incoming*/)
+{
+    int32_t best = -1;
+    for (uint32_t i = 0; i < v.P; i++) {
+        if (v.slot_of[i] < 0 || (int32_t)i == except) continue;
+        if (best < 0 || v.waiting[i] < v.waiting[best] ||
+            (v.waiting[i] == v.waiting[best] && v.last_used[i] < v.last_used[best]))
+            best = (int32_t)i;
+    }
+    return best;
+}
+
+void Policy::prefetch_order(const SchedView &v, uint32_t exclude, std::vector<uint32_t> &out)
+{
+    out.clear();
+    for (uint32_t i = 0; i < v.P; i++)
+        if (i != exclude && v.slot_of[i] < 0 && v.waiting[i] > 0) out.push_back(i);
+    std::stable_sort(out.begin(), out.end(), [&](uint32_t a, uint32_t b) { return v.waiting[a] > v.waiting[b]; });
+}
+
+// FIFO_SCHE nextPartition (src/Scheduler.h:393-416): sweep partitions in id
+// order, returning each one that has walkers; a finished sweep returns false
+// once, after which the caller's outer loop starts the next sweep.
+bool FifoPolicy::next(const SchedView &v, int32_t /*prev*/, bool /*sync*/, uint32_t &choice)
+{
+    if (cursor_ == 0) {
+        bool any = false;
+        for (uint32_t i = 0; i < v.P && !any; i++) any = v.waiting[i] > 0;
+        if (!any) return false;
+    }
+    while (cursor_ < v.P) {
+        choice = cursor_++;
+        if (v.waiting[choice] > 0) return true;
+    }
+    cursor_ = 0;
+    return false;
+}
+
+// FIFO victim (src/Scheduler.h:177-184): the first cached partition after the
+// one loaded last, in cyclic id order.
+int32_t FifoPolicy::victim(const SchedView &v, int32_t except, uint32_t /*incoming*/)
+{
+    const uint32_t start = except < 0 ? 0 : (uint32_t)except;
+    for (uint32_t k = 1; k <= v.P; k++) {
+        const uint32_t i = (start + k) % v.P;
+        if ((int32_t)i != except && v.slot_of[i] >= 0) return (int32_t)i;
+    }
+    return -1;
+}
+
+}  // namespace lt

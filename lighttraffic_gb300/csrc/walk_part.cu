@@ -1,0 +1,369 @@
+// walk_part.cu -- step kernel for partially cached graphs and the bucketing
+// (scatter) kernel.
+//
+// Replaces randomWalkInsidePool[AllBatch] / randomWalkOutsidePool and the
+// insertToQueue kernels (src/WalkManager.h:60-282) together with the 1-thread
+// page kernels of src/buffer/Pool.h:484-528.
+//
+// Step kernel (persistent, one walker per lane, warp-aggregated refill):
+//   input  = the chunks queued for one partition, plus walkers created lazily
+//            from their ordinal (PPR source walkers, per-vertex starts);
+//   a walker keeps stepping while the partition holding its vertex is readable
+//   -- cached in a device slot, or mapped from pinned host memory for a
+//   zero-copy pass -- which generalises the reference's "walk while inside the
+//   partition" (src/WalkManager.h:239-240) to every cached partition;
+//   updates that read no graph data (the final PPR / PageRank count, PageRank
+//   teleports) run wherever the walker is;
+//   a walker whose next update needs an unreadable partition is written to a
+//   staging area (warp-aggregated slot reservation) and counted in a
+//   per-destination histogram (shared memory, flushed once per CTA).
+// Scatter kernel: appends staged walkers to their destination queues; a CTA
+// counts its tile per destination in shared memory and reserves one range per
+// destination with one global atomic (the two-level scheme of
+// src/WalkManager.h:122-190), into chunks the host allocated beforehand.
+#include "lt_core.cuh"
+#include "walk_part.h"
+
+namespace lt {
+
+namespace {
+
+constexpr unsigned kFull = 0xFFFFFFFFu;
+
+__device__ __forceinline__ uint32_t find_part(const uint32_t *off, uint32_t P, uint32_t v)
+{
+    uint32_t lo = 0, hi = P - 1;
+    while (lo < hi) {
+        const uint32_t mid = lo + (hi - lo + 1) / 2;
+        if (v < off[mid])
+            hi = mid - 1;
+        else
+            lo = mid;
+    }
+    return lo;
+}
+
+__device__ __forceinline__ uint64_t ld_u64(unsigned long long addr)
+{
+    return __ldg(reinterpret_cast<const unsigned long long *>(addr));
+}
+__device__ __forceinline__ uint32_t ld_u32(unsigned long long addr)
+{
+    return __ldg(reinterpret_cast<const unsigned int *>(addr));
+}
+
+template <int APP>
+__global__ void __launch_bounds__(kPartBlock) walk_part_kernel(StepArgs a)
+{
+    extern __shared__ uint32_t smem[];
+    const uint32_t P = a.t.P;
+    const bool in_smem = P <= kSmemPartMax;
+    uint32_t *s_off = smem;
+    uint32_t *s_hist = smem + (P + 1);
+    if (in_smem) {
+        for (uint32_t i = threadIdx.x; i <= P; i += blockDim.x) s_off[i] = a.t.node_off[i];
+        for (uint32_t i = threadIdx.x; i < P; i += blockDim.x) s_hist[i] = 0;
+    }
+    __syncthreads();
+    const uint32_t *off = in_smem ? s_off : a.t.node_off;
+    uint32_t *hist = in_smem ? s_hist : a.hist;
+
+    const int lane = threadIdx.x & 31;
+    const unsigned lt_mask = (1u << lane) - 1u;
+    const uint64_t total = a.n_chunk_walkers + a.lazy_count;
+
+    uint32_t cur = 0, step = 0, idx = 0, hop = 0;
+    bool active = false, exhausted = false;
+    // cached readable partition of the lane
+    uint32_t cp_nb = 1, cp_ne = 0;
+    unsigned long long cp_rp = 0, cp_col = 0;
+    uint64_t cp_eb = 0;
+    bool cp_zc = false;
+    uint64_t n_upd = 0, n_mov = 0, n_tel = 0, n_zc = 0, n_exit = 0, n_fin = 0;
+
+    while (true) {
+        const unsigned idle = __ballot_sync(kFull, !active);
+        if (idle != 0u && !exhausted) {
+            const int leader = __ffs(idle) - 1;
+            unsigned long long base = 0;
+            if (lane == leader) base = atomicAdd(a.next, (unsigned long long)__popc(idle));
+            base = __shfl_sync(kFull, base, leader);
+            if (base + __popc(idle) >= total) exhausted = true;
+            if (!active) {
+                const uint64_t my = base + __popc(idle & lt_mask);
+                if (my < a.n_chunk_walkers) {
+                    const uint32_t k = a.work_chunks[my / kChunk];
+                    const uint32_t j = (uint32_t)(my % kChunk);
+                    const uint32_t *c = reinterpret_cast<const uint32_t *>(a.arena + (uint64_t)k * kChunkBytes);
+                    cur = c[j];
+                    step = c[kChunk + j];
+                    idx = c[2 * kChunk + j];
+                    active = true;
+                } else if (my < total) {
+                    const uint64_t t = a.lazy_begin + (my - a.n_chunk_walkers);
+                    if (a.lazy_mode == kStartPerVertex) {
+                        const uint32_t nb = a.t.node_off[a.lazy_part];
+                        const uint32_t n = a.t.node_off[a.lazy_part + 1] - nb;
+                        idx = (uint32_t)per_vertex_id(t, nb, n, a.V);
+                        cur = nb + (uint32_t)(t % n);
+                    } else {
+                        idx = (uint32_t)t;
+                        cur = start_vertex(a.lazy_mode, a.source, a.V, a.seed, a.run, idx);
+                    }
+                    step = APP == kPPR ? ppr_length(a.seed, a.run, idx, a.thr) : a.length;
+                    if (APP == kWalk && a.paths) a.paths[(uint64_t)idx * (a.length + 1)] = cur;
+                    active = true;
+                }
+                hop = a.length - step;
+            }
+        }
+        if (__ballot_sync(kFull, active) == 0u) {
+            if (exhausted) break;
+            continue;
+        }
+
+        // Does the next update read the graph, and is the walker's partition readable?
+        Rand4 r{};
+        bool need_graph = false, emit = false;
+        uint32_t dest = 0;
+        if (active) {
+            if (APP == kPPR) {
+                need_graph = step >= 2;
+            } else if (APP == kPageRank) {
+                if (step >= 2) {
+                    r = walk_draw(a.seed, step, kTagStep, a.run, idx);
+                    need_graph = m53_of(r) < a.thr;
+                }
+            } else {
+                need_graph = true;
+            }
+            if (need_graph && (cur < cp_nb || cur >= cp_ne)) {
+                const uint32_t p = find_part(off, P, cur);
+                const unsigned long long rp = a.t.rp_addr[p];
+                if (rp == 0ull) {
+                    emit = true;
+                    dest = p;
+                } else {
+                    cp_nb = off[p];
+                    cp_ne = off[p + 1];
+                    cp_rp = rp;
+                    cp_col = a.t.col_addr[p];
+                    cp_eb = a.t.edge_off[p];
+                    cp_zc = a.t.host_mapped[p] != 0;
+                }
+            }
+        }
+        const unsigned em = __ballot_sync(kFull, emit);
+        if (em != 0u) {
+            const int leader = __ffs(em) - 1;
+            unsigned long long base = 0;
+            if (lane == leader) base = atomicAdd(a.out_n, (unsigned long long)__popc(em));
+            base = __shfl_sync(kFull, base, leader);
+            if (emit) {
+                const uint64_t pos = base + __popc(em & lt_mask);
+                a.out_cur[pos] = cur;
+                a.out_step[pos] = step;
+                a.out_idx[pos] = idx;
+                a.out_dest[pos] = dest;
+                atomicAdd(&hist[dest], 1u);
+                active = false;
+                n_exit++;
+            }
+        }
+        if (!active) continue;
+
+        const uint32_t s = step;
+        n_upd++;
+        bool done = false;
+        if (APP == kPPR) {
+            // app/ppr.cu:22-42
+            if (s == 1) {
+                atomicAdd((unsigned long long *)&a.counts[cur], 1ull);
+                done = true;
+            } else {
+                step = s - 1;
+                const uint64_t first = ld_u64(cp_rp + 8ull * (cur - cp_nb));
+                const uint64_t deg = ld_u64(cp_rp + 8ull * (cur - cp_nb + 1)) - first;
+                if (deg > 0) {
+                    const Rand4 q = walk_draw(a.seed, s, kTagStep, a.run, idx);
+                    cur = ld_u32(cp_col + 4ull * (first + mod_u64(r64_of(q), deg) - cp_eb));
+                    n_mov++;
+                    n_zc += cp_zc;
+                } else {
+                    atomicAdd((unsigned long long *)&a.counts[cur], 1ull);
+                    done = true;
+                }
+            }
+        } else if (APP == kPageRank) {
+            // app/pagerank.cu:26-44; a vertex without out-edges teleports.
+            atomicAdd((unsigned long long *)&a.counts[cur], 1ull);
+            if (s == 1) {
+                done = true;
+            } else {
+                step = s - 1;
+                const uint64_t r64 = r64_of(r);
+                bool tele = !need_graph;
+                if (!tele) {
+                    const uint64_t first = ld_u64(cp_rp + 8ull * (cur - cp_nb));
+                    const uint64_t deg = ld_u64(cp_rp + 8ull * (cur - cp_nb + 1)) - first;
+                    if (deg > 0) {
+                        cur = ld_u32(cp_col + 4ull * (first + mod_u64(r64, deg) - cp_eb));
+                        n_mov++;
+                        n_zc += cp_zc;
+                    } else {
+                        tele = true;
+                    }
+                }
+                if (tele) {
+                    cur = (uint32_t)mod_u64(r64, a.V);
+                    n_tel++;
+                }
+            }
+        } else {
+            // app/genericwalk.cu:22-32
+            const uint64_t first = ld_u64(cp_rp + 8ull * (cur - cp_nb));
+            const uint64_t deg = ld_u64(cp_rp + 8ull * (cur - cp_nb + 1)) - first;
+            uint32_t *path = a.paths ? a.paths + (uint64_t)idx * (a.length + 1) : nullptr;
+            if (deg > 0) {
+                const Rand4 q = walk_draw(a.seed, s, kTagStep, a.run, idx);
+                cur = ld_u32(cp_col + 4ull * (first + mod_u64(r64_of(q), deg) - cp_eb));
+                n_mov++;
+                n_zc += cp_zc;
+                hop++;
+                if (path) path[hop] = cur;
+                step = s - 1;
+            } else {
+                if (path)
+                    for (uint32_t h = hop + 1; h <= a.length; h++) path[h] = kInvalidNode;
+                step = 0;
+            }
+            done = step == 0;
+        }
+        if (done) {
+            active = false;
+            n_fin++;
+            if (a.endpoints) a.endpoints[idx] = cur;
+        }
+    }
+
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        n_upd += __shfl_down_sync(kFull, n_upd, o);
+        n_mov += __shfl_down_sync(kFull, n_mov, o);
+        n_tel += __shfl_down_sync(kFull, n_tel, o);
+        n_zc += __shfl_down_sync(kFull, n_zc, o);
+        n_exit += __shfl_down_sync(kFull, n_exit, o);
+        n_fin += __shfl_down_sync(kFull, n_fin, o);
+    }
+    if (lane == 0) {
+        atomicAdd(&a.stats[0], (unsigned long long)n_upd);
+        atomicAdd(&a.stats[1], (unsigned long long)n_mov);
+        atomicAdd(&a.stats[2], (unsigned long long)n_tel);
+        atomicAdd(&a.stats[3], (unsigned long long)n_zc);
+        atomicAdd(&a.stats[4], (unsigned long long)n_exit);
+        atomicAdd(&a.stats[5], (unsigned long long)n_fin);
+    }
+    if (in_smem) {
+        __syncthreads();
+        for (uint32_t i = threadIdx.x; i < P; i += blockDim.x)
+            if (s_hist[i]) atomicAdd(&a.hist[i], s_hist[i]);
+    }
+}
+
+// Tile of kScatterItems walkers per thread.
+constexpr int kScatterItems = 4;
+
+__global__ void __launch_bounds__(kPartBlock) scatter_kernel(ScatterArgs a)
+{
+    extern __shared__ uint32_t smem[];
+    const uint32_t P = a.P;
+    const bool in_smem = P <= kSmemPartMax;
+    uint32_t *s_cnt = smem;       // P: walkers of this tile per destination
+    uint32_t *s_base = smem + P;  // P: reserved base slot per destination
+    const uint64_t tile = (uint64_t)kPartBlock * kScatterItems;
+    for (uint64_t t0 = (uint64_t)blockIdx.x * tile; t0 < a.n; t0 += (uint64_t)gridDim.x * tile) {
+        uint32_t rank[kScatterItems], dest[kScatterItems];
+        if (in_smem) {
+            for (uint32_t i = threadIdx.x; i < P; i += blockDim.x) s_cnt[i] = 0;
+            __syncthreads();
+        }
+#pragma unroll
+        for (int k = 0; k < kScatterItems; k++) {
+            const uint64_t i = t0 + (uint64_t)k * kPartBlock + threadIdx.x;
+            dest[k] = 0xFFFFFFFFu;
+            if (i < a.n) {
+                dest[k] = a.in_dest[i];
+                rank[k] = in_smem ? atomicAdd(&s_cnt[dest[k]], 1u) : atomicAdd(&a.cursor[dest[k]], 1u);
+            }
+        }
+        if (in_smem) {
+            __syncthreads();
+            for (uint32_t i = threadIdx.x; i < P; i += blockDim.x)
+                if (s_cnt[i]) s_base[i] = atomicAdd(&a.cursor[i], s_cnt[i]);
+            __syncthreads();
+        }
+#pragma unroll
+        for (int k = 0; k < kScatterItems; k++) {
+            const uint64_t i = t0 + (uint64_t)k * kPartBlock + threadIdx.x;
+            if (i < a.n) {
+                const uint32_t d = dest[k];
+                const uint32_t pos = in_smem ? s_base[d] + rank[k] : rank[k];
+                const uint32_t chunk = a.plan_chunks[a.win_off[d] + pos / kChunk];
+                uint32_t *c = reinterpret_cast<uint32_t *>(a.arena + (uint64_t)chunk * kChunkBytes);
+                const uint32_t j = pos % kChunk;
+                c[j] = a.in_cur[i];
+                c[kChunk + j] = a.in_step[i];
+                c[2 * kChunk + j] = a.in_idx[i];
+            }
+        }
+        if (in_smem) __syncthreads();
+    }
+}
+
+template <int APP>
+int occ_part(size_t smem)
+{
+    int n = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, walk_part_kernel<APP>, kPartBlock, smem);
+    return n;
+}
+
+}  // namespace
+
+size_t part_smem(uint32_t P) { return P <= kSmemPartMax ? sizeof(uint32_t) * (2ull * P + 1) : 0; }
+
+int part_grid(int app, int /*start*/, int device, size_t smem)
+{
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+    int occ = app == kPPR ? occ_part<kPPR>(smem) : app == kPageRank ? occ_part<kPageRank>(smem) : occ_part<kWalk>(smem);
+    if (occ < 1) occ = 1;
+    return sms * occ;
+}
+
+cudaError_t launch_walk_part(const StepArgs &a, int app, int grid, cudaStream_t st)
+{
+    const size_t smem = part_smem(a.t.P);
+    switch (app) {
+    case kPPR: walk_part_kernel<kPPR><<<grid, kPartBlock, smem, st>>>(a); break;
+    case kPageRank: walk_part_kernel<kPageRank><<<grid, kPartBlock, smem, st>>>(a); break;
+    default: walk_part_kernel<kWalk><<<grid, kPartBlock, smem, st>>>(a); break;
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_scatter(const ScatterArgs &a, int device, cudaStream_t st)
+{
+    if (a.n == 0) return cudaSuccess;
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+    const uint64_t tile = (uint64_t)kPartBlock * kScatterItems;
+    uint64_t blocks = (a.n + tile - 1) / tile;
+    const uint64_t cap = (uint64_t)sms * 8;
+    if (blocks > cap) blocks = cap;
+    const size_t smem = a.P <= kSmemPartMax ? sizeof(uint32_t) * 2ull * a.P : 0;
+    scatter_kernel<<<(unsigned)blocks, kPartBlock, smem, st>>>(a);
+    return cudaGetLastError();
+}
+
+}  // namespace lt

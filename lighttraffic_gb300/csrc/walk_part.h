@@ -1,0 +1,82 @@
+// walk_part.h -- out-of-core step and bucketing kernels.
+//
+// Walkers wait in per-partition queues made of fixed-size chunks.  A chunk is
+// one contiguous block of kChunk walkers in structure-of-arrays form:
+//     u32 cur[kChunk] | u32 step[kChunk] | u32 idx[kChunk]
+// so a chunk moves between device and host with a single copy.  Every chunk of
+// a queue is full except its last one.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace lt {
+
+constexpr uint32_t kChunk = 8192;                         // walkers per chunk
+constexpr uint64_t kChunkBytes = 12ull * kChunk;           // 96 KiB
+constexpr int kPartBlock = 256;
+constexpr uint32_t kSmemPartMax = 8192;                    // P up to this keeps node_off / histograms in smem
+
+// Device view of the partition table: node / edge ranges of every partition
+// and, for partitions readable by the kernel (cached in a device slot, or
+// mapped from pinned host memory for a zero-copy pass), the addresses of
+// their rowptr slice (n+1 global edge offsets) and col slice.
+struct PartTable {
+    const uint32_t *node_off;             // P+1
+    const uint64_t *edge_off;             // P+1
+    const unsigned long long *rp_addr;    // P, 0 = not readable
+    const unsigned long long *col_addr;   // P
+    const uint8_t *host_mapped;           // P, 1 = the slice is read over the host link (zero-copy)
+    uint32_t P;
+};
+
+struct StepArgs {
+    PartTable t;
+    uint8_t *arena;                // chunk arena
+    const uint32_t *work_chunks;   // chunk ids of the partition being processed
+    uint64_t n_chunk_walkers;      // walkers in those chunks ((n-1) * kChunk + tail fill)
+    uint64_t lazy_begin;           // first lazy ordinal to create
+    uint64_t lazy_count;           // lazy walkers to create in this pass
+    uint32_t lazy_part;            // partition the lazy walkers start in
+    int lazy_mode;                 // lt::Start of the lazy walkers
+    uint64_t W;                    // walkers of the run (per-vertex ordinal mapping)
+    uint32_t V;
+    uint32_t source;
+    uint32_t length;
+    uint32_t run;
+    uint64_t seed;
+    uint64_t thr;
+    uint64_t *counts;
+    uint32_t *endpoints;
+    uint32_t *paths;
+    // outputs for walkers that leave the readable partitions
+    uint32_t *out_cur, *out_step, *out_idx, *out_dest;
+    unsigned long long *out_n;     // staged walkers (atomic)
+    uint32_t *hist;                // P: staged walkers per destination
+    unsigned long long *next;      // scratch: next input ordinal
+    unsigned long long *stats;     // 8: updates, moves, teleports, zc moves, exits, finished, -, -
+};
+
+struct ScatterArgs {
+    const uint32_t *in_cur, *in_step, *in_idx, *in_dest;
+    uint64_t n;
+    uint8_t *arena;
+    uint32_t *cursor;              // P: next free slot offset in the destination's chunk window
+    const uint32_t *win_off;       // P: start of the destination's window in plan_chunks
+    const uint32_t *plan_chunks;   // chunk ids of every window
+    uint32_t P;
+};
+
+int part_grid(int app, int start, int device, size_t smem);
+size_t part_smem(uint32_t P);
+cudaError_t launch_walk_part(const StepArgs &a, int app, int grid, cudaStream_t st);
+cudaError_t launch_scatter(const ScatterArgs &a, int device, cudaStream_t st);
+
+// Ordinal t of the lazily created walkers of partition [nb, ne) under the
+// per-vertex start: walkers j*V + v (v in [nb, ne)), ordered j-major.
+__host__ __device__ inline uint64_t per_vertex_id(uint64_t t, uint32_t nb, uint32_t n, uint32_t V)
+{
+    return (t / n) * (uint64_t)V + nb + (t % n);
+}
+
+}  // namespace lt
