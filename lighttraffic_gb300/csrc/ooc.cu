@@ -168,7 +168,10 @@ lt_status load_partition(Ooc &o, uint32_t p)
         }
     if (slot < 0) {
         SchedView v = view(o);
-        const int32_t victim = o.policy->victim(v, o.prev_loaded, p);
+        int32_t victim = o.policy->victim(v, o.prev_loaded, p);
+        // with a single slot the partition loaded last is the only candidate
+        // (the reference asserts here, src/Scheduler.h:169)
+        if (victim < 0) victim = o.policy->victim(v, -1, p);
         if (victim < 0) return fail(LT_ERR_CAPACITY, "no cached partition can be evicted");
         slot = o.slot_of[victim];
         LT_TRY(evict_partition(o, (uint32_t)victim));

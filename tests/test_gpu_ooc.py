@@ -1,0 +1,114 @@
+"""GPU parity of the out-of-core path (device cache smaller than the graph).
+
+The partition cache size (-p), walker budget (-b, forcing host spills),
+zero-copy threshold and scheduling policy change the schedule, never the
+result: counts, endpoints and paths must equal the oracle's bit for bit.
+"""
+import numpy as np
+import pytest
+
+import oracle
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def g16():
+    rp, col = oracle.rmat(16, 1 << 20, seed=21)
+    return rp, col
+
+
+def _eng(lt, rp, col, part_bytes, **kw):
+    g = lt.Graph.from_csr(rp, col, part_bytes)
+    return g, lt.Engine(g, **kw)
+
+
+CASES = [
+    # (partitions cached, walker budget, zero-copy threshold, scheduler)
+    (4, 0, 0, 0),            # plain, no zero-copy
+    (1, 0, 0, 0),            # a single slot
+    (4, 0, 1 << 40, 0),      # every cold partition read zero-copy
+    (4, 0, None, 0),         # default threshold partitionSize/128/2
+    (3, 20000, 0, 0),        # tiny walker pool: host spills
+    (5, 0, 0, 1),            # FIFO policy
+]
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_ppr_ooc(lt, require_gpu, g16, case):
+    K, B, zc, sched = case
+    rp, col = g16
+    g, e = _eng(lt, rp, col, 256 << 10, partitions=K, batch=B, zerocopy_threshold=zc, sched=sched, seed=9)
+    assert g.num_partitions > K
+    W = 300000
+    got = e.ppr(0, W, 0.15)
+    want, _, st = oracle.ppr(rp, col, 0, W, prob=0.15, seed=9)
+    assert (got == want).all()
+    s = e.stats()
+    assert s["moves"] == st[1]
+    assert s["iterations"] > 1
+    if zc == 0:
+        assert s["h2d_graph_bytes"] > 0 and s["zerocopy_calls"] == 0
+    if zc == 1 << 40:
+        assert s["zerocopy_calls"] > 0
+    if B:
+        assert s["d2h_walker_bytes"] > 0 and s["h2d_walker_bytes"] > 0
+
+
+@pytest.mark.parametrize("case", CASES)
+@pytest.mark.parametrize("start", [1, 2])
+def test_pagerank_ooc(lt, require_gpu, g16, case, start):
+    K, B, zc, sched = case
+    rp, col = g16
+    V = len(rp) - 1
+    g, e = _eng(lt, rp, col, 256 << 10, partitions=K, batch=B, zerocopy_threshold=zc, sched=sched, seed=4)
+    got = e.pagerank(2 * V, length=8, runs=2, start=start)
+    want, st = oracle.pagerank(rp, col, 2 * V, length=8, runs=2, seed=4, start_mode=start)
+    assert (got == want).all()
+    s = e.stats()
+    assert (s["updates"], s["moves"], s["teleports"]) == tuple(int(x) for x in st)
+
+
+@pytest.mark.parametrize("case", CASES[:3] + CASES[4:5])
+def test_walk_ooc(lt, require_gpu, g16, case):
+    K, B, zc, sched = case
+    rp, col = g16
+    V = len(rp) - 1
+    g, e = _eng(lt, rp, col, 256 << 10, partitions=K, batch=B, zerocopy_threshold=zc, sched=sched, seed=6)
+    for start in (1, 2):
+        ep, pa, _ = oracle.generic_walk(rp, col, V + 77, length=6, start_mode=start, run=1, seed=6, paths=True)
+        gep, gpa = e.walk(V + 77, length=6, run=1, start=start, paths=True)
+        assert (gep == ep).all() and (gpa == pa).all()
+
+
+def test_resident_and_ooc_agree(lt, require_gpu, g16):
+    rp, col = g16
+    V = len(rp) - 1
+    g = lt.Graph.from_csr(rp, col, 128 << 10)
+    full = lt.Engine(g, seed=3)
+    part = lt.Engine(g, partitions=2, seed=3)
+    assert (full.ppr(7, 200000, 0.2) == part.ppr(7, 200000, 0.2)).all()
+    assert (full.pagerank(3 * V, 10, start=2) == part.pagerank(3 * V, 10, start=2)).all()
+
+
+def test_repeated_runs_and_drop_cache(lt, require_gpu, g16):
+    rp, col = g16
+    g, e = _eng(lt, rp, col, 256 << 10, partitions=3, seed=12)
+    a = e.ppr(0, 100000, 0.15)
+    b = e.ppr(0, 100000, 0.15)                 # warm cache
+    e.drop_cache()
+    c = e.ppr(0, 100000, 0.15)                 # cold again
+    assert (a == b).all() and (a == c).all()
+
+
+def test_c0_ooc_full_size(lt, require_gpu):
+    """c0 graph with one 32 MiB slot for its 3+ partitions."""
+    g = lt.Graph.rmat(20, 1 << 24, seed=1, part_bytes=32 << 20)
+    rp, col = g.csr()
+    V = g.num_nodes
+    e = lt.Engine(g, partitions=1, seed=1)
+    got = e.ppr(0, 2 * V, 0.15)
+    want, _, _ = oracle.ppr(rp, col, 0, 2 * V, prob=0.15, seed=1)
+    assert (got == want).all()
+    s = e.stats()
+    assert s["partition_loads"] >= 2
