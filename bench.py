@@ -1,26 +1,28 @@
 #!/usr/bin/env python3
 """Benchmark of the random-walk hot path on GB300.
 
-    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference] [--config c1|c0]
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference] [--config c2|c1|c0]
 
-One "step" is one full pass of the app over its workload:
-  c1 (default): walk-based PageRank on RMAT(2^23 vertices, 2^27 edges, a/b/c/d =
-      .57/.19/.19/.05, seed 1, isolated vertices removed), 32 MiB partitions all
-      cached in HBM, W = 2|V| walkers starting one per vertex (walker i at vertex
-      i mod V), l = 10, teleport when U > 0.85 -> W * l walk steps per pass.
-  c0: PPR on RMAT(2^20, 2^24), source 0, W = 2|V|, stop probability 0.15; steps
-      are the hops taken (the reference's 2|V|/0.15 estimate, counted exactly).
-Synthetic inputs stand in for the reference's datasets (absent, no network).
-
-value  : device-resident passes through lt_walk_device (graph already in HBM,
-         counters zeroed inside each pass), CUDA events on the launching stream.
-e2e    : the public API call lt_run_pagerank / lt_run_ppr with host buffers; each
-         step drops the device cache first, so the timed region holds the H2D
-         copy of every partition (pinned host memory) and the D2H of the counts.
-Graph inputs (576 MiB for c1) exceed the 129 MB L2, so no flush is needed
-between passes.
+Workloads (synthetic RMAT graphs, a=.57 b=.19 c=.19 d=.05, seed 1, isolated
+vertices removed, stand in for the reference's datasets, which are absent):
+  c2 (default): out-of-core PPR -- RMAT(2^30 vertices, 2^33 edges), 32 MiB
+      partitions in pinned host memory, 256 cached on the device (-p 256,
+      8 GiB), walker pool 2^28 (-b), W = 2|V| walks from source 0, stop
+      probability 0.15.  One step = one full run from a cold device cache,
+      through the public API (lt_run_ppr with a pinned host count buffer):
+      every partition load, zero-copy read and walker spill is inside the
+      timed region.  `value` is the learned scheduler; the plain (reference)
+      scheduler is timed beside it under "plain".
+  c1: walk-based PageRank on RMAT(2^23, 2^27) resident in HBM (32 MiB
+      partitions all cached), 2|V| walkers one per vertex, l = 10, teleport
+      when U > 0.85; `value` times lt_walk_device passes on device buffers,
+      `e2e` the public API with the graph re-copied from pinned host memory.
+  c0: PPR on RMAT(2^20, 2^24) resident in HBM, source 0, W = 2|V|.
+Steps per run: hops taken (PPR, the reference's 2|V|/0.15 estimate counted
+exactly) or updates (PageRank, W * l).
 --impl reference times the CPU restatement of the reference walk semantics
-(oracle/, OpenMP over all host cores) on a bounded sample of the same workload.
+(oracle/, OpenMP over all host cores) on a bounded sample of the same
+workload; the c2 input graph for it is made by the GPU generator.
 """
 from __future__ import annotations
 
@@ -40,6 +42,8 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 CONFIGS = {
+    "c2": dict(workload="ppr-rmat30-e33-outofcore-p256-b2^28", app=0, scale=30, edges=1 << 33, length=0,
+               start=0, prob=0.15, part_mb=32, partitions=256, batch=1 << 28),
     "c1": dict(workload="pagerank-rmat23-e27-resident", app=1, scale=23, edges=1 << 27, length=10,
                start=2, prob=0.85, part_mb=32),
     "c0": dict(workload="ppr-rmat20-e24-resident", app=0, scale=20, edges=1 << 24, length=0,
@@ -52,10 +56,10 @@ SEED_WALK = 1
 def parse():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
-    p.add_argument("--steps", type=int, default=50)
-    p.add_argument("--warmup", type=int, default=5)
+    p.add_argument("--steps", type=int, default=3)
+    p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    p.add_argument("--config", default="c1", choices=sorted(CONFIGS))
+    p.add_argument("--config", default="c2", choices=sorted(CONFIGS))
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--cpu-seconds", type=float, default=12.0,
                    help="target CPU time of the cpu_baseline sample")
@@ -63,10 +67,8 @@ def parse():
 
 
 def dist_env():
-    ws = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    return ws, rank, local
+    return (int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("RANK", "0")),
+            int(os.environ.get("LOCAL_RANK", "0")))
 
 
 # ------------------------------------------------------------- clocks
@@ -103,11 +105,11 @@ class ClockSampler:
             except subprocess.TimeoutExpired:
                 self.proc.kill()
 
-    def summary(self, t0=None, t1=None):
+    def summary(self, t0, t1):
         sm, mx, reasons = [], None, set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         for t, line in self.lines:
-            if t0 is not None and (t < t0 or t > t1):
+            if t < t0 or t > t1:
                 continue
             parts = [x.strip() for x in line.split(",")]
             if len(parts) < 9:
@@ -120,17 +122,31 @@ class ClockSampler:
             for n, v in zip(names, parts[5:9]):
                 if v.lower().startswith("active"):
                     reasons.add(n)
-        if not sm:
-            return {"sm_mhz": None, "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": 0}
-        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons),
-                "samples": len(sm)}
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sm)}
 
 
-# ---------------------------------------------------------- reference arm
+def measured_peak(key, fallback):
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            return float(json.load(f)[key]), "measured"
+    return fallback, "fallback"
+
+
+def profiled_traffic(workload):
+    path = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            return json.load(f).get(workload)
+    return None
+
+
+# ---------------------------------------------------------- CPU oracle
 
 def cpu_rate(cfg, rp, col, seconds, threads):
-    """Oracle (CPU restatement of the reference semantics) on a bounded sample;
-    returns (steps/s, sample description, threads)."""
+    """Oracle (CPU restatement of the reference semantics) on a bounded
+    sample: the first n walkers of the run.  Returns (steps/s, description)."""
     import oracle
     V = len(rp) - 1
     W = 2 * V
@@ -152,47 +168,48 @@ def cpu_rate(cfg, rp, col, seconds, threads):
     if n2 > n:
         steps, dt = run(n2)
         n = n2
-    return steps / dt, f"first {n} of {W} walkers ({steps} steps, {dt:.1f} s)", threads
-
-
-def host_graph(cfg):
-    """The same RMAT graph on the host, from the oracle's generator (identical bytes)."""
-    import oracle
-    return oracle.rmat(cfg["scale"], cfg["edges"], seed=SEED_GRAPH)
+    return steps / dt, f"first {n} of {W} walkers ({steps} steps, {dt:.1f} s)"
 
 
 def reference_arm(args, cfg):
-    ws, rank, _ = dist_env()
+    ws, rank, local = dist_env()
     if rank != 0:
         return 0
-    rp, col = host_graph(cfg)
     threads = os.cpu_count() or 1
+    if cfg["scale"] >= 26:
+        # input graph only: the oracle's CPU generator would take tens of minutes
+        import lighttraffic_gb300 as lt
+        g = lt.Graph.rmat(cfg["scale"], cfg["edges"], seed=SEED_GRAPH, part_bytes=cfg["part_mb"] << 20,
+                          device=local)
+        rp, col = g.csr_views()
+    else:
+        import oracle
+        g = None
+        rp, col = oracle.rmat(cfg["scale"], cfg["edges"], seed=SEED_GRAPH)
     per_step = max(1.0, min(6.0, 150.0 / max(1, args.steps + args.warmup)))
-    rates = []
-    desc = ""
+    rates, desc = [], ""
     for i in range(args.warmup + args.steps):
-        r, desc, _ = cpu_rate(cfg, rp, col, per_step, threads)
+        r, desc = cpu_rate(cfg, rp, col, per_step, threads)
         if i >= args.warmup:
             rates.append(r)
     value = statistics.median(rates)
     line = {
         "impl": "reference", "metric": "walk steps/s", "value": value, "unit": "steps/s",
-        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": None, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "u64", "data": "synthetic RMAT (seeded), stand-in for the reference datasets",
-        "config": {"workload": cfg["workload"], "V": len(rp) - 1, "E": len(col),
-                   "walkers": 2 * (len(rp) - 1), "length": cfg["length"]},
-        "cpu_baseline": {"value": value, "unit": "steps/s", "cores": threads, "kind": "port",
-                         "sample": desc},
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": None,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64",
+        "data": "synthetic RMAT (seeded), stand-in for the reference datasets",
+        "config": {"workload": cfg["workload"], "V": len(rp) - 1, "E": len(col), "walkers": 2 * (len(rp) - 1)},
+        "cpu_baseline": {"value": value, "unit": "steps/s", "cores": threads, "kind": "port", "sample": desc},
         "e2e": {"value": value, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
+    del g
     return 0
 
 
 # ------------------------------------------------------------ GB300 arm
 
-def gb300_arm(args, cfg):
+def init_dist():
     import torch
     ws, rank, local = dist_env()
     dist = None
@@ -200,24 +217,163 @@ def gb300_arm(args, cfg):
         import torch.distributed as dist
         dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
     torch.cuda.set_device(local)
+    return ws, rank, local, dist
+
+
+def max_over_ranks(dist, local, x):
+    if not dist:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64, device=f"cuda:{local}")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def host_link_peak(local):
+    """Pinned host -> device copy bandwidth, best of 5 (GB/s)."""
+    import torch
+    n = 1 << 30
+    src = torch.empty(n, dtype=torch.uint8, pin_memory=True)
+    dst = torch.empty(n, dtype=torch.uint8, device=f"cuda:{local}")
+    best = 0.0
+    for _ in range(5):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        dst.copy_(src, non_blocking=True)
+        b.record()
+        torch.cuda.synchronize()
+        best = max(best, n / (a.elapsed_time(b) / 1e3) / 1e9)
+    del src, dst
+    return best
+
+
+def link_bytes(s):
+    return s["h2d_graph_bytes"] + s["h2d_walker_bytes"] + s["d2h_walker_bytes"] + s["zerocopy_bytes"]
+
+
+def gb300_ooc(args, cfg):
+    import torch
+    ws, rank, local, dist = init_dist()
     import lighttraffic_gb300 as lt
 
-    g = lt.Graph.rmat(cfg["scale"], cfg["edges"], seed=SEED_GRAPH, part_bytes=cfg["part_mb"] << 20,
-                      device=local)
+    g = lt.Graph.rmat(cfg["scale"], cfg["edges"], seed=SEED_GRAPH, part_bytes=cfg["part_mb"] << 20, device=local)
+    V, E = g.num_nodes, g.num_edges
+    W = 2 * V
+    link_peak = host_link_peak(local)
+    counts = torch.empty(V, dtype=torch.int64, pin_memory=True).numpy().view(np.uint64)
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.3)
+    wall0 = time.time()
+    # both engines live side by side and their runs alternate, so drift on
+    # the box (or order effects) hits both schedulers alike
+    engines = {name: lt.Engine(g, partitions=cfg["partitions"], batch=cfg["batch"], seed=SEED_WALK, sched=sched,
+                               device=local)
+               for name, sched in [("learned", lt.SCHED_LEARNED), ("plain", lt.SCHED_PLAIN)]}
+    for _ in range(args.warmup):
+        for e in engines.values():
+            e.drop_cache()
+            e.ppr(0, W, cfg["prob"], out=counts)
+    if dist:
+        dist.barrier()
+    times = {name: [] for name in engines}
+    stats = {}
+    for _ in range(args.steps):
+        for name, e in engines.items():
+            e.drop_cache()
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            e.ppr(0, W, cfg["prob"], out=counts)
+            t1 = time.perf_counter()
+            assert int(counts.sum()) == W, "PPR invariant (one count per walk) violated"
+            times[name].append(t1 - t0)
+            stats[name] = e.stats()
+    results = {}
+    for name, e in engines.items():
+        s = stats[name]
+        results[name] = {"elapsed": max_over_ranks(dist, local, sum(times[name])), "stats": s,
+                         "policy": e.policy_stats(), "steps": s["moves"], "times": times[name]}
+        e.close()
+    clocks.stop()
+    clk = clocks.summary(wall0 - 0.5, time.time())
+    if rank != 0:
+        if dist:
+            dist.destroy_process_group()
+        return 0
+    L, Pn = results["learned"], results["plain"]
+    value = L["steps"] * args.steps * ws / L["elapsed"]
+    plain_value = Pn["steps"] * args.steps * ws / Pn["elapsed"]
+    s = L["stats"]
+    launches = s["computing_calls"] + s["zerocopy_calls"]
+    # step kernel: 20 B per hop (rowptr pair + col), 16 B per count (one per
+    # walk), 48 B per hand-off (walker read + staged write + scatter read +
+    # queue write, 12 B each)
+    alg = 20 * s["moves"] + 16 * W + 48 * s["handoffs"]
+    kern_s = max(s["step_kernel_ms"], 1e-6) / 1e3
+    peak, peak_src = measured_peak("hbm_gbs", 6800.0)
+    achieved = alg / kern_s / 1e9
+    line = {
+        "metric": "walk steps/s", "value": value, "unit": "steps/s", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": L["elapsed"] / args.steps * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "u64",
+        "data": "synthetic RMAT (seeded), stand-in for the reference datasets",
+        "config": {"workload": cfg["workload"], "V": V, "E": E, "partitions": g.num_partitions,
+                   "cached_partitions": cfg["partitions"], "walker_pool": cfg["batch"], "walkers": W,
+                   "prob": cfg["prob"], "scheduler": "learned",
+                   "l2": "graph (%d GiB) in host memory, far larger than L2; cache dropped before every step"
+                         % ((8 * (V + 1) + 4 * E) >> 30),
+                   "parallelism": "replicas" if ws > 1 else "1 GPU"},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": profiled_traffic(cfg["workload"]), "kernel": "walk_part_kernel",
+                     "alg_bytes_per_launch": alg / max(1, launches),
+                     "mean_launch_ms": s["step_kernel_ms"] / max(1, launches), "launches": launches,
+                     "peak_source": peak_src},
+        "host_link": {"bytes_per_step": link_bytes(s) / s["moves"], "achieved_gbs": link_bytes(s) / (L["elapsed"] / args.steps) / 1e9,
+                      "peak_gbs": link_peak, "peak_source": "measured pinned H2D copy in this run",
+                      "zerocopy_bytes_model": "256 B per zero-copy hop (two 128 B host lines)"},
+        "plain": {"value": plain_value, "bytes_per_step": link_bytes(Pn["stats"]) / Pn["steps"],
+                  "iterations": Pn["stats"]["iterations"], "partition_loads": Pn["stats"]["partition_loads"],
+                  "ms_per_step": Pn["elapsed"] / args.steps * 1e3, "step_s": Pn["times"]},
+        "learned": {"value": value, "bytes_per_step": link_bytes(s) / s["moves"], "iterations": s["iterations"],
+                    "partition_loads": s["partition_loads"], "policy": L["policy"], "step_s": L["times"]},
+        "learned_over_plain": {"steps_per_s": value / plain_value,
+                               "bytes_per_step": (link_bytes(s) / s["moves"]) / (link_bytes(Pn["stats"]) / Pn["steps"])},
+        "e2e": {"value": value, "unit": "steps/s", "h2d_bytes_per_step": s["h2d_graph_bytes"] + s["h2d_walker_bytes"],
+                "d2h_bytes_per_step": 8 * V + s["d2h_walker_bytes"],
+                "note": "each step is a full run through lt_run_ppr from a cold cache with host output buffers"},
+        "gpu_launches": s["kernel_launches"] * args.steps,
+        "clocks": clk,
+    }
+    if not args.no_cpu_baseline and ws == 1:
+        rp, col = g.csr_views()
+        r, desc = cpu_rate(cfg, rp, col, args.cpu_seconds, os.cpu_count() or 1)
+        line["cpu_baseline"] = {"value": r, "unit": "steps/s", "cores": os.cpu_count() or 1, "kind": "port",
+                                "sample": desc}
+    print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
+def gb300_resident(args, cfg):
+    import torch
+    ws, rank, local, dist = init_dist()
+    import lighttraffic_gb300 as lt
+
+    g = lt.Graph.rmat(cfg["scale"], cfg["edges"], seed=SEED_GRAPH, part_bytes=cfg["part_mb"] << 20, device=local)
     rp, col = g.csr()
     V, E = g.num_nodes, g.num_edges
     W = 2 * V
-    d_rp = torch.from_numpy(rp.view(np.int64)).to(f"cuda:{local}")
-    d_col = torch.from_numpy(col.view(np.int32)).to(f"cuda:{local}")
-    d_cnt = torch.zeros(V, dtype=torch.int64, device=f"cuda:{local}")
-    d_scr = torch.zeros(max(1, lt.lib.lt_walk_scratch_bytes() // 8), dtype=torch.int64,
-                        device=f"cuda:{local}")
-    d_st = torch.zeros(3, dtype=torch.int64, device=f"cuda:{local}")
+    dev = f"cuda:{local}"
+    d_rp = torch.from_numpy(rp.view(np.int64)).to(dev)
+    d_col = torch.from_numpy(col.view(np.int32)).to(dev)
+    d_cnt = torch.zeros(V, dtype=torch.int64, device=dev)
+    d_scr = torch.zeros(max(1, lt.lib.lt_walk_scratch_bytes() // 8), dtype=torch.int64, device=dev)
+    d_st = torch.zeros(3, dtype=torch.int64, device=dev)
     stream = torch.cuda.current_stream()
     app, start, length, prob = cfg["app"], cfg["start"], cfg["length"], cfg["prob"]
 
-    def one_pass():
-        d_cnt.zero_()
+    def launch():
         lt.check(lt.lib.lt_walk_device(app, start, d_rp.data_ptr(), d_col.data_ptr(), V, 0, W, length,
                                        ctypes.c_float(prob), 0, SEED_WALK, d_cnt.data_ptr(), None, None,
                                        d_scr.data_ptr(), d_st.data_ptr(), stream.cuda_stream))
@@ -226,7 +382,8 @@ def gb300_arm(args, cfg):
     clocks.start()
     time.sleep(0.3)
     for _ in range(args.warmup):
-        one_pass()
+        d_cnt.zero_()
+        launch()
     torch.cuda.synchronize()
     d_st.zero_()
     starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
@@ -240,53 +397,27 @@ def gb300_arm(args, cfg):
     for i in range(args.steps):
         d_cnt.zero_()
         starts[i].record()
-        lt.check(lt.lib.lt_walk_device(app, start, d_rp.data_ptr(), d_col.data_ptr(), V, 0, W, length,
-                                       ctypes.c_float(prob), 0, SEED_WALK, d_cnt.data_ptr(), None, None,
-                                       d_scr.data_ptr(), d_st.data_ptr(), stream.cuda_stream))
+        launch()
         ends[i].record()
     t_all1.record()
     torch.cuda.synchronize()
-    wall1 = time.time()
-    if dist:
-        dist.barrier()
-    elapsed_ms = t_all0.elapsed_time(t_all1)
-    kern_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+    elapsed_ms = max_over_ranks(dist, local, t_all0.elapsed_time(t_all1))
+    kern_ms = [a.elapsed_time(b) for a, b in zip(starts, ends)]
     st = d_st.cpu().numpy().astype(np.uint64) // np.uint64(args.steps)
     updates, moves, tele = (int(x) for x in st)
     steps_per_pass = updates if app == 1 else moves
-    # correctness of the timed passes: Σ counts is the reference's invariant
     total = int(d_cnt.sum().item())
     assert total == (W * length if app == 1 else W), "invariant violated in the timed pass"
-    if dist:
-        t = torch.tensor([elapsed_ms], device=f"cuda:{local}")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        elapsed_ms = float(t.item())
     value = steps_per_pass * args.steps * ws / (elapsed_ms / 1e3)
-
-    # roofline of the step kernel: algorithmic bytes per launch / mean launch time
-    # 20 B per graph hop (rowptr[c], rowptr[c+1], col[e]) + 16 B per counter update
-    # (u64 read + write); PageRank counts every update, PPR once per walk.
     counter_updates = updates if app == 1 else W
     alg_bytes = 20 * moves + 16 * counter_updates
     mean_kern_s = statistics.mean(kern_ms) / 1e3
-    peaks_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
-    peak, peak_src = 6800.0, "fallback"
-    if os.path.exists(peaks_path):
-        with open(peaks_path) as f:
-            peak = float(json.load(f)["hbm_gbs"])
-        peak_src = "measured"
+    peak, peak_src = measured_peak("hbm_gbs", 6800.0)
     achieved = alg_bytes / mean_kern_s / 1e9
-    traffic = None
-    tpath = os.path.join(ROOT, "profiles", "traffic.json")
-    if os.path.exists(tpath):
-        with open(tpath) as f:
-            traffic = json.load(f).get(cfg["workload"])
 
-    # e2e through the public API with host buffers
     eng = lt.Engine(g, seed=SEED_WALK, device=local)
     host_counts = torch.empty(V, dtype=torch.int64, pin_memory=True).numpy().view(np.uint64)
-    e2e_times = []
-    h2d = 0
+    e2e_times, h2d = [], 0
     for i in range(args.warmup + max(3, min(args.steps, 10))):
         eng.drop_cache()
         t0 = time.perf_counter()
@@ -299,36 +430,34 @@ def gb300_arm(args, cfg):
             e2e_times.append(t1 - t0)
             h2d = eng.stats()["h2d_graph_bytes"]
     e2e_s = statistics.mean(e2e_times)
-    e2e_value = steps_per_pass * ws / e2e_s
     clocks.stop()
     clk = clocks.summary(wall0 - 0.5, time.time())
-
     if rank != 0:
         if dist:
             dist.destroy_process_group()
         return 0
     line = {
-        "metric": "walk steps/s", "value": value, "unit": "steps/s", "n_gpus": ws,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": elapsed_ms / args.steps,
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64",
+        "metric": "walk steps/s", "value": value, "unit": "steps/s", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": elapsed_ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "u64",
         "data": "synthetic RMAT (seeded), stand-in for the reference datasets",
-        "config": {"workload": cfg["workload"], "V": V, "E": E, "partitions": g.num_partitions,
-                   "walkers": W, "length": length, "steps_per_pass": steps_per_pass,
+        "config": {"workload": cfg["workload"], "V": V, "E": E, "partitions": g.num_partitions, "walkers": W,
+                   "length": length, "steps_per_pass": steps_per_pass,
                    "l2": "inputs larger than L2 (graph %d MiB > 129 MB L2), no flush" % ((8 * (V + 1) + 4 * E) >> 20),
                    "parallelism": "replicas" if ws > 1 else "1 GPU"},
-        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "traffic": traffic,
-                     "kernel": "walk_whole_kernel", "alg_bytes_per_launch": alg_bytes,
-                     "mean_launch_ms": mean_kern_s * 1e3, "peak_source": peak_src},
-        "e2e": {"value": e2e_value, "unit": "steps/s", "h2d_bytes_per_step": h2d,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": profiled_traffic(cfg["workload"]), "kernel": "walk_whole_kernel",
+                     "alg_bytes_per_launch": alg_bytes, "mean_launch_ms": mean_kern_s * 1e3,
+                     "peak_source": peak_src},
+        "e2e": {"value": steps_per_pass * ws / e2e_s, "unit": "steps/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": 8 * V, "ms_per_step": e2e_s * 1e3},
         "gpu_launches": args.steps,
         "clocks": clk,
         "stats_per_pass": {"updates": updates, "moves": moves, "teleports": tele},
     }
     if not args.no_cpu_baseline and ws == 1:
-        r, desc, threads = cpu_rate(cfg, rp, col, args.cpu_seconds, os.cpu_count() or 1)
-        line["cpu_baseline"] = {"value": r, "unit": "steps/s", "cores": threads, "kind": "port",
+        r, desc = cpu_rate(cfg, rp, col, args.cpu_seconds, os.cpu_count() or 1)
+        line["cpu_baseline"] = {"value": r, "unit": "steps/s", "cores": os.cpu_count() or 1, "kind": "port",
                                 "sample": desc}
     print(json.dumps(line), flush=True)
     if dist:
@@ -341,7 +470,9 @@ def main():
     cfg = CONFIGS[args.config]
     if args.impl == "reference":
         return reference_arm(args, cfg)
-    return gb300_arm(args, cfg)
+    if "partitions" in cfg:
+        return gb300_ooc(args, cfg)
+    return gb300_resident(args, cfg)
 
 
 if __name__ == "__main__":

@@ -53,7 +53,11 @@ typedef enum lt_app { LT_APP_PPR = 0, LT_APP_PAGERANK = 1, LT_APP_WALK = 2 } lt_
  * PER_VERTEX: walker i starts at vertex i mod V. */
 typedef enum lt_start { LT_START_SOURCE = 0, LT_START_UNIFORM = 1, LT_START_PER_VERTEX = 2 } lt_start;
 
-typedef enum lt_sched { LT_SCHED_PLAIN = 0, LT_SCHED_FIFO = 1, LT_SCHED_LEARNED = 2 } lt_sched;
+/* PLAIN: the reference policy (src/Scheduler.h:84-171, :243-252, :368-388);
+ * FIFO: its FIFO_SCHE variant (:113-127, :391-418); LEARNED: partitions scored
+ * by the visits the online-trained prefetcher network predicts; FREQUENCY: the
+ * same decisions scored by a moving average of visits (ablation). */
+typedef enum lt_sched { LT_SCHED_PLAIN = 0, LT_SCHED_FIFO = 1, LT_SCHED_LEARNED = 2, LT_SCHED_FREQUENCY = 3 } lt_sched;
 
 typedef struct lt_graph lt_graph;
 typedef struct lt_engine lt_engine;
@@ -104,6 +108,7 @@ typedef struct lt_stats {
     uint64_t walker_loading_calls;
     uint64_t walker_evicting_calls;
     double step_kernel_ms;    /* CUDA-event time of the step kernels of the last run */
+    uint64_t handoffs;        /* walkers staged and bucketed into another partition's queue */
 } lt_stats;
 
 const char *lt_strerror(lt_status s);
@@ -220,6 +225,30 @@ lt_status lt_walk_device_noalloc(int app, int start_mode, const uint64_t *d_rowp
                                  uint32_t length, float prob, uint32_t run, uint64_t seed,
                                  uint64_t *d_counts, uint32_t *d_endpoints, uint32_t *d_paths,
                                  uint64_t *d_stats, void *stream);
+
+/* ------------------------------------------------------ learned prefetcher */
+
+typedef struct lt_policy_stats {
+    char name[16];          /* "plain", "fifo", "learned", "frequency" */
+    uint64_t train_steps;   /* SGD steps taken by the prefetcher network */
+    double net_loss;        /* mean squared error of the network on the last half of its training batches */
+    double baseline_loss;   /* the same for the moving-average predictor on those batches */
+    uint64_t predictions;   /* prediction passes consumed by the policy */
+} lt_policy_stats;
+
+/* Scheduling-policy statistics of the engine's last out-of-core runs.  No
+ * counterpart in the reference. */
+lt_status lt_engine_policy_stats(const lt_engine *e, lt_policy_stats *out);
+
+/* Forward and backward pass (and, when lr > 0, one SGD-with-momentum step) of
+ * the learned prefetcher's network on caller data, on `device`: a 2-layer FP32
+ * MLP with 16 inputs, 64 ReLU units and one output, mean squared error loss.
+ * params / grad_out / params_out use the layout W1[i*64+j] | b1[64] | W2[64] |
+ * b2 (1153 floats); x is n*16, y / pred_out are n.  No counterpart in the
+ * reference (its scheduler has no learned component); exposed so the kernels
+ * can be checked against a CPU implementation. */
+lt_status lt_mlp_check(int device, uint32_t n, const float *x, const float *y, const float *params, float lr,
+                       float momentum, float *pred_out, float *grad_out, float *loss_out, float *params_out);
 
 #ifdef __cplusplus
 }

@@ -25,7 +25,7 @@ BIN_DIR = os.path.join(PKG, "bin")
 
 APP_PPR, APP_PAGERANK, APP_WALK = 0, 1, 2
 START_SOURCE, START_UNIFORM, START_PER_VERTEX = 0, 1, 2
-SCHED_PLAIN, SCHED_FIFO, SCHED_LEARNED = 0, 1, 2
+SCHED_PLAIN, SCHED_FIFO, SCHED_LEARNED, SCHED_FREQUENCY = 0, 1, 2, 3
 INVALID_NODE = 0xFFFFFFFF
 
 STATUS = {0: "LT_OK", 1: "LT_ERR_INVALID", 2: "LT_ERR_IO", 3: "LT_ERR_FORMAT", 4: "LT_ERR_NOMEM",
@@ -52,6 +52,11 @@ class EngineCfg(C.Structure):
                 ("ctas_per_sm", C.c_int)]
 
 
+class PolicyStats(C.Structure):
+    _fields_ = [("name", C.c_char * 16), ("train_steps", C.c_uint64), ("net_loss", C.c_double),
+                ("baseline_loss", C.c_double), ("predictions", C.c_uint64)]
+
+
 class Stats(C.Structure):
     _fields_ = [("updates", C.c_uint64), ("moves", C.c_uint64), ("teleports", C.c_uint64),
                 ("iterations", C.c_uint64), ("explicit_iterations", C.c_uint64),
@@ -63,7 +68,8 @@ class Stats(C.Structure):
                 ("walker_loading_ms", C.c_double), ("walker_evicting_ms", C.c_double),
                 ("graph_loading_calls", C.c_uint64), ("computing_calls", C.c_uint64),
                 ("zerocopy_calls", C.c_uint64), ("walker_loading_calls", C.c_uint64),
-                ("walker_evicting_calls", C.c_uint64), ("step_kernel_ms", C.c_double)]
+                ("walker_evicting_calls", C.c_uint64), ("step_kernel_ms", C.c_double),
+                ("handoffs", C.c_uint64)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -99,6 +105,10 @@ def _load():
         "lt_run_walk": ([vp, C.c_uint64, C.c_uint32, C.c_uint32, C.c_int, u32p, u32p], C.c_int),
         "lt_engine_stats": ([vp, C.POINTER(Stats)], C.c_int),
         "lt_walk_scratch_bytes": ([], C.c_size_t),
+        "lt_engine_policy_stats": ([vp, C.POINTER(PolicyStats)], C.c_int),
+        "lt_mlp_check": ([C.c_int, C.c_uint32, C.POINTER(C.c_float), C.POINTER(C.c_float),
+                          C.POINTER(C.c_float), C.c_float, C.c_float, C.POINTER(C.c_float),
+                          C.POINTER(C.c_float), C.POINTER(C.c_float), C.POINTER(C.c_float)], C.c_int),
         "lt_walk_device": ([C.c_int, C.c_int, vp, vp, C.c_uint32, C.c_uint32, C.c_uint64, C.c_uint32,
                             C.c_float, C.c_uint32, C.c_uint64, vp, vp, vp, vp, vp, vp], C.c_int),
     }
@@ -132,6 +142,27 @@ def partition_equal_size(rowptr, max_bytes: int):
     check(lib.lt_partition_equal_size(_ptr(rowptr, C.c_uint64), V, max_bytes, _ptr(no, C.c_uint32),
                                       _ptr(eo, C.c_uint64), cap, C.byref(P)))
     return no[: P.value + 1].copy(), eo[: P.value + 1].copy()
+
+
+MLP_PARAMS = 16 * 64 + 2 * 64 + 1
+
+
+def mlp_check(x, y, params, lr=0.0, momentum=0.0, device=0):
+    """Forward + backward (+ one SGD step when lr > 0) of the prefetcher
+    network on the GPU.  Returns (pred, grad, loss, new_params)."""
+    x = np.ascontiguousarray(x, np.float32)
+    y = np.ascontiguousarray(y, np.float32)
+    params = np.ascontiguousarray(params, np.float32)
+    n = len(y)
+    pred = np.zeros(n, np.float32)
+    grad = np.zeros(MLP_PARAMS, np.float32)
+    newp = np.zeros(MLP_PARAMS, np.float32)
+    loss = C.c_float(0)
+    f = C.POINTER(C.c_float)
+    check(lib.lt_mlp_check(device, n, x.ctypes.data_as(f), y.ctypes.data_as(f), params.ctypes.data_as(f),
+                           lr, momentum, pred.ctypes.data_as(f), grad.ctypes.data_as(f), C.byref(loss),
+                           newp.ctypes.data_as(f)))
+    return pred, grad, loss.value, newp
 
 
 class Graph:
@@ -184,6 +215,14 @@ class Graph:
         eo = np.zeros(P + 1, dtype=np.uint64)
         check(lib.lt_graph_partitions(self._h, _ptr(no, C.c_uint32), _ptr(eo, C.c_uint64)))
         return no, eo
+
+    def csr_views(self):
+        """(rowptr, col) as numpy views of the graph's host memory (no copy;
+        valid while the graph is open)."""
+        rp, cl = C.POINTER(C.c_uint64)(), C.POINTER(C.c_uint32)()
+        check(lib.lt_graph_csr(self._h, C.byref(rp), C.byref(cl)))
+        V, E = self.num_nodes, self.num_edges
+        return (np.ctypeslib.as_array(rp, shape=(V + 1,)), np.ctypeslib.as_array(cl, shape=(E,)))
 
     def csr(self):
         """Copies of (rowptr, col)."""
@@ -254,6 +293,12 @@ class Engine:
         check(lib.lt_run_walk(self._h, walkers, length, run, start, _ptr(ep, C.c_uint32),
                               _ptr(pa, C.c_uint32)))
         return ep, pa
+
+    def policy_stats(self) -> dict:
+        s = PolicyStats()
+        check(lib.lt_engine_policy_stats(self._h, C.byref(s)))
+        return {"name": s.name.decode(), "train_steps": s.train_steps, "net_loss": s.net_loss,
+                "baseline_loss": s.baseline_loss, "predictions": s.predictions}
 
     def drop_cache(self):
         check(lib.lt_engine_drop_cache(self._h))

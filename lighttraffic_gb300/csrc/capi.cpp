@@ -233,6 +233,18 @@ lt_status lt_engine_stats(const lt_engine *e, lt_stats *out)
     return LT_OK;
 }
 
+lt_status lt_engine_policy_stats(const lt_engine *e, lt_policy_stats *out)
+{
+    if (!e || !out) return fail(LT_ERR_INVALID, "null argument");
+    std::memset(out, 0, sizeof *out);
+    if (!e->ooc) {
+        std::strncpy(out->name, "resident", sizeof out->name - 1);
+        return LT_OK;
+    }
+    ooc_policy_stats(e->ooc, *out);
+    return LT_OK;
+}
+
 size_t lt_walk_scratch_bytes(void) { return walk_scratch_bytes(); }
 
 lt_status lt_walk_device(int app, int start_mode, const uint64_t *d_rowptr, const uint32_t *d_col, uint32_t num_nodes,

@@ -3,14 +3,18 @@
 // One iteration (GPUScheduler::run, src/Scheduler.h:311-330):
 //   1. the policy picks partition p;
 //   2. p is made readable: loaded into a cache slot (evicting the policy's
-//      victim) or, below the zero-copy threshold, mapped from pinned host
-//      memory (zeroCopyCompute, :254-273);
+//      victim) or, below the zero-copy threshold, read from pinned host memory
+//      over the host link (zeroCopyCompute, :254-273);
 //   3. p's spilled walkers come back from the host (walkerLoadingPhase,
 //      :215-233), evicting other partitions' walkers to the host if the
 //      device pool is short (handleWalkerPoolOverflow, :59-82);
-//   4. one step-kernel launch drains p's queue (and creates the walkers that
+//   4. the policy may start loading partitions it expects to need next into
+//      free or evictable slots; the copies overlap the step kernel
+//      (the reference overlaps loads with computing other cached partitions,
+//      :194-208);
+//   5. one step-kernel launch drains p's queue (and creates the walkers that
 //      start in p), walking every walker through all readable partitions;
-//   5. walkers that leave for an unreadable partition are bucketed into their
+//   6. walkers that leave for an unreadable partition are bucketed into their
 //      destination queues by the scatter kernel, into chunks allocated here.
 // Queue bookkeeping lives on the host (exact counts, no per-decision D2H of
 // queue metadata as in src/buffer/Pool.h:604-606); per iteration one small
@@ -24,6 +28,7 @@
 
 #include "engine.h"
 #include "lt_core.cuh"
+#include "mlp.h"
 #include "walk_part.h"
 
 namespace lt {
@@ -37,6 +42,7 @@ uint64_t Queue::host_count() const { return (uint64_t)host_chunks.size() * kChun
 namespace {
 
 constexpr uint32_t kHostSlabChunks = 32;  // chunks per pinned host slab (3 MiB)
+constexpr uint32_t kNoPart = 0xFFFFFFFFu;
 
 double now_ms()
 {
@@ -54,9 +60,7 @@ lt_status dalloc(T **p, uint64_t count)
     return LT_OK;
 }
 
-struct EvPair {
-    cudaEvent_t a = nullptr, b = nullptr;
-};
+enum TimerKind { kTGraph = 0, kTCompute = 1, kTZero = 2 };
 
 }  // namespace
 
@@ -69,12 +73,10 @@ struct Ooc {
     std::vector<int32_t> slot_of, part_in_slot;
     std::vector<uint64_t> last_used;
     std::vector<unsigned long long> h_rp, h_col;
-    std::vector<uint8_t> h_mapped;
 
     uint32_t *d_node_off = nullptr;
     uint64_t *d_edge_off = nullptr;
     unsigned long long *d_rp = nullptr, *d_col = nullptr;
-    uint8_t *d_mapped = nullptr;
 
     uint8_t *d_arena = nullptr;
     uint32_t n_chunks = 0;
@@ -84,88 +86,211 @@ struct Ooc {
     std::vector<uint32_t> host_free;
 
     uint64_t staging_cap = 0;
-    uint32_t *d_out = nullptr;  // 4 arrays of staging_cap
-    unsigned long long *d_out_n = nullptr;
-    uint32_t *d_hist = nullptr;
-    uint32_t *d_cursor = nullptr, *d_win_off = nullptr;
-    uint32_t *d_plan = nullptr;
+    uint32_t *d_out = nullptr;      // 4 arrays of staging_cap
+    uint32_t *d_ctl = nullptr;      // hist[P] | visits[P] | pad | out_n (u64) | next (u64)
+    uint64_t ctl_words = 0;         // u32 words of d_ctl
+    uint32_t *d_planbuf = nullptr;  // cursor[P] | win_off[P] | plan chunks
     uint64_t plan_cap = 0;
     uint32_t *d_work = nullptr;
     uint64_t work_cap = 0;
-    unsigned long long *d_next = nullptr, *d_stats = nullptr;
+    unsigned long long *d_stats = nullptr;
 
-    HostBuf h_hist;  // pinned: P u32 hist + out_n
-    std::vector<uint32_t> h_cursor, h_win_off, h_plan, h_work;
-    std::vector<uint32_t> arrivals;
-    std::vector<uint64_t> waiting;
+    HostBuf h_ctl;   // pinned mirror of d_ctl's hist + out_n
+    HostBuf h_plan;  // pinned plan block
+    HostBuf h_work;  // pinned work list
+    std::vector<uint32_t> arrivals, visits;
+    std::vector<uint64_t> waiting, lazy_left;
 
     std::vector<Queue> q;
     std::unique_ptr<Policy> policy;
     int32_t prev_loaded = -1, prev_computed = -1;
     uint64_t iteration = 0;
     uint64_t zc_threshold = 0;
+    unsigned long long zc_rp_base = 0, zc_col_base = 0;  // device view of the pinned host CSR
+    bool single = false;  // single-pass run: partitions outside the cache are read zero-copy
     int grid[3] = {0, 0, 0};
 
-    uint8_t *host_chunk(uint32_t id) { return (uint8_t *)host_slabs[id / kHostSlabChunks].ptr + (uint64_t)(id % kHostSlabChunks) * kChunkBytes; }
+    std::vector<cudaEvent_t> ev_free;
+    struct Timed {
+        cudaEvent_t a, b;
+        int kind;
+    };
+    std::vector<Timed> timed;
+
+    uint8_t *host_chunk(uint32_t id)
+    {
+        return (uint8_t *)host_slabs[id / kHostSlabChunks].ptr + (uint64_t)(id % kHostSlabChunks) * kChunkBytes;
+    }
+    uint32_t hist_words() const { return (2 * P + 1) & ~1u; }
+    uint32_t *ctl_hist() { return d_ctl; }
+    uint32_t *ctl_visits() { return d_ctl + P; }
+    unsigned long long *ctl_out_n() { return (unsigned long long *)(d_ctl + hist_words()); }
+    unsigned long long *ctl_next() { return ctl_out_n() + 1; }
 };
 
 namespace {
 
-__global__ void set_entry_kernel(unsigned long long *rp, unsigned long long *col, uint8_t *mapped, uint32_t p,
-                                 unsigned long long rv, unsigned long long cv, uint8_t mv)
+cudaEvent_t ev_get(Ooc &o)
+{
+    if (o.ev_free.empty()) {
+        cudaEvent_t ev;
+        cudaEventCreate(&ev);
+        return ev;
+    }
+    cudaEvent_t ev = o.ev_free.back();
+    o.ev_free.pop_back();
+    return ev;
+}
+
+// Resolve the event timers of finished work into the phase timers.
+void drain_timers(Ooc &o, bool all)
+{
+    lt_engine &e = *o.e;
+    size_t keep = 0;
+    for (size_t i = 0; i < o.timed.size(); i++) {
+        Ooc::Timed &t = o.timed[i];
+        if (!all && cudaEventQuery(t.b) != cudaSuccess) {
+            cudaGetLastError();
+            o.timed[keep++] = t;
+            continue;
+        }
+        float ms = 0;
+        cudaEventSynchronize(t.b);
+        cudaEventElapsedTime(&ms, t.a, t.b);
+        if (t.kind == kTGraph)
+            e.stats.graph_loading_ms += ms;
+        else if (t.kind == kTCompute)
+            e.stats.computing_ms += ms;
+        else
+            e.stats.zerocopy_ms += ms;
+        if (t.kind != kTGraph) e.stats.step_kernel_ms += ms;
+        o.ev_free.push_back(t.a);
+        o.ev_free.push_back(t.b);
+    }
+    o.timed.resize(keep);
+}
+
+__global__ void set_entry_kernel(unsigned long long *rp, unsigned long long *col, uint32_t p, unsigned long long rv,
+                                 unsigned long long cv)
 {
     rp[p] = rv;
     col[p] = cv;
-    mapped[p] = mv;
 }
 
 // Table updates travel as kernel arguments, so they are ordered on `st` with
 // the kernels that read the table and capture the values at call time.
 lt_status set_entry(Ooc &o, uint32_t p, cudaStream_t st)
 {
-    set_entry_kernel<<<1, 1, 0, st>>>(o.d_rp, o.d_col, o.d_mapped, p, o.h_rp[p], o.h_col[p], o.h_mapped[p]);
+    set_entry_kernel<<<1, 1, 0, st>>>(o.d_rp, o.d_col, p, o.h_rp[p], o.h_col[p]);
     LT_CUDA_TRY(cudaGetLastError());
+    o.e->stats.kernel_launches++;
     return LT_OK;
+}
+
+// waiting[] is kept current by refresh() wherever a queue changes.
+void refresh(Ooc &o, uint32_t p)
+{
+    o.waiting[p] = o.q[p].total();
+    o.lazy_left[p] = o.q[p].lazy_left();
+}
+void refresh_all(Ooc &o)
+{
+    for (uint32_t p = 0; p < o.P; p++) refresh(o, p);
 }
 
 SchedView view(Ooc &o)
 {
-    for (uint32_t p = 0; p < o.P; p++) o.waiting[p] = o.q[p].total();
     SchedView v;
     v.P = o.P;
+    v.K = o.K;
     v.waiting = o.waiting.data();
+    v.lazy = o.lazy_left.data();
     v.slot_of = o.slot_of.data();
     v.last_used = o.last_used.data();
     v.arrivals = o.arrivals.data();
+    v.visits = o.visits.data();
     v.iteration = o.iteration;
+    v.zc_threshold = o.zc_threshold;
     return v;
+}
+
+// Clear v's table entry on the compute stream.  Kernels enqueued before this
+// point may still read the slot; loads into the slot wait for this point.
+// Table entry of a partition outside the cache: unreadable, or in a
+// single-pass run its pinned host slices (bit 0 marks zero-copy).
+void uncached_entry(Ooc &o, uint32_t p)
+{
+    if (o.single) {
+        o.h_rp[p] = (o.zc_rp_base + 8ull * o.g->node_off[p]) | 1ull;
+        o.h_col[p] = o.zc_col_base + 4ull * o.g->edge_off[p];
+    } else {
+        o.h_rp[p] = 0;
+        o.h_col[p] = 0;
+    }
 }
 
 lt_status evict_partition(Ooc &o, uint32_t v)
 {
-    lt_engine &e = *o.e;
     const int32_t s = o.slot_of[v];
     o.slot_of[v] = -1;
     o.part_in_slot[s] = -1;
-    o.h_rp[v] = 0;
-    o.h_col[v] = 0;
-    LT_TRY(set_entry(o, v, e.s_compute));
-    return LT_OK;
+    uncached_entry(o, v);
+    return set_entry(o, v, o.e->s_compute);
 }
 
-// GPUGraph::loadAsync (src/GraphLoader.h:193-214): rowptr slice, then col
-// slice at the next 16-byte boundary of the slot.
-lt_status load_partition(Ooc &o, uint32_t p)
+int32_t free_slot(Ooc &o)
+{
+    for (uint32_t s = 0; s < o.K; s++)
+        if (o.part_in_slot[s] < 0) return (int32_t)s;
+    return -1;
+}
+
+// GPUGraph::loadAsync (src/GraphLoader.h:193-214): the rowptr slice, then the
+// col slice at the next 16-byte boundary of slot `slot`, on the copy stream
+// after every compute operation enqueued so far (the slot's previous occupant
+// may still be read by them).  The table entry is published on the compute
+// stream once the copy is done: right away (the next kernel waits for the
+// copy), or, for prefetches, after the kernel about to be launched.
+lt_status start_load(Ooc &o, uint32_t p, int32_t slot, std::vector<std::pair<uint32_t, cudaEvent_t>> *deferred)
 {
     lt_engine &e = *o.e;
     lt_graph &g = *o.g;
+    cudaEvent_t free_ev = ev_get(o);
+    LT_CUDA_TRY(cudaEventRecord(free_ev, e.s_compute));
+    LT_CUDA_TRY(cudaStreamWaitEvent(e.s_copy, free_ev, 0));
+    o.ev_free.push_back(free_ev);
+
+    const uint64_t n0 = g.node_off[p], n1 = g.node_off[p + 1];
+    const uint64_t e0 = g.edge_off[p], e1 = g.edge_off[p + 1];
+    uint8_t *base = o.d_slots + (uint64_t)slot * o.slot_stride;
+    const uint64_t rp_bytes = 8 * (n1 - n0 + 1);
+    const uint64_t col_off = (rp_bytes + 15) & ~15ull;
+    Ooc::Timed t{ev_get(o), ev_get(o), kTGraph};
+    LT_CUDA_TRY(cudaEventRecord(t.a, e.s_copy));
+    LT_CUDA_TRY(cudaMemcpyAsync(base, g.rowptr() + n0, rp_bytes, cudaMemcpyHostToDevice, e.s_copy));
+    if (e1 > e0) LT_CUDA_TRY(cudaMemcpyAsync(base + col_off, g.col() + e0, 4 * (e1 - e0), cudaMemcpyHostToDevice, e.s_copy));
+    LT_CUDA_TRY(cudaEventRecord(t.b, e.s_copy));
+    o.timed.push_back(t);
+    o.h_rp[p] = (unsigned long long)(uintptr_t)base;
+    o.h_col[p] = (unsigned long long)(uintptr_t)(base + col_off);
+    o.slot_of[p] = slot;
+    o.part_in_slot[slot] = (int32_t)p;
+    if (deferred) {
+        deferred->push_back({p, t.b});
+    } else {
+        LT_CUDA_TRY(cudaStreamWaitEvent(e.s_compute, t.b, 0));
+        LT_TRY(set_entry(o, p, e.s_compute));
+    }
+    e.stats.graph_loading_calls++;
+    e.stats.h2d_graph_bytes += rp_bytes + 4 * (e1 - e0);
+    e.stats.partition_loads++;
+    return LT_OK;
+}
+
+lt_status load_partition(Ooc &o, uint32_t p)
+{
     if (o.slot_of[p] >= 0) return LT_OK;
-    int32_t slot = -1;
-    for (uint32_t s = 0; s < o.K; s++)
-        if (o.part_in_slot[s] < 0) {
-            slot = (int32_t)s;
-            break;
-        }
+    int32_t slot = free_slot(o);
     if (slot < 0) {
         SchedView v = view(o);
         int32_t victim = o.policy->victim(v, o.prev_loaded, p);
@@ -176,43 +301,7 @@ lt_status load_partition(Ooc &o, uint32_t p)
         slot = o.slot_of[victim];
         LT_TRY(evict_partition(o, (uint32_t)victim));
     }
-    // the slot's previous occupant may still be read by queued compute work
-    cudaEvent_t free_ev;
-    LT_CUDA_TRY(cudaEventCreateWithFlags(&free_ev, cudaEventDisableTiming));
-    LT_CUDA_TRY(cudaEventRecord(free_ev, e.s_compute));
-    LT_CUDA_TRY(cudaStreamWaitEvent(e.s_copy, free_ev, 0));
-    cudaEventDestroy(free_ev);
-
-    const uint64_t n0 = g.node_off[p], n1 = g.node_off[p + 1];
-    const uint64_t e0 = g.edge_off[p], e1 = g.edge_off[p + 1];
-    uint8_t *base = o.d_slots + (uint64_t)slot * o.slot_stride;
-    const uint64_t rp_bytes = 8 * (n1 - n0 + 1);
-    const uint64_t col_off = (rp_bytes + 15) & ~15ull;
-    EvPair t;
-    cudaEventCreate(&t.a);
-    cudaEventCreate(&t.b);
-    LT_CUDA_TRY(cudaEventRecord(t.a, e.s_copy));
-    LT_CUDA_TRY(cudaMemcpyAsync(base, g.rowptr() + n0, rp_bytes, cudaMemcpyHostToDevice, e.s_copy));
-    if (e1 > e0) LT_CUDA_TRY(cudaMemcpyAsync(base + col_off, g.col() + e0, 4 * (e1 - e0), cudaMemcpyHostToDevice, e.s_copy));
-    LT_CUDA_TRY(cudaEventRecord(t.b, e.s_copy));
-    // publish the slot to kernels once its data is in place
-    LT_CUDA_TRY(cudaStreamWaitEvent(e.s_compute, t.b, 0));
-    o.h_rp[p] = (unsigned long long)(uintptr_t)base;
-    o.h_col[p] = (unsigned long long)(uintptr_t)(base + col_off);
-    o.h_mapped[p] = 0;
-    LT_TRY(set_entry(o, p, e.s_compute));
-    o.slot_of[p] = slot;
-    o.part_in_slot[slot] = (int32_t)p;
-    LT_CUDA_TRY(cudaEventSynchronize(t.b));
-    float ms = 0;
-    cudaEventElapsedTime(&ms, t.a, t.b);
-    cudaEventDestroy(t.a);
-    cudaEventDestroy(t.b);
-    e.stats.graph_loading_ms += ms;
-    e.stats.graph_loading_calls++;
-    e.stats.h2d_graph_bytes += rp_bytes + 4 * (e1 - e0);
-    e.stats.partition_loads++;
-    return LT_OK;
+    return start_load(o, p, slot, nullptr);
 }
 
 lt_status host_chunk_alloc(Ooc &o, uint32_t &id)
@@ -242,8 +331,9 @@ lt_status spill_until(Ooc &o, uint64_t need, int32_t except)
         for (uint32_t i = 0; i < o.P; i++) {
             if ((int32_t)i == except) continue;
             const Queue &qi = o.q[i];
-            const size_t full = qi.dev_chunks.size() - (qi.dev_chunks.empty() || qi.tail_fill == kChunk ? 0 : 1);
-            if (qi.dev_chunks.empty() || full == 0) continue;
+            if (qi.dev_chunks.empty()) continue;
+            const size_t full = qi.dev_chunks.size() - (qi.tail_fill == kChunk ? 0 : 1);
+            if (full == 0) continue;
             if (best < 0 || qi.total() < o.q[best].total()) best = (int32_t)i;
         }
         if (best < 0)
@@ -254,7 +344,6 @@ lt_status spill_until(Ooc &o, uint64_t need, int32_t except)
             t0 = now_ms();
         }
         Queue &qb = o.q[best];
-        // spill full chunks from the front; the partially filled tail stays
         const size_t full = qb.dev_chunks.size() - (qb.tail_fill == kChunk ? 0 : 1);
         size_t moved = 0;
         for (size_t k = 0; k < full && o.free_chunks.size() + moved < need; k++) {
@@ -264,12 +353,13 @@ lt_status spill_until(Ooc &o, uint64_t need, int32_t except)
             LT_CUDA_TRY(cudaMemcpyAsync(o.host_chunk(hid), o.d_arena + (uint64_t)dc * kChunkBytes, kChunkBytes,
                                         cudaMemcpyDeviceToHost, e.s_copyback));
             qb.host_chunks.push_back(hid);
-            o.free_chunks.push_back(dc);
             moved++;
             e.stats.d2h_walker_bytes += kChunkBytes;
         }
+        for (size_t k = 0; k < moved; k++) o.free_chunks.push_back(qb.dev_chunks[k]);
         qb.dev_chunks.erase(qb.dev_chunks.begin(), qb.dev_chunks.begin() + moved);
         if (qb.dev_chunks.empty()) qb.tail_fill = 0;
+        refresh(o, (uint32_t)best);
         e.stats.walker_evicting_calls++;
     }
     if (t0 >= 0) {
@@ -302,12 +392,13 @@ lt_status unspill(Ooc &o, uint32_t p, uint64_t max_chunks)
     }
     if (qp.dev_chunks.empty()) qp.tail_fill = kChunk;
     qp.dev_chunks.insert(qp.dev_chunks.begin(), fresh.begin(), fresh.end());
+    refresh(o, p);
+    // the host slots are reused only after the copy: wait here
     LT_CUDA_TRY(cudaStreamSynchronize(e.s_copy));
     e.stats.walker_loading_ms += now_ms() - t0;
     e.stats.walker_loading_calls++;
     return LT_OK;
 }
-
 
 struct RunParams {
     int app, start;
@@ -317,36 +408,90 @@ struct RunParams {
     uint32_t *endpoints, *paths;
 };
 
+// Loads the policy wants started before the step kernel of partition p.
+// Victims are cleared from the table before the kernel is enqueued, so the
+// kernel never reads a slot that is being overwritten; the new entries are
+// published after the kernel.
+lt_status prefetch(Ooc &o, uint32_t p, std::vector<std::pair<uint32_t, cudaEvent_t>> &deferred)
+{
+    lt_engine &e = *o.e;
+    if (!e.cfg.pipeline) return LT_OK;
+    SchedView v = view(o);
+    std::vector<uint32_t> order;
+    o.policy->prefetch_order(v, p, order);
+    const size_t depth = o.policy->prefetch_depth(v);
+    for (size_t i = 0; i < order.size() && i < depth; i++) {
+        const uint32_t c = order[i];
+        if (o.slot_of[c] >= 0) continue;
+        int32_t slot = free_slot(o);
+        if (slot < 0) {
+            v = view(o);
+            const int32_t victim = o.policy->victim_for_prefetch(v, (int32_t)p, c);
+            if (victim < 0) break;
+            slot = o.slot_of[victim];
+            LT_TRY(evict_partition(o, (uint32_t)victim));
+        }
+        LT_TRY(start_load(o, c, slot, &deferred));
+    }
+    return LT_OK;
+}
+
 // Launch the step kernel over p's device chunks plus G lazily created walkers
 // (ordinals lazy_begin..), then bucket the walkers that left.  p < 0: the
 // lazily created walkers have uniform random starts and belong to no
 // partition yet (the reference's createWalkers / insert, src/WalkManager.h:341-360).
-lt_status step_and_bucket(Ooc &o, const RunParams &rp, int32_t p, uint64_t lazy_begin, uint64_t G, bool zero_copy)
+struct Lazy {
+    int mode;           // lt::Start
+    uint32_t nb, n;     // per-vertex starts: vertex range
+    uint64_t begin, count;
+};
+
+Lazy lazy_of(Ooc &o, const RunParams &rp, int32_t p, uint64_t begin, uint64_t count)
 {
+    Lazy z{};
+    z.begin = begin;
+    z.count = count;
+    if (p < 0) {
+        z.mode = rp.start;
+        z.nb = 0;
+        z.n = o.g->V;
+    } else {
+        z.mode = rp.start == kStartPerVertex ? kStartPerVertex : kStartSource;
+        z.nb = o.g->node_off[p];
+        z.n = o.g->node_off[p + 1] - z.nb;
+    }
+    return z;
+}
+
+lt_status step_and_bucket(Ooc &o, const RunParams &rp, int32_t p, const Lazy &lz, bool zero_copy,
+                          std::vector<std::pair<uint32_t, cudaEvent_t>> *deferred)
+{
+    const uint64_t G = lz.count;
     lt_engine &e = *o.e;
     lt_graph &g = *o.g;
     Queue *qp = p >= 0 ? &o.q[p] : nullptr;
     const uint64_t n_chunk_walkers = qp ? qp->dev_count() : 0;
     if (n_chunk_walkers + G == 0) return LT_OK;
     if (n_chunk_walkers + G > o.staging_cap) return fail(LT_ERR_CAPACITY, "staging area too small");
-    o.h_work.clear();
-    if (qp) o.h_work.assign(qp->dev_chunks.begin(), qp->dev_chunks.end());
-    if (o.h_work.size() > o.work_cap) return fail(LT_ERR_CAPACITY, "work list too small");
-    if (!o.h_work.empty())
-        LT_CUDA_TRY(cudaMemcpyAsync(o.d_work, o.h_work.data(), 4 * o.h_work.size(), cudaMemcpyHostToDevice, e.s_compute));
-    LT_CUDA_TRY(cudaMemsetAsync(o.d_next, 0, 8, e.s_compute));
-    LT_CUDA_TRY(cudaMemsetAsync(o.d_out_n, 0, 8, e.s_compute));
-    LT_CUDA_TRY(cudaMemsetAsync(o.d_hist, 0, 4ull * o.P, e.s_compute));
+    const uint64_t nw = qp ? qp->dev_chunks.size() : 0;
+    if (nw > o.work_cap) return fail(LT_ERR_CAPACITY, "work list too small");
+    uint32_t *h_work = (uint32_t *)o.h_work.ptr;
+    if (nw) {
+        std::memcpy(h_work, qp->dev_chunks.data(), 4 * nw);
+        LT_CUDA_TRY(cudaMemcpyAsync(o.d_work, h_work, 4 * nw, cudaMemcpyHostToDevice, e.s_compute));
+    }
+    LT_CUDA_TRY(cudaMemsetAsync(o.d_ctl, 0, 4 * o.ctl_words, e.s_compute));
 
     StepArgs a{};
-    a.t = PartTable{o.d_node_off, o.d_edge_off, o.d_rp, o.d_col, o.d_mapped, o.P};
+    a.t = PartTable{o.d_node_off, o.d_edge_off, o.d_rp, o.d_col, o.P};
     a.arena = o.d_arena;
     a.work_chunks = o.d_work;
     a.n_chunk_walkers = n_chunk_walkers;
-    a.lazy_begin = lazy_begin;
+    a.lazy_begin = lz.begin;
     a.lazy_count = G;
-    a.lazy_part = p >= 0 ? (uint32_t)p : 0;
-    a.lazy_mode = p < 0 ? kStartUniform : (rp.start == kStartPerVertex ? kStartPerVertex : kStartSource);
+    a.lazy_nb = lz.nb;
+    a.lazy_n = lz.n;
+    a.lazy_mode = lz.mode;
     a.W = rp.W;
     a.V = g.V;
     a.source = rp.source;
@@ -361,44 +506,49 @@ lt_status step_and_bucket(Ooc &o, const RunParams &rp, int32_t p, uint64_t lazy_
     a.out_step = o.d_out + o.staging_cap;
     a.out_idx = o.d_out + 2 * o.staging_cap;
     a.out_dest = o.d_out + 3 * o.staging_cap;
-    a.out_n = o.d_out_n;
-    a.hist = o.d_hist;
-    a.next = o.d_next;
+    a.out_n = o.ctl_out_n();
+    a.hist = o.ctl_hist();
+    a.visits = o.ctl_visits();
+    a.next = o.ctl_next();
     a.stats = o.d_stats;
+    a.zc_part = kNoPart;
+    if (zero_copy) {
+        a.zc_part = (uint32_t)p;
+        a.zc_rp = o.zc_rp_base + 8ull * g.node_off[p];
+        a.zc_col = o.zc_col_base + 4ull * g.edge_off[p];
+    }
 
-    EvPair t;
-    cudaEventCreate(&t.a);
-    cudaEventCreate(&t.b);
+    Ooc::Timed t{ev_get(o), ev_get(o), zero_copy ? kTZero : kTCompute};
     LT_CUDA_TRY(cudaEventRecord(t.a, e.s_compute));
     LT_CUDA_TRY(launch_walk_part(a, rp.app, o.grid[rp.app], e.s_compute));
     LT_CUDA_TRY(cudaEventRecord(t.b, e.s_compute));
-    e.stats.kernel_launches++;
-    uint32_t *h_hist = (uint32_t *)o.h_hist.ptr;
-    unsigned long long *h_n = (unsigned long long *)(h_hist + o.P + (o.P & 1));
-    LT_CUDA_TRY(cudaMemcpyAsync(h_hist, o.d_hist, 4ull * o.P, cudaMemcpyDeviceToHost, e.s_compute));
-    LT_CUDA_TRY(cudaMemcpyAsync(h_n, o.d_out_n, 8, cudaMemcpyDeviceToHost, e.s_compute));
-    LT_CUDA_TRY(cudaStreamSynchronize(e.s_compute));
-    float ms = 0;
-    cudaEventElapsedTime(&ms, t.a, t.b);
-    cudaEventDestroy(t.a);
-    cudaEventDestroy(t.b);
-    e.stats.step_kernel_ms += ms;
-    if (zero_copy) {
-        e.stats.zerocopy_ms += ms;
+    o.timed.push_back(t);
+    if (zero_copy)
         e.stats.zerocopy_calls++;
-    } else {
-        e.stats.computing_ms += ms;
+    else
         e.stats.computing_calls++;
+    e.stats.kernel_launches++;
+    if (deferred) {
+        for (auto &d : *deferred) {
+            LT_CUDA_TRY(cudaStreamWaitEvent(e.s_compute, d.second, 0));
+            LT_TRY(set_entry(o, d.first, e.s_compute));
+        }
+        deferred->clear();
     }
+    uint32_t *h_hist = (uint32_t *)o.h_ctl.ptr;
+    LT_CUDA_TRY(cudaMemcpyAsync(h_hist, o.d_ctl, 4ull * o.hist_words() + 8, cudaMemcpyDeviceToHost, e.s_compute));
+    LT_CUDA_TRY(cudaStreamSynchronize(e.s_compute));
+    const uint64_t staged = *(const unsigned long long *)(h_hist + o.hist_words());
     // p's queue is drained: its chunks return to the pool.
     if (qp) {
         for (uint32_t c : qp->dev_chunks) o.free_chunks.push_back(c);
         qp->dev_chunks.clear();
         qp->tail_fill = 0;
         qp->lazy_next += G;
+        refresh(o, (uint32_t)p);
     }
-    const uint64_t staged = *h_n;
-    for (uint32_t d = 0; d < o.P; d++) o.arrivals[d] = h_hist[d];
+    std::memcpy(o.arrivals.data(), h_hist, 4ull * o.P);
+    std::memcpy(o.visits.data(), h_hist + o.P, 4ull * o.P);
     if (staged == 0) return LT_OK;
 
     // Plan the append of h_hist[d] walkers to each destination queue.
@@ -412,10 +562,13 @@ lt_status step_and_bucket(Ooc &o, const RunParams &rp, int32_t p, uint64_t lazy_
     }
     if (need > o.free_chunks.size()) LT_TRY(spill_until(o, need, -1));
     if (need > o.free_chunks.size()) return fail(LT_ERR_CAPACITY, "walker pool exhausted");
-    o.h_plan.clear();
+    uint32_t *h_cursor = (uint32_t *)o.h_plan.ptr;
+    uint32_t *h_win = h_cursor + o.P;
+    uint32_t *h_chunks = h_win + o.P;
+    uint64_t n_plan = 0;
     for (uint32_t d = 0; d < o.P; d++) {
-        o.h_cursor[d] = 0;
-        o.h_win_off[d] = 0;
+        h_cursor[d] = 0;
+        h_win[d] = 0;
         if (!h_hist[d]) continue;
         Queue &qd = o.q[d];
         if (qd.dev_chunks.empty() || qd.tail_fill == kChunk) {
@@ -423,23 +576,22 @@ lt_status step_and_bucket(Ooc &o, const RunParams &rp, int32_t p, uint64_t lazy_
             o.free_chunks.pop_back();
             qd.tail_fill = 0;
         }
-        o.h_win_off[d] = (uint32_t)o.h_plan.size();
-        o.h_cursor[d] = qd.tail_fill;
-        o.h_plan.push_back(qd.dev_chunks.back());
+        h_win[d] = (uint32_t)n_plan;
+        h_cursor[d] = qd.tail_fill;
+        h_chunks[n_plan++] = qd.dev_chunks.back();
         const uint64_t tot = (uint64_t)qd.tail_fill + h_hist[d];
         const uint64_t extra = (tot + kChunk - 1) / kChunk - 1;
         for (uint64_t k = 0; k < extra; k++) {
             const uint32_t c = o.free_chunks.back();
             o.free_chunks.pop_back();
             qd.dev_chunks.push_back(c);
-            o.h_plan.push_back(c);
+            h_chunks[n_plan++] = c;
         }
         qd.tail_fill = (uint32_t)(tot - extra * kChunk);
+        refresh(o, d);
     }
-    if (o.h_plan.size() > o.plan_cap) return fail(LT_ERR_CAPACITY, "plan buffer too small");
-    LT_CUDA_TRY(cudaMemcpyAsync(o.d_cursor, o.h_cursor.data(), 4ull * o.P, cudaMemcpyHostToDevice, e.s_compute));
-    LT_CUDA_TRY(cudaMemcpyAsync(o.d_win_off, o.h_win_off.data(), 4ull * o.P, cudaMemcpyHostToDevice, e.s_compute));
-    LT_CUDA_TRY(cudaMemcpyAsync(o.d_plan, o.h_plan.data(), 4ull * o.h_plan.size(), cudaMemcpyHostToDevice, e.s_compute));
+    if (n_plan > o.plan_cap) return fail(LT_ERR_CAPACITY, "plan buffer too small");
+    LT_CUDA_TRY(cudaMemcpyAsync(o.d_planbuf, h_cursor, 4ull * (2ull * o.P + n_plan), cudaMemcpyHostToDevice, e.s_compute));
     ScatterArgs sa{};
     sa.in_cur = a.out_cur;
     sa.in_step = a.out_step;
@@ -447,9 +599,9 @@ lt_status step_and_bucket(Ooc &o, const RunParams &rp, int32_t p, uint64_t lazy_
     sa.in_dest = a.out_dest;
     sa.n = staged;
     sa.arena = o.d_arena;
-    sa.cursor = o.d_cursor;
-    sa.win_off = o.d_win_off;
-    sa.plan_chunks = o.d_plan;
+    sa.cursor = o.d_planbuf;
+    sa.win_off = o.d_planbuf + o.P;
+    sa.plan_chunks = o.d_planbuf + 2ull * o.P;
     sa.P = o.P;
     LT_CUDA_TRY(launch_scatter(sa, e.device, e.s_compute));
     e.stats.kernel_launches++;
@@ -480,18 +632,22 @@ lt_status ensure_pool(Ooc &o, uint64_t W)
     const uint64_t want = (B + kChunk - 1) / kChunk + 2ull * o.P + 2;
     if (want > 0xFFFFFFF0ull) return fail(LT_ERR_CAPACITY, "walker pool too large");
     if (o.d_arena && o.n_chunks == want) return LT_OK;
-    for (void *p : {(void *)o.d_arena, (void *)o.d_out, (void *)o.d_plan, (void *)o.d_work})
+    for (void *p : {(void *)o.d_arena, (void *)o.d_out, (void *)o.d_planbuf, (void *)o.d_work})
         if (p) cudaFree(p);
+    host_free(o.h_plan);
+    host_free(o.h_work);
     o.d_arena = nullptr;
-    o.d_out = o.d_plan = o.d_work = nullptr;
+    o.d_out = o.d_planbuf = o.d_work = nullptr;
     o.n_chunks = (uint32_t)want;
     o.staging_cap = (uint64_t)o.n_chunks * kChunk;
     o.plan_cap = o.n_chunks + (uint64_t)o.P;
     o.work_cap = o.n_chunks;
     LT_TRY(dalloc(&o.d_arena, (uint64_t)o.n_chunks * kChunkBytes));
     LT_TRY(dalloc(&o.d_out, 4 * o.staging_cap));
-    LT_TRY(dalloc(&o.d_plan, o.plan_cap));
+    LT_TRY(dalloc(&o.d_planbuf, 2ull * o.P + o.plan_cap));
     LT_TRY(dalloc(&o.d_work, o.work_cap));
+    LT_TRY(host_alloc(o.h_plan, 4 * (2ull * o.P + o.plan_cap), true));
+    LT_TRY(host_alloc(o.h_work, 4 * o.work_cap, true));
     return LT_OK;
 }
 
@@ -514,17 +670,9 @@ lt_status process(Ooc &o, const RunParams &rp, uint32_t p)
     o.last_used[p] = o.iteration;
     o.prev_computed = (int32_t)p;
     Queue &qp = o.q[p];
-    const bool zero_copy = o.slot_of[p] < 0 && qp.total() < o.zc_threshold;
-    if (zero_copy) {
-        lt_graph &g = *o.g;
-        void *rp_dev = nullptr, *col_dev = nullptr;
-        LT_CUDA_TRY(cudaHostGetDevicePointer(&rp_dev, (void *)(g.rowptr() + g.node_off[p]), 0));
-        LT_CUDA_TRY(cudaHostGetDevicePointer(&col_dev, (void *)(g.col() + g.edge_off[p]), 0));
-        o.h_rp[p] = (unsigned long long)(uintptr_t)rp_dev;
-        o.h_col[p] = (unsigned long long)(uintptr_t)col_dev;
-        o.h_mapped[p] = 1;
-        LT_TRY(set_entry(o, p, e.s_compute));
-    } else {
+    SchedView v0 = view(o);
+    const bool zero_copy = o.slot_of[p] < 0 && o.policy->zero_copy(v0, p, o.zc_threshold);
+    if (!zero_copy) {
         e.stats.explicit_iterations++;
         LT_TRY(load_partition(o, p));
         o.prev_loaded = (int32_t)p;
@@ -547,15 +695,68 @@ lt_status process(Ooc &o, const RunParams &rp, uint32_t p)
         LT_TRY(spill_until(o, (uint64_t)o.P + 2 + 1, (int32_t)p));
         G = lazy_budget(o, (int32_t)p, qp.lazy_left());
     }
-    LT_TRY(step_and_bucket(o, rp, (int32_t)p, qp.lazy_next, G, zero_copy));
-    if (zero_copy) {
-        o.h_rp[p] = 0;
-        o.h_col[p] = 0;
-        o.h_mapped[p] = 0;
-        LT_TRY(set_entry(o, p, e.s_compute));
-    }
+    std::vector<std::pair<uint32_t, cudaEvent_t>> deferred;
+    LT_TRY(prefetch(o, p, deferred));
+    LT_TRY(step_and_bucket(o, rp, (int32_t)p, lazy_of(o, rp, (int32_t)p, qp.lazy_next, G), zero_copy, &deferred));
+    drain_timers(o, false);
     SchedView v = view(o);
     o.policy->observe(v);
+    return LT_OK;
+}
+
+// Single-pass cache update: fill free slots with the best-scored partitions,
+// then swap the worst cached partition for a clearly better one, at most
+// swap_budget times per batch.  Loads are published after the next kernel.
+lt_status update_cache(Ooc &o, std::vector<std::pair<uint32_t, cudaEvent_t>> &deferred)
+{
+    SchedView v = view(o);
+    std::vector<double> sc(o.P);
+    for (uint32_t p = 0; p < o.P; p++) sc[p] = o.policy->cache_score(v, p);
+    std::vector<uint32_t> out_set, in_set;
+    for (uint32_t p = 0; p < o.P; p++) (o.slot_of[p] < 0 ? out_set : in_set).push_back(p);
+    std::sort(out_set.begin(), out_set.end(), [&](uint32_t a, uint32_t b) { return sc[a] != sc[b] ? sc[a] > sc[b] : a < b; });
+    std::sort(in_set.begin(), in_set.end(), [&](uint32_t a, uint32_t b) { return sc[a] != sc[b] ? sc[a] < sc[b] : a < b; });
+    size_t next_in = 0, swaps = 0;
+    for (uint32_t c : out_set) {
+        if (sc[c] <= 0.0) break;
+        int32_t slot = free_slot(o);
+        if (slot < 0) {
+            if (swaps >= o.policy->swap_budget() || next_in >= in_set.size()) break;
+            const uint32_t w = in_set[next_in];
+            if (!(sc[c] > 1.25 * sc[w] + 1.0)) break;
+            next_in++;
+            swaps++;
+            slot = o.slot_of[w];
+            LT_TRY(evict_partition(o, w));
+        }
+        LT_TRY(start_load(o, c, slot, &deferred));
+    }
+    return LT_OK;
+}
+
+// Single-pass run: every partition readable, walkers created in batches and
+// walked to completion; between batches the policy reshapes the cache.
+lt_status single_pass_run(Ooc &o, const RunParams &rp, uint64_t W)
+{
+    lt_engine &e = *o.e;
+    for (uint32_t p = 0; p < o.P; p++)
+        if (o.slot_of[p] < 0) {
+            uncached_entry(o, p);
+            LT_TRY(set_entry(o, p, e.s_compute));
+        }
+    const uint64_t batch = std::max<uint64_t>(uint64_t(1) << 22, W / 48);
+    uint64_t made = 0;
+    std::vector<std::pair<uint32_t, cudaEvent_t>> deferred;
+    while (made < W) {
+        const uint64_t G = std::min(batch, W - made);
+        o.iteration++;
+        e.stats.iterations++;
+        LT_TRY(update_cache(o, deferred));
+        LT_TRY(step_and_bucket(o, rp, -1, lazy_of(o, rp, -1, made, G), false, &deferred));
+        made += G;
+        drain_timers(o, false);
+        o.policy->observe(view(o));
+    }
     return LT_OK;
 }
 
@@ -574,6 +775,7 @@ lt_status ooc_create(lt_engine *e, Ooc **out)
     uint64_t max_slot = 0;
     for (uint32_t p = 0; p < o->P; p++) max_slot = std::max<uint64_t>(max_slot, g.slot_bytes(p) + 16);
     if (max_slot > o->slot_stride) o->slot_stride = (max_slot + 255) & ~255ull;
+    o->ctl_words = o->hist_words() + 4;
     auto bail = [&](lt_status s) {
         ooc_destroy(o);
         return s;
@@ -583,38 +785,47 @@ lt_status ooc_create(lt_engine *e, Ooc **out)
     if (s == LT_OK) s = dalloc(&o->d_edge_off, o->P + 1);
     if (s == LT_OK) s = dalloc(&o->d_rp, o->P);
     if (s == LT_OK) s = dalloc(&o->d_col, o->P);
-    if (s == LT_OK) s = dalloc(&o->d_mapped, o->P);
-    if (s == LT_OK) s = dalloc(&o->d_out_n, 1);
-    if (s == LT_OK) s = dalloc(&o->d_hist, o->P);
-    if (s == LT_OK) s = dalloc(&o->d_cursor, o->P);
-    if (s == LT_OK) s = dalloc(&o->d_win_off, o->P);
-    if (s == LT_OK) s = dalloc(&o->d_next, 1);
+    if (s == LT_OK) s = dalloc(&o->d_ctl, o->ctl_words);
     if (s == LT_OK) s = dalloc(&o->d_stats, 8);
-    if (s == LT_OK) s = host_alloc(o->h_hist, 4ull * o->P + 16, true);
+    if (s == LT_OK) s = host_alloc(o->h_ctl, 4 * o->ctl_words, true);
     if (s != LT_OK) return bail(s);
     if (cudaMemcpy(o->d_node_off, g.node_off.data(), 4ull * (o->P + 1), cudaMemcpyHostToDevice) != cudaSuccess ||
         cudaMemcpy(o->d_edge_off, g.edge_off.data(), 8ull * (o->P + 1), cudaMemcpyHostToDevice) != cudaSuccess ||
-        cudaMemset(o->d_rp, 0, 8ull * o->P) != cudaSuccess || cudaMemset(o->d_col, 0, 8ull * o->P) != cudaSuccess ||
-        cudaMemset(o->d_mapped, 0, o->P) != cudaSuccess)
+        cudaMemset(o->d_rp, 0, 8ull * o->P) != cudaSuccess || cudaMemset(o->d_col, 0, 8ull * o->P) != cudaSuccess)
         return bail(fail(LT_ERR_CUDA, "partition table upload failed"));
     o->slot_of.assign(o->P, -1);
     o->part_in_slot.assign(o->K, -1);
     o->last_used.assign(o->P, 0);
     o->h_rp.assign(o->P, 0);
     o->h_col.assign(o->P, 0);
-    o->h_mapped.assign(o->P, 0);
-    o->h_cursor.assign(o->P, 0);
-    o->h_win_off.assign(o->P, 0);
     o->arrivals.assign(o->P, 0);
+    o->visits.assign(o->P, 0);
     o->waiting.assign(o->P, 0);
+    o->lazy_left.assign(o->P, 0);
     o->q.assign(o->P, Queue{});
-    if (e->cfg.sched == LT_SCHED_FIFO)
+    if (e->cfg.sched == LT_SCHED_FIFO) {
         o->policy.reset(new FifoPolicy());
-    else
+    } else if (e->cfg.sched == LT_SCHED_LEARNED || e->cfg.sched == LT_SCHED_FREQUENCY) {
+        Policy *lp = nullptr;
+        s = make_learned_policy(g, e->device, e->cfg.sched == LT_SCHED_LEARNED, &lp);
+        if (s != LT_OK) return bail(s);
+        o->policy.reset(lp);
+    } else {
         o->policy.reset(new Policy());
+    }
     o->zc_threshold = e->cfg.zerocopy_threshold == UINT64_MAX ? g.part_bytes / 128 / 2 : e->cfg.zerocopy_threshold;
+    if (g.rowptr_buf.pinned && g.col_buf.pinned) {
+        void *rp_dev = nullptr, *col_dev = nullptr;
+        if (cudaHostGetDevicePointer(&rp_dev, (void *)g.rowptr(), 0) != cudaSuccess ||
+            cudaHostGetDevicePointer(&col_dev, (void *)g.col(), 0) != cudaSuccess)
+            return bail(fail(LT_ERR_CUDA, "pinned graph is not mapped for zero-copy reads"));
+        o->zc_rp_base = (unsigned long long)(uintptr_t)rp_dev;
+        o->zc_col_base = (unsigned long long)(uintptr_t)col_dev;
+    } else {
+        o->zc_threshold = 0;  // the graph is not in pinned memory: always load
+    }
     const size_t smem = part_smem(o->P);
-    if (smem > 48 * 1024) return bail(fail(LT_ERR_UNSUPPORTED, "partition count %u needs %zu bytes of shared memory", o->P, smem));
+    if (smem > 64 * 1024) return bail(fail(LT_ERR_UNSUPPORTED, "partition count %u needs %zu bytes of shared memory", o->P, smem));
     for (int app = 0; app < 3; app++) o->grid[app] = part_grid(app, 0, e->device, smem);
     *out = o;
     return LT_OK;
@@ -623,23 +834,30 @@ lt_status ooc_create(lt_engine *e, Ooc **out)
 void ooc_destroy(Ooc *o)
 {
     if (!o) return;
+    drain_timers(*o, true);
     for (void *p : {(void *)o->d_slots, (void *)o->d_node_off, (void *)o->d_edge_off, (void *)o->d_rp, (void *)o->d_col,
-                    (void *)o->d_mapped, (void *)o->d_arena, (void *)o->d_out, (void *)o->d_out_n, (void *)o->d_hist,
-                    (void *)o->d_cursor, (void *)o->d_win_off, (void *)o->d_plan, (void *)o->d_work, (void *)o->d_next,
+                    (void *)o->d_arena, (void *)o->d_out, (void *)o->d_ctl, (void *)o->d_planbuf, (void *)o->d_work,
                     (void *)o->d_stats})
         if (p) cudaFree(p);
     for (HostBuf &b : o->host_slabs) host_free(b);
-    host_free(o->h_hist);
+    host_free(o->h_ctl);
+    host_free(o->h_plan);
+    host_free(o->h_work);
+    for (cudaEvent_t ev : o->ev_free) cudaEventDestroy(ev);
     delete o;
 }
+
+void ooc_policy_stats(const Ooc *o, lt_policy_stats &s) { o->policy->stats(s); }
 
 lt_status ooc_drop_cache(Ooc *o)
 {
     lt_engine &e = *o->e;
     LT_CUDA_TRY(cudaStreamSynchronize(e.s_compute));
+    LT_CUDA_TRY(cudaStreamSynchronize(e.s_copy));
     for (uint32_t p = 0; p < o->P; p++)
         if (o->slot_of[p] >= 0) LT_TRY(evict_partition(*o, p));
     LT_CUDA_TRY(cudaStreamSynchronize(e.s_compute));
+    o->policy->reset();
     return LT_OK;
 }
 
@@ -679,8 +897,28 @@ lt_status ooc_run(lt_engine *e, int app, int start, uint32_t source, uint64_t W,
     for (uint32_t r = 0; r < runs; r++) {
         rp.run = run_base + r;
         reset_queues(o);
+        refresh_all(o);
         o.prev_computed = -1;
-        if (start == kStartSource) {
+        bool fresh = true;
+        o.single = o.policy->single_pass() && o.zc_rp_base != 0;
+        if (o.single) {
+            LT_TRY(single_pass_run(o, rp, W));
+            refresh_all(o);
+            bool left = false;
+            for (uint32_t p = 0; p < o.P && !left; p++) left = o.waiting[p] > 0;
+            if (!left) continue;
+            // a walker left the readable set (cannot happen while every
+            // partition is mapped); drain it with the regular loop
+            o.single = false;
+            for (uint32_t p = 0; p < o.P; p++)
+                if (o.slot_of[p] < 0) {
+                    uncached_entry(o, p);
+                    LT_TRY(set_entry(o, p, e->s_compute));
+                }
+            fresh = false;
+        }
+        if (!fresh) {
+        } else if (start == kStartSource) {
             o.q[g.find_partition(source)].lazy_total = W;
         } else if (start == kStartPerVertex) {
             const uint64_t wraps = W / g.V, rem = W % g.V;
@@ -699,10 +937,11 @@ lt_status ooc_run(lt_engine *e, int app, int start, uint32_t source, uint64_t W,
                     G = lazy_budget(o, -1, W - made);
                     if (G == 0) return fail(LT_ERR_CAPACITY, "walker pool too small to create walkers");
                 }
-                LT_TRY(step_and_bucket(o, rp, -1, made, G, false));
+                LT_TRY(step_and_bucket(o, rp, -1, lazy_of(o, rp, -1, made, G), false, nullptr));
                 made += G;
             }
         }
+        refresh_all(o);
         // Scheduler::start (src/Scheduler.h:425-438)
         bool sync = false;
         uint32_t p = 0;
@@ -724,10 +963,13 @@ lt_status ooc_run(lt_engine *e, int app, int start, uint32_t source, uint64_t W,
     if (paths_out)
         LT_CUDA_TRY(cudaMemcpyAsync(paths_out, e->d_paths, 4 * W * ((uint64_t)length + 1), cudaMemcpyDeviceToHost, st));
     LT_CUDA_TRY(cudaStreamSynchronize(st));
+    LT_CUDA_TRY(cudaStreamSynchronize(e->s_copy));
+    drain_timers(o, true);
     e->stats.updates = hs[0];
     e->stats.moves = hs[1];
     e->stats.teleports = hs[2];
     e->stats.zerocopy_bytes = hs[3] * 256;  // two 128-byte host lines per zero-copy hop
+    e->stats.handoffs = hs[4];
     e->stats.running_ms = now_ms() - t0;
     return LT_OK;
 }

@@ -34,6 +34,7 @@ struct Ooc;
 lt_status ooc_create(lt_engine *e, Ooc **out);
 void ooc_destroy(Ooc *o);
 lt_status ooc_drop_cache(Ooc *o);
+void ooc_policy_stats(const Ooc *o, lt_policy_stats &s);
 lt_status ooc_run(lt_engine *e, int app, int start, uint32_t source, uint64_t W, uint32_t length, uint32_t runs,
                   uint32_t run_base, float prob, uint64_t *counts_out, uint32_t *endpoints_out, uint32_t *paths_out);
 

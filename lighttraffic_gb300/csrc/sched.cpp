@@ -32,14 +32,6 @@ int32_t Policy::victim(const SchedView &v, int32_t except, uint32_t /*incoming*/
     return best;
 }
 
-void Policy::prefetch_order(const SchedView &v, uint32_t exclude, std::vector<uint32_t> &out)
-{
-    out.clear();
-    for (uint32_t i = 0; i < v.P; i++)
-        if (i != exclude && v.slot_of[i] < 0 && v.waiting[i] > 0) out.push_back(i);
-    std::stable_sort(out.begin(), out.end(), [&](uint32_t a, uint32_t b) { return v.waiting[a] > v.waiting[b]; });
-}
-
 // FIFO_SCHE nextPartition (src/Scheduler.h:393-416): sweep partitions in id
 // order, returning each one that has walkers; a finished sweep returns false
 // once, after which the caller's outer loop starts the next sweep.

@@ -8,26 +8,36 @@
 //                     other than the one loaded last
 //                     (findPartitionwithleastWalker, :149-171); ties, which the
 //                     reference breaks by unordered_map order, go to the
-//                     partition loaded longest ago;
+//                     partition used longest ago;
 //   zero-copy       = a partition that is not cached and has fewer waiting
 //                     walkers than the threshold is read over the host link
-//                     (shouldZerocopy, :243-252).
+//                     (shouldZerocopy, :243-252);
+//   no look-ahead loads (the reference loads the partition it is about to
+//                     compute, :173-213).
 // The FIFO policy restates the FIFO_SCHE variant (:113-127, :391-418).
-// The learned policy (mlp.h) orders the same decisions by predicted arrivals.
+// The learned policy (mlp.h) keeps these rules but scores partitions by the
+// walker arrivals a small MLP predicts, and loads predicted partitions ahead.
 #pragma once
 
 #include <cstdint>
+#include <cstring>
 #include <vector>
+
+#include "../../include/lighttraffic.h"
 
 namespace lt {
 
 struct SchedView {
     uint32_t P = 0;
+    uint32_t K = 0;                      // cache slots
     const uint64_t *waiting = nullptr;   // P: walkers waiting per partition (device + host + not yet created)
+    const uint64_t *lazy = nullptr;      // P: of those, walkers not yet created
     const int32_t *slot_of = nullptr;    // P: cache slot or -1
     const uint64_t *last_used = nullptr; // P: iteration the partition was last loaded or computed
-    const uint32_t *arrivals = nullptr;  // P: walkers that arrived in the last iteration
+    const uint32_t *arrivals = nullptr;  // P: walkers queued at each partition in the last iteration
+    const uint32_t *visits = nullptr;    // P: walkers that entered each partition (cached or not) in it
     uint64_t iteration = 0;
+    uint64_t zc_threshold = 0;           // walkers below which a cold partition is read zero-copy
 };
 
 class Policy {
@@ -37,10 +47,30 @@ public:
     virtual bool next(const SchedView &v, int32_t prev_computed, bool sync, uint32_t &choice);
     // findPartitionwithleastWalker over cached partitions other than `except`; -1 if none.
     virtual int32_t victim(const SchedView &v, int32_t except, uint32_t incoming);
-    // Partitions worth loading ahead of need (best first); plain: by waiting walkers.
-    virtual void prefetch_order(const SchedView &v, uint32_t exclude, std::vector<uint32_t> &out);
-    // Called after every iteration with the walkers that arrived per partition.
+    // shouldZerocopy for a partition that is not cached.
+    virtual bool zero_copy(const SchedView &v, uint32_t p, uint64_t threshold) { return v.waiting[p] < threshold; }
+    // Look-ahead loads: candidates (best first), how many per iteration, and
+    // the cached partition to give up for candidate c (-1: do not load c).
+    virtual void prefetch_order(const SchedView &v, uint32_t exclude, std::vector<uint32_t> &out) { out.clear(); }
+    virtual size_t prefetch_depth(const SchedView &v) { return 0; }
+    virtual int32_t victim_for_prefetch(const SchedView &v, int32_t computing, uint32_t c) { return -1; }
+    // Called after every iteration; v.arrivals holds that iteration's arrivals.
     virtual void observe(const SchedView &v) {}
+    // Single-pass mode: every partition stays readable -- cached, or read
+    // zero-copy from pinned host memory -- so walkers never queue and every
+    // batch of walkers finishes in one step kernel; the policy only chooses
+    // which partitions hold cache slots, by cache_score (higher = keep), and
+    // swaps at most swap_budget partitions per batch.
+    virtual bool single_pass() const { return false; }
+    virtual double cache_score(const SchedView &v, uint32_t p) { return 0.0; }
+    virtual size_t swap_budget() const { return 0; }
+    // Cache emptied (the learned state of a policy survives).
+    virtual void reset() {}
+    virtual void stats(lt_policy_stats &s) const
+    {
+        std::memset(&s, 0, sizeof s);
+        std::strncpy(s.name, name(), sizeof s.name - 1);
+    }
     virtual const char *name() const { return "plain"; }
 };
 
@@ -50,6 +80,7 @@ class FifoPolicy : public Policy {
 public:
     bool next(const SchedView &v, int32_t prev_computed, bool sync, uint32_t &choice) override;
     int32_t victim(const SchedView &v, int32_t except, uint32_t incoming) override;
+    void reset() override { cursor_ = 0; }
     const char *name() const override { return "fifo"; }
 };
 

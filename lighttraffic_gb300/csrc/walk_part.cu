@@ -60,13 +60,18 @@ __global__ void __launch_bounds__(kPartBlock) walk_part_kernel(StepArgs a)
     const bool in_smem = P <= kSmemPartMax;
     uint32_t *s_off = smem;
     uint32_t *s_hist = smem + (P + 1);
+    uint32_t *s_visit = s_hist + P;
     if (in_smem) {
         for (uint32_t i = threadIdx.x; i <= P; i += blockDim.x) s_off[i] = a.t.node_off[i];
-        for (uint32_t i = threadIdx.x; i < P; i += blockDim.x) s_hist[i] = 0;
+        for (uint32_t i = threadIdx.x; i < P; i += blockDim.x) {
+            s_hist[i] = 0;
+            s_visit[i] = 0;
+        }
     }
     __syncthreads();
     const uint32_t *off = in_smem ? s_off : a.t.node_off;
     uint32_t *hist = in_smem ? s_hist : a.hist;
+    uint32_t *visit = in_smem ? s_visit : a.visits;
 
     const int lane = threadIdx.x & 31;
     const unsigned lt_mask = (1u << lane) - 1u;
@@ -102,10 +107,8 @@ __global__ void __launch_bounds__(kPartBlock) walk_part_kernel(StepArgs a)
                 } else if (my < total) {
                     const uint64_t t = a.lazy_begin + (my - a.n_chunk_walkers);
                     if (a.lazy_mode == kStartPerVertex) {
-                        const uint32_t nb = a.t.node_off[a.lazy_part];
-                        const uint32_t n = a.t.node_off[a.lazy_part + 1] - nb;
-                        idx = (uint32_t)per_vertex_id(t, nb, n, a.V);
-                        cur = nb + (uint32_t)(t % n);
+                        idx = (uint32_t)per_vertex_id(t, a.lazy_nb, a.lazy_n, a.V);
+                        cur = a.lazy_nb + (uint32_t)(t % a.lazy_n);
                     } else {
                         idx = (uint32_t)t;
                         cur = start_vertex(a.lazy_mode, a.source, a.V, a.seed, a.run, idx);
@@ -139,17 +142,20 @@ __global__ void __launch_bounds__(kPartBlock) walk_part_kernel(StepArgs a)
             }
             if (need_graph && (cur < cp_nb || cur >= cp_ne)) {
                 const uint32_t p = find_part(off, P, cur);
-                const unsigned long long rp = a.t.rp_addr[p];
+                atomicAdd(&visit[p], 1u);
+                const bool zc = p == a.zc_part;
+                const unsigned long long rp = zc ? (a.zc_rp | 1ull)
+                                                 : *(volatile const unsigned long long *)&a.t.rp_addr[p];
                 if (rp == 0ull) {
                     emit = true;
                     dest = p;
                 } else {
                     cp_nb = off[p];
                     cp_ne = off[p + 1];
-                    cp_rp = rp;
-                    cp_col = a.t.col_addr[p];
+                    cp_rp = rp & ~1ull;
+                    cp_col = zc ? a.zc_col : *(volatile const unsigned long long *)&a.t.col_addr[p];
                     cp_eb = a.t.edge_off[p];
-                    cp_zc = a.t.host_mapped[p] != 0;
+                    cp_zc = (rp & 1ull) != 0;
                 }
             }
         }
@@ -265,8 +271,10 @@ __global__ void __launch_bounds__(kPartBlock) walk_part_kernel(StepArgs a)
     }
     if (in_smem) {
         __syncthreads();
-        for (uint32_t i = threadIdx.x; i < P; i += blockDim.x)
+        for (uint32_t i = threadIdx.x; i < P; i += blockDim.x) {
             if (s_hist[i]) atomicAdd(&a.hist[i], s_hist[i]);
+            if (s_visit[i]) atomicAdd(&a.visits[i], s_visit[i]);
+        }
     }
 }
 
@@ -323,6 +331,8 @@ __global__ void __launch_bounds__(kPartBlock) scatter_kernel(ScatterArgs a)
 template <int APP>
 int occ_part(size_t smem)
 {
+    if (smem > 48 * 1024)
+        cudaFuncSetAttribute(walk_part_kernel<APP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     int n = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, walk_part_kernel<APP>, kPartBlock, smem);
     return n;
@@ -330,7 +340,7 @@ int occ_part(size_t smem)
 
 }  // namespace
 
-size_t part_smem(uint32_t P) { return P <= kSmemPartMax ? sizeof(uint32_t) * (2ull * P + 1) : 0; }
+size_t part_smem(uint32_t P) { return P <= kSmemPartMax ? sizeof(uint32_t) * (3ull * P + 1) : 0; }
 
 int part_grid(int app, int /*start*/, int device, size_t smem)
 {

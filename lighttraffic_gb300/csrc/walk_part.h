@@ -15,18 +15,20 @@ namespace lt {
 constexpr uint32_t kChunk = 8192;                         // walkers per chunk
 constexpr uint64_t kChunkBytes = 12ull * kChunk;           // 96 KiB
 constexpr int kPartBlock = 256;
-constexpr uint32_t kSmemPartMax = 8192;                    // P up to this keeps node_off / histograms in smem
+constexpr uint32_t kSmemPartMax = 4096;                    // P up to this keeps node_off / histograms in smem
 
 // Device view of the partition table: node / edge ranges of every partition
-// and, for partitions readable by the kernel (cached in a device slot, or
-// mapped from pinned host memory for a zero-copy pass), the addresses of
-// their rowptr slice (n+1 global edge offsets) and col slice.
+// and, for readable partitions, the addresses of their rowptr slice (n+1
+// global edge offsets) and col slice -- a device cache slot, or pinned host
+// memory read zero-copy, marked by bit 0 of the rowptr address.  An entry may
+// change while a step kernel runs only from unreadable or zero-copy to a
+// cache slot whose copy has completed; a slot is never overwritten while a
+// kernel that may read it runs.
 struct PartTable {
     const uint32_t *node_off;             // P+1
     const uint64_t *edge_off;             // P+1
     const unsigned long long *rp_addr;    // P, 0 = not readable
     const unsigned long long *col_addr;   // P
-    const uint8_t *host_mapped;           // P, 1 = the slice is read over the host link (zero-copy)
     uint32_t P;
 };
 
@@ -37,7 +39,7 @@ struct StepArgs {
     uint64_t n_chunk_walkers;      // walkers in those chunks ((n-1) * kChunk + tail fill)
     uint64_t lazy_begin;           // first lazy ordinal to create
     uint64_t lazy_count;           // lazy walkers to create in this pass
-    uint32_t lazy_part;            // partition the lazy walkers start in
+    uint32_t lazy_nb, lazy_n;      // per-vertex starts: vertex range [lazy_nb, lazy_nb + lazy_n)
     int lazy_mode;                 // lt::Start of the lazy walkers
     uint64_t W;                    // walkers of the run (per-vertex ordinal mapping)
     uint32_t V;
@@ -53,8 +55,13 @@ struct StepArgs {
     uint32_t *out_cur, *out_step, *out_idx, *out_dest;
     unsigned long long *out_n;     // staged walkers (atomic)
     uint32_t *hist;                // P: staged walkers per destination
+    uint32_t *visits;              // P: walkers entering each partition (readable or not)
     unsigned long long *next;      // scratch: next input ordinal
     unsigned long long *stats;     // 8: updates, moves, teleports, zc moves, exits, finished, -, -
+    // partition read zero-copy in this launch (0xFFFFFFFF = none) and its
+    // device-visible addresses of pinned host memory
+    uint32_t zc_part;
+    unsigned long long zc_rp, zc_col;
 };
 
 struct ScatterArgs {

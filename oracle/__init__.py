@@ -237,3 +237,37 @@ def ref_partition(bcsr_path: str, max_bytes: int):
     pairs = [tuple(int(x) for x in l.split()) for l in lines]
     return (np.array([p[0] for p in pairs], dtype=np.uint32),
             np.array([p[1] for p in pairs], dtype=np.uint64))
+
+
+# ------------------------------------------------- learned prefetcher MLP
+
+MLP_IN, MLP_HIDDEN = 16, 64
+MLP_PARAMS = MLP_IN * MLP_HIDDEN + 2 * MLP_HIDDEN + 1
+
+
+def mlp_forward_backward(x, y, params):
+    """Float64 restatement of the prefetcher network: 2 layers, ReLU, mean
+    squared error.  Parameter layout W1[i*H+j] | b1 | W2 | b2.  Returns
+    (pred, grad, loss)."""
+    F, H = MLP_IN, MLP_HIDDEN
+    x = np.asarray(x, np.float64).reshape(-1, F)
+    y = np.asarray(y, np.float64).reshape(-1)
+    p = np.asarray(params, np.float64)
+    W1 = p[: F * H].reshape(F, H)
+    b1 = p[F * H: F * H + H]
+    W2 = p[F * H + H: F * H + 2 * H]
+    b2 = p[-1]
+    a = x @ W1 + b1
+    h = np.maximum(a, 0.0)
+    pred = h @ W2 + b2
+    n = len(x)
+    diff = pred - y
+    loss = float(np.mean(diff * diff))
+    dy = 2.0 * diff / n
+    gW2 = h.T @ dy
+    gb2 = dy.sum()
+    da = dy[:, None] * W2[None, :] * (a > 0)
+    gW1 = x.T @ da
+    gb1 = da.sum(axis=0)
+    grad = np.concatenate([gW1.ravel(), gb1, gW2, [gb2]])
+    return pred, grad, loss

@@ -1,0 +1,32 @@
+"""Learned prefetcher vs the plain (reference) scheduler.
+
+Both schedules must give bit-identical visit counts (the random stream is
+keyed by walker and step).  What the trained network gains over the method
+without it is measured on the engine's own traces: its mean squared error
+predicting per-partition visits over the next iterations, against the moving
+average of visits it replaces (the frequency policy's predictor).
+"""
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def test_learned_matches_plain_and_beats_moving_average(lt, require_gpu):
+    g = lt.Graph.rmat(20, 1 << 24, seed=1, part_bytes=1 << 20)
+    V = g.num_nodes
+    assert g.num_partitions > 40
+    runs = {}
+    for name, sched in [("plain", lt.SCHED_PLAIN), ("frequency", lt.SCHED_FREQUENCY), ("learned", lt.SCHED_LEARNED)]:
+        e = lt.Engine(g, partitions=12, seed=1, sched=sched)
+        counts = e.ppr(0, 8 * V, 0.15)
+        s = e.stats()
+        runs[name] = (counts, s, e.policy_stats())
+        link = s["h2d_graph_bytes"] + s["h2d_walker_bytes"] + s["d2h_walker_bytes"] + s["zerocopy_bytes"]
+        print(name, "iterations", s["iterations"], "loads", s["partition_loads"],
+              "bytes/step %.1f" % (link / s["moves"]), "ms %.1f" % s["running_ms"])
+    assert (runs["plain"][0] == runs["learned"][0]).all()
+    assert (runs["plain"][0] == runs["frequency"][0]).all()
+    ps = runs["learned"][2]
+    assert ps["name"] == "learned" and ps["train_steps"] >= 20 and ps["predictions"] >= 10
+    print("network loss %.5f, moving-average loss %.5f" % (ps["net_loss"], ps["baseline_loss"]))
+    assert ps["net_loss"] < ps["baseline_loss"]

@@ -31,6 +31,8 @@ CASES = [
     (4, 0, None, 0),         # default threshold partitionSize/128/2
     (3, 20000, 0, 0),        # tiny walker pool: host spills
     (5, 0, 0, 1),            # FIFO policy
+    (4, 0, None, 2),         # learned: cache by predicted visits, the rest zero-copy
+    (2, 20000, None, 3),     # frequency ablation
 ]
 
 
@@ -46,7 +48,9 @@ def test_ppr_ooc(lt, require_gpu, g16, case):
     assert (got == want).all()
     s = e.stats()
     assert s["moves"] == st[1]
-    assert s["iterations"] > 1
+    assert s["iterations"] >= 1
+    if sched >= 2:
+        return                                   # single pass: no queues, no spills
     if zc == 0:
         assert s["h2d_graph_bytes"] > 0 and s["zerocopy_calls"] == 0
     if zc == 1 << 40:
