@@ -226,6 +226,39 @@ lt_status lt_walk_device_noalloc(int app, int start_mode, const uint64_t *d_rowp
                                  uint64_t *d_counts, uint32_t *d_endpoints, uint32_t *d_paths,
                                  uint64_t *d_stats, void *stream);
 
+/* ------------------------------------------------- batched multi-source PPR */
+
+/* Many PPR queries in one persistent launch (no counterpart in the
+ * reference, which runs one source per process, app/ppr.cu:96-113).  Query q
+ * runs walkers[q] walks from sources[q] keyed by seeds[q] (NULL: the engine
+ * seed for every query), so its counts equal lt_run_ppr(sources[q],
+ * walkers[q]) on an engine with that seed, alone or in any batch.  Output:
+ * the (vertex, count) pairs of query q are out_vertices / out_counts
+ * [out_offsets[q], out_offsets[q+1]), u32 counts, pairs of one query in
+ * unspecified order.  out_offsets holds n+1 entries; out_capacity must be at
+ * least the sum of walkers[].  Needs every partition cached on the device.
+ * The batch pipeline is captured in a CUDA graph on first use and replayed. */
+lt_status lt_ppr_batch(lt_engine *e, uint32_t n, const uint32_t *sources, const uint64_t *walkers,
+                       const uint64_t *seeds, float prob, uint64_t *out_offsets, uint32_t *out_vertices,
+                       uint32_t *out_counts, uint64_t out_capacity);
+/* The same on device buffers, on `stream`; returns without waiting. */
+lt_status lt_ppr_batch_device(lt_engine *e, uint32_t n, const uint32_t *d_sources, const uint64_t *d_walkers,
+                              const uint64_t *d_seeds, float prob, uint64_t *d_out_offsets,
+                              uint32_t *d_out_vertices, uint32_t *d_out_counts, uint64_t out_capacity,
+                              void *stream);
+
+typedef struct lt_batch_tune {
+    int block;        /* threads per CTA of the walk kernel */
+    int ctas_per_sm;  /* 0 = occupancy maximum */
+    int load_shift;   /* per-query table capacity = next_pow2(walkers << load_shift) */
+    int tuned;        /* 1 once lt_engine_autotune ran */
+} lt_batch_tune;
+
+/* Time the batch pipeline on a synthetic batch for each block size and table
+ * load factor and keep the fastest for this engine. */
+lt_status lt_engine_autotune(lt_engine *e);
+lt_status lt_engine_batch_tune(const lt_engine *e, lt_batch_tune *out);
+
 /* ------------------------------------------------------ learned prefetcher */
 
 typedef struct lt_policy_stats {

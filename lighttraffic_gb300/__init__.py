@@ -52,6 +52,10 @@ class EngineCfg(C.Structure):
                 ("ctas_per_sm", C.c_int)]
 
 
+class BatchTune(C.Structure):
+    _fields_ = [("block", C.c_int), ("ctas_per_sm", C.c_int), ("load_shift", C.c_int), ("tuned", C.c_int)]
+
+
 class PolicyStats(C.Structure):
     _fields_ = [("name", C.c_char * 16), ("train_steps", C.c_uint64), ("net_loss", C.c_double),
                 ("baseline_loss", C.c_double), ("predictions", C.c_uint64)]
@@ -106,6 +110,10 @@ def _load():
         "lt_engine_stats": ([vp, C.POINTER(Stats)], C.c_int),
         "lt_walk_scratch_bytes": ([], C.c_size_t),
         "lt_engine_policy_stats": ([vp, C.POINTER(PolicyStats)], C.c_int),
+        "lt_ppr_batch": ([vp, C.c_uint32, u32p, u64p, u64p, C.c_float, u64p, u32p, u32p, C.c_uint64], C.c_int),
+        "lt_ppr_batch_device": ([vp, C.c_uint32, vp, vp, vp, C.c_float, vp, vp, vp, C.c_uint64, vp], C.c_int),
+        "lt_engine_autotune": ([vp], C.c_int),
+        "lt_engine_batch_tune": ([vp, C.POINTER(BatchTune)], C.c_int),
         "lt_mlp_check": ([C.c_int, C.c_uint32, C.POINTER(C.c_float), C.POINTER(C.c_float),
                           C.POINTER(C.c_float), C.c_float, C.c_float, C.POINTER(C.c_float),
                           C.POINTER(C.c_float), C.POINTER(C.c_float), C.POINTER(C.c_float)], C.c_int),
@@ -293,6 +301,31 @@ class Engine:
         check(lib.lt_run_walk(self._h, walkers, length, run, start, _ptr(ep, C.c_uint32),
                               _ptr(pa, C.c_uint32)))
         return ep, pa
+
+    def ppr_batch(self, sources, walkers, seeds=None, prob: float = 0.15):
+        """Batched multi-source PPR: returns (offsets[n+1], vertices, counts);
+        query q's pairs are [offsets[q], offsets[q+1])."""
+        src = np.ascontiguousarray(sources, dtype=np.uint32)
+        w = np.ascontiguousarray(walkers, dtype=np.uint64)
+        sd = None if seeds is None else np.ascontiguousarray(seeds, dtype=np.uint64)
+        n = len(src)
+        cap = int(w.sum())
+        off = np.zeros(n + 1, np.uint64)
+        v = np.zeros(max(1, cap), np.uint32)
+        c = np.zeros(max(1, cap), np.uint32)
+        check(lib.lt_ppr_batch(self._h, n, _ptr(src, C.c_uint32), _ptr(w, C.c_uint64), _ptr(sd, C.c_uint64),
+                               prob, _ptr(off, C.c_uint64), _ptr(v, C.c_uint32), _ptr(c, C.c_uint32), cap))
+        tot = int(off[-1])
+        return off, v[:tot], c[:tot]
+
+    def autotune(self) -> dict:
+        check(lib.lt_engine_autotune(self._h))
+        return self.batch_tune()
+
+    def batch_tune(self) -> dict:
+        t = BatchTune()
+        check(lib.lt_engine_batch_tune(self._h, C.byref(t)))
+        return {"block": t.block, "ctas_per_sm": t.ctas_per_sm, "load_shift": t.load_shift, "tuned": bool(t.tuned)}
 
     def policy_stats(self) -> dict:
         s = PolicyStats()

@@ -247,6 +247,43 @@ lt_status lt_engine_policy_stats(const lt_engine *e, lt_policy_stats *out)
 
 size_t lt_walk_scratch_bytes(void) { return walk_scratch_bytes(); }
 
+lt_status lt_ppr_batch(lt_engine *e, uint32_t n, const uint32_t *sources, const uint64_t *walkers,
+                       const uint64_t *seeds, float prob, uint64_t *out_offsets, uint32_t *out_vertices,
+                       uint32_t *out_counts, uint64_t out_capacity)
+{
+    if (!e || !sources || !walkers || !out_offsets || !out_vertices || !out_counts)
+        return fail(LT_ERR_INVALID, "null argument");
+    return batch_run(e, n, sources, walkers, seeds, prob, out_offsets, out_vertices, out_counts, out_capacity);
+}
+
+lt_status lt_ppr_batch_device(lt_engine *e, uint32_t n, const uint32_t *d_sources, const uint64_t *d_walkers,
+                              const uint64_t *d_seeds, float prob, uint64_t *d_out_offsets,
+                              uint32_t *d_out_vertices, uint32_t *d_out_counts, uint64_t out_capacity,
+                              void *stream)
+{
+    if (!e || !d_sources || !d_walkers || !d_seeds || !d_out_offsets || !d_out_vertices || !d_out_counts)
+        return fail(LT_ERR_INVALID, "null argument");
+    return batch_run_device(e, n, d_sources, d_walkers, d_seeds, prob, d_out_offsets, d_out_vertices, d_out_counts,
+                            out_capacity, (cudaStream_t)stream);
+}
+
+lt_status lt_engine_autotune(lt_engine *e)
+{
+    if (!e) return fail(LT_ERR_INVALID, "null engine");
+    return batch_autotune(e);
+}
+
+lt_status lt_engine_batch_tune(const lt_engine *e, lt_batch_tune *out)
+{
+    if (!e || !out) return fail(LT_ERR_INVALID, "null argument");
+    const BatchTune t = batch_tune(e);
+    out->block = t.block;
+    out->ctas_per_sm = t.ctas_per_sm;
+    out->load_shift = t.load_shift;
+    out->tuned = t.tuned ? 1 : 0;
+    return LT_OK;
+}
+
 lt_status lt_walk_device(int app, int start_mode, const uint64_t *d_rowptr, const uint32_t *d_col, uint32_t num_nodes,
                          uint32_t source, uint64_t num_walkers, uint32_t length, float prob, uint32_t run,
                          uint64_t seed, uint64_t *d_counts, uint32_t *d_endpoints, uint32_t *d_paths,

@@ -129,6 +129,7 @@ void engine_destroy(lt_engine *e)
     cudaSetDevice(e->device);
     if (e->s_compute) cudaStreamSynchronize(e->s_compute);
     if (e->ooc) ooc_destroy(e->ooc);
+    if (e->batch) batch_destroy(e->batch);
     for (void *p : {(void *)e->d_rowptr, (void *)e->d_col, (void *)e->d_counts, e->d_scratch, (void *)e->d_stats,
                     (void *)e->d_endpoints, (void *)e->d_paths})
         if (p) cudaFree(p);
@@ -183,6 +184,12 @@ lt_status load_all(lt_engine *e)
 }
 
 }  // namespace
+
+lt_status engine_ensure_loaded(lt_engine *e)
+{
+    if (!e->resident) return LT_OK;
+    return load_all(e);
+}
 
 lt_status engine_run(lt_engine *e, int app, int start, uint32_t source, uint64_t W, uint32_t length, uint32_t runs,
                      uint32_t run_base, float prob, uint64_t *counts_out, uint32_t *endpoints_out,

@@ -7,6 +7,7 @@
 
 #include "common.h"
 #include "graph.h"
+#include "batch.h"
 #include "ooc.h"
 
 namespace lt {
@@ -37,7 +38,8 @@ struct lt_engine {
     uint32_t *d_paths = nullptr;
     uint64_t paths_cap = 0;
 
-    lt::Ooc *ooc = nullptr;  // out-of-core state when not every partition is cached
+    lt::Ooc *ooc = nullptr;          // out-of-core state when not every partition is cached
+    lt::BatchState *batch = nullptr;  // batched multi-source PPR buffers and captured graph
 
     lt_stats stats{};
 };
@@ -46,6 +48,8 @@ namespace lt {
 lt_status engine_create(lt_graph *g, const lt_engine_cfg &cfg, lt_engine **out);
 void engine_destroy(lt_engine *e);
 lt_status engine_drop_cache(lt_engine *e);
+// Resident mode: copy the graph to the device if it is not there yet.
+lt_status engine_ensure_loaded(lt_engine *e);
 lt_status engine_run(lt_engine *e, int app, int start, uint32_t source, uint64_t W, uint32_t length, uint32_t runs,
                      uint32_t run_base, float prob, uint64_t *counts_out, uint32_t *endpoints_out,
                      uint32_t *paths_out);

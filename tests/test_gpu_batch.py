@@ -1,0 +1,91 @@
+"""Batched multi-source PPR: every query's sparse counts equal the oracle's
+PPR with that query's seed, alone or in any batch, before and after tuning."""
+import numpy as np
+import pytest
+
+import oracle
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def graph16():
+    return oracle.rmat(16, 1 << 20, seed=21)
+
+
+def _as_dict(off, v, c, q):
+    a, b = int(off[q]), int(off[q + 1])
+    return dict(zip(v[a:b].tolist(), c[a:b].tolist()))
+
+
+def _oracle_dict(rp, col, src, w, seed):
+    counts, _, _ = oracle.ppr(rp, col, src, w, prob=0.15, seed=seed)
+    nz = np.nonzero(counts)[0]
+    return dict(zip(nz.tolist(), counts[nz].astype(np.uint32).tolist()))
+
+
+def test_batch_matches_oracle(lt, require_gpu, graph16):
+    rp, col = graph16
+    V = len(rp) - 1
+    g = lt.Graph.from_csr(rp, col, 1 << 30)
+    e = lt.Engine(g, seed=5)
+    rng = np.random.default_rng(3)
+    n = 60
+    src = rng.integers(0, V, n).astype(np.uint32)
+    src[:5] = 0                                   # repeated sources are distinct queries
+    w = rng.integers(1, 20000, n).astype(np.uint64)
+    w[7] = 1
+    seeds = rng.integers(1, 1 << 62, n, dtype=np.uint64)
+    off, v, c = e.ppr_batch(src, w, seeds)
+    assert off[0] == 0 and len(off) == n + 1
+    for q in range(n):
+        got = _as_dict(off, v, c, q)
+        assert sum(got.values()) == int(w[q])
+        assert got == _oracle_dict(rp, col, int(src[q]), int(w[q]), int(seeds[q])), q
+
+
+def test_alone_equals_in_mix_and_single_run(lt, require_gpu, graph16):
+    rp, col = graph16
+    V = len(rp) - 1
+    g = lt.Graph.from_csr(rp, col, 1 << 30)
+    e = lt.Engine(g, seed=77)
+    src = np.array([3, 11, 3, 900, 4000], np.uint32)
+    w = np.array([5000, 300, 7000, 1, 20000], np.uint64)
+    seeds = np.array([77, 8, 9, 10, 11], np.uint64)
+    off, v, c = e.ppr_batch(src, w, seeds)
+    for q in range(len(src)):
+        o1, v1, c1 = e.ppr_batch(src[q:q + 1], w[q:q + 1], seeds[q:q + 1])
+        assert _as_dict(o1, v1, c1, 0) == _as_dict(off, v, c, q)
+    # query 0 uses the engine seed: equals the single-source run
+    dense = e.ppr(3, 5000, 0.15)
+    nz = np.nonzero(dense)[0]
+    assert _as_dict(off, v, c, 0) == dict(zip(nz.tolist(), dense[nz].astype(np.uint32).tolist()))
+
+
+def test_autotune_and_replay(lt, require_gpu, graph16):
+    rp, col = graph16
+    V = len(rp) - 1
+    g = lt.Graph.from_csr(rp, col, 1 << 30)
+    e = lt.Engine(g, seed=1)
+    src = (np.arange(200, dtype=np.uint64) * 97 % V).astype(np.uint32)
+    w = (np.arange(200, dtype=np.uint64) % 13 + 1) * 500
+    seeds = np.arange(200, dtype=np.uint64) + 1000
+    before = e.ppr_batch(src, w, seeds)
+    t = e.autotune()
+    assert t["tuned"] and t["block"] in (128, 256, 512) and t["load_shift"] in (1, 2)
+    after = e.ppr_batch(src, w, seeds)
+    for q in range(0, 200, 17):
+        assert _as_dict(*before, q) == _as_dict(*after, q)
+    # replays with other batch sizes reuse the captured graph
+    for n in (1, 37, 200):
+        o, v, c = e.ppr_batch(src[:n], w[:n], seeds[:n])
+        for q in range(0, n, 11):
+            assert _as_dict(o, v, c, q) == _as_dict(*before, q)
+
+
+def test_batch_needs_resident_graph(lt, require_gpu, graph16):
+    rp, col = graph16
+    g = lt.Graph.from_csr(rp, col, 256 << 10)
+    e = lt.Engine(g, partitions=2)
+    with pytest.raises(lt.LTError):
+        e.ppr_batch([0], [10])
