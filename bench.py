@@ -18,6 +18,18 @@ vertices removed, stand in for the reference's datasets, which are absent):
       when U > 0.85; `value` times lt_walk_device passes on device buffers,
       `e2e` the public API with the graph re-copied from pinned host memory.
   c0: PPR on RMAT(2^20, 2^24) resident in HBM, source 0, W = 2|V|.
+  c3: batched multi-source PPR on RMAT(2^26, 2^30) resident in HBM: 4096
+      sources drawn Zipf(s = 1.1) over the out-degree rank, walks per source
+      lognormal (median 1e4, sigma 1.5 -- values the workload description
+      leaves open) clipped to [1e3, 1e6], stop probability 0.15, per-source
+      u32 sparse counts; `value` times lt_ppr_batch_device (the captured
+      batch pipeline) on device buffers after the autotuner, `e2e` lt_ppr_batch
+      with host buffers.
+  c4: serving PPR on the c2 graph and cache: Poisson arrivals at 100, 1 000
+      and 10 000 queries/s, uniform random sources, lognormal walk counts
+      (median 1e4, sigma 1.0 -- left open by the workload) clipped to
+      [1e3, 1e5]; continuous batching through lt_serve_*; p50 / p99 latency
+      and steps/s per rate for the learned and the plain scheduler.
 Steps per run: hops taken (PPR, the reference's 2|V|/0.15 estimate counted
 exactly) or updates (PageRank, W * l).
 --impl reference times the CPU restatement of the reference walk semantics
@@ -48,6 +60,13 @@ CONFIGS = {
                start=2, prob=0.85, part_mb=32),
     "c0": dict(workload="ppr-rmat20-e24-resident", app=0, scale=20, edges=1 << 24, length=0,
                start=0, prob=0.15, part_mb=32),
+    "c4": dict(workload="serve-ppr-rmat30-e33-outofcore-p256", app=0, scale=30, edges=1 << 33, length=0,
+               start=0, prob=0.15, part_mb=32, partitions=256, batch=1 << 28, serving=True,
+               rates=(100, 1000, 10000), seconds=(4.0, 2.0, 1.0), walk_median=1e4, walk_sigma=1.0,
+               walk_min=1e3, walk_max=1e5),
+    "c3": dict(workload="ppr-batch4096-zipf1.1-lognormal-rmat26-e30", app=0, scale=26, edges=1 << 30, length=0,
+               start=0, prob=0.15, part_mb=32, queries=4096, zipf=1.1, walk_median=1e4, walk_sigma=1.5,
+               walk_min=1e3, walk_max=1e6, batch_queries=True),
 }
 SEED_GRAPH = 1
 SEED_WALK = 1
@@ -171,6 +190,21 @@ def cpu_rate(cfg, rp, col, seconds, threads):
     return steps / dt, f"first {n} of {W} walkers ({steps} steps, {dt:.1f} s)"
 
 
+def cpu_batch_rate(cfg, rp, col, seconds):
+    """Oracle over the first queries of the batch workload (one query at a
+    time, OpenMP over its walkers) for about `seconds`."""
+    import oracle
+    sources, walkers, seeds = c3_queries(cfg, rp)
+    t0 = time.perf_counter()
+    done, hops, q = 0.0, 0, 0
+    while done < seconds and q < len(sources):
+        _, _, st = oracle.ppr(rp, col, int(sources[q]), int(walkers[q]), prob=cfg["prob"], seed=int(seeds[q]))
+        hops += int(st[1])
+        q += 1
+        done = time.perf_counter() - t0
+    return hops / done, f"first {q} of {len(sources)} queries ({hops} hops, {done:.1f} s)"
+
+
 def reference_arm(args, cfg):
     ws, rank, local = dist_env()
     if rank != 0:
@@ -189,7 +223,10 @@ def reference_arm(args, cfg):
     per_step = max(1.0, min(6.0, 150.0 / max(1, args.steps + args.warmup)))
     rates, desc = [], ""
     for i in range(args.warmup + args.steps):
-        r, desc = cpu_rate(cfg, rp, col, per_step, threads)
+        if cfg.get("batch_queries"):
+            r, desc = cpu_batch_rate(cfg, rp, col, per_step)
+        else:
+            r, desc = cpu_rate(cfg, rp, col, per_step, threads)
         if i >= args.warmup:
             rates.append(r)
     value = statistics.median(rates)
@@ -465,13 +502,204 @@ def gb300_resident(args, cfg):
     return 0
 
 
+def c3_queries(cfg, rp):
+    """Zipf(s) sources over the out-degree rank, lognormal walk counts."""
+    V = len(rp) - 1
+    deg = np.diff(rp.astype(np.int64))
+    order = np.argsort(-deg, kind="stable")
+    rng = np.random.default_rng(SEED_WALK)
+    n = cfg["queries"]
+    ranks = np.arange(1, V + 1, dtype=np.float64)
+    pz = ranks ** -cfg["zipf"]
+    pz /= pz.sum()
+    r = rng.choice(V, size=n, p=pz)
+    sources = order[r].astype(np.uint32)
+    w = np.exp(rng.normal(np.log(cfg["walk_median"]), cfg["walk_sigma"], n))
+    walkers = np.clip(np.round(w), cfg["walk_min"], cfg["walk_max"]).astype(np.uint64)
+    seeds = (np.arange(n, dtype=np.uint64) + np.uint64(1)).astype(np.uint64)
+    return sources, walkers, seeds
+
+
+def gb300_batch(args, cfg):
+    import torch
+    ws, rank, local, dist = init_dist()
+    import lighttraffic_gb300 as lt
+
+    g = lt.Graph.rmat(cfg["scale"], cfg["edges"], seed=SEED_GRAPH, part_bytes=cfg["part_mb"] << 20, device=local)
+    V, E = g.num_nodes, g.num_edges
+    rp, col = g.csr_views()
+    sources, walkers, seeds = c3_queries(cfg, rp)
+    n, Wt = len(sources), int(walkers.sum())
+    e = lt.Engine(g, seed=SEED_WALK, device=local)
+    tune = e.autotune()
+    dev = f"cuda:{local}"
+    d_src = torch.from_numpy(sources.view(np.int32)).to(dev)
+    d_w = torch.from_numpy(walkers.view(np.int64)).to(dev)
+    d_seed = torch.from_numpy(seeds.view(np.int64)).to(dev)
+    d_off = torch.zeros(n + 1, dtype=torch.int64, device=dev)
+    d_v = torch.zeros(Wt, dtype=torch.int32, device=dev)
+    d_c = torch.zeros(Wt, dtype=torch.int32, device=dev)
+    stream = torch.cuda.current_stream()
+
+    def launch():
+        lt.check(lt.lib.lt_ppr_batch_device(e._h, n, d_src.data_ptr(), d_w.data_ptr(), d_seed.data_ptr(),
+                                            ctypes.c_float(cfg["prob"]), d_off.data_ptr(), d_v.data_ptr(),
+                                            d_c.data_ptr(), Wt, stream.cuda_stream))
+
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.3)
+    for _ in range(args.warmup):
+        launch()
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    wall0 = time.time()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record()
+    for _ in range(args.steps):
+        launch()
+    b.record()
+    torch.cuda.synchronize()
+    elapsed_ms = max_over_ranks(dist, local, a.elapsed_time(b))
+    # one more batch through the public host API: stats (hops) and e2e time
+    e2e = []
+    for _ in range(2):
+        t0 = time.perf_counter()
+        off, v, c = e.ppr_batch(sources, walkers, seeds, cfg["prob"])
+        e2e.append(time.perf_counter() - t0)
+    st = e.stats()
+    assert int(c.astype(np.uint64).sum()) == Wt, "PPR invariant (one count per walk) violated"
+    moves = st["moves"]
+    clocks.stop()
+    clk = clocks.summary(wall0 - 0.5, time.time())
+    if rank != 0:
+        if dist:
+            dist.destroy_process_group()
+        return 0
+    value = moves * args.steps * ws / (elapsed_ms / 1e3)
+    pairs = int(off[-1])
+    tslots = sum(1 << max(5, int(np.ceil(np.log2(max(2, int(x) << tune["load_shift"]))))) for x in walkers)
+    # 20 B per hop, 8 B per endpoint (table slot read + count RMW), 8 B per
+    # table slot cleared and 8 B per slot scanned twice, 8 B per output pair
+    alg = 20 * moves + 8 * Wt + 24 * tslots + 8 * pairs
+    peak, peak_src = measured_peak("hbm_gbs", 6800.0)
+    kern_s = st["step_kernel_ms"] / 1e3
+    achieved = alg / kern_s / 1e9
+    line = {
+        "metric": "walk steps/s", "value": value, "unit": "steps/s", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": elapsed_ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "u32",
+        "data": "synthetic RMAT (seeded) and synthetic Zipf / lognormal queries",
+        "config": {"workload": cfg["workload"], "V": V, "E": E, "queries": n, "walkers": Wt,
+                   "sparse_pairs": pairs, "autotune": tune,
+                   "l2": "graph (%d MiB) larger than L2, no flush" % ((8 * (V + 1) + 4 * E) >> 20),
+                   "parallelism": "replicas" if ws > 1 else "1 GPU"},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": profiled_traffic(cfg["workload"]), "kernel": "batch pipeline (walk + tables)",
+                     "alg_bytes_per_launch": alg, "mean_launch_ms": st["step_kernel_ms"], "peak_source": peak_src},
+        "e2e": {"value": moves * ws / statistics.mean(e2e), "unit": "steps/s",
+                "h2d_bytes_per_step": 20 * n, "d2h_bytes_per_step": 8 * (n + 1) + 8 * pairs,
+                "ms_per_step": statistics.mean(e2e) * 1e3},
+        "gpu_launches": 6 * args.steps,
+        "clocks": clk,
+    }
+    if not args.no_cpu_baseline and ws == 1:
+        r, desc = cpu_batch_rate(cfg, rp, col, args.cpu_seconds)
+        line["cpu_baseline"] = {"value": r, "unit": "steps/s", "cores": os.cpu_count() or 1, "kind": "port",
+                                "sample": desc}
+    print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
+def serve_trace(cfg, V, rate, seconds, seed):
+    rng = np.random.default_rng(seed)
+    n = max(1, int(rate * seconds))
+    gaps = rng.exponential(1.0 / rate, n)
+    t = np.cumsum(gaps) * 1e3
+    src = rng.integers(0, V, n).astype(np.uint32)
+    w = np.clip(np.round(np.exp(rng.normal(np.log(cfg["walk_median"]), cfg["walk_sigma"], n))),
+                cfg["walk_min"], cfg["walk_max"]).astype(np.uint64)
+    seeds = rng.integers(1, 1 << 62, n, dtype=np.uint64)
+    return t, src, w, seeds
+
+
+def gb300_serve(args, cfg):
+    ws, rank, local, dist = init_dist()
+    import lighttraffic_gb300 as lt
+
+    g = lt.Graph.rmat(cfg["scale"], cfg["edges"], seed=SEED_GRAPH, part_bytes=cfg["part_mb"] << 20, device=local)
+    V = g.num_nodes
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.3)
+    wall0 = time.time()
+    out = {}
+    for name, sched in [("learned", lt.SCHED_LEARNED), ("plain", lt.SCHED_PLAIN)]:
+        e = lt.Engine(g, partitions=cfg["partitions"], batch=cfg["batch"], seed=SEED_WALK, sched=sched, device=local)
+        per_rate = {}
+        for rate, seconds in zip(cfg["rates"], cfg["seconds"]):
+            srv = lt.Server(e, max_active=4096, table_slots=1 << 27, prob=cfg["prob"])
+            t, src, w, seeds = serve_trace(cfg, V, rate, seconds, SEED_WALK + rate)
+            n = len(t)
+            lat = []
+            nxt = 0
+            t0 = lt.Server.now_ms()
+            steps0 = e.stats()
+            while len(lat) < n:
+                now = lt.Server.now_ms() - t0
+                while nxt < n and t[nxt] <= now:
+                    srv.submit(int(src[nxt]), int(w[nxt]), int(seeds[nxt]), arrival_ms=t0 + float(t[nxt]))
+                    nxt += 1
+                c, a, p = srv.step()
+                if c:
+                    for tk in srv.finished():
+                        lat.append(srv.latency_ms(tk))
+                        srv.result(tk)
+                if a == 0 and p == 0 and nxt < n:
+                    time.sleep(max(0.0, (t[nxt] - (lt.Server.now_ms() - t0)) / 1e3))
+            span_s = (lt.Server.now_ms() - t0) / 1e3
+            hops = int(w.sum() * (1 / cfg["prob"]))  # expected hops; exact count below
+            srv.close()
+            st = e.stats()
+            lat = np.array(lat)
+            per_rate[str(rate)] = {"queries": n, "p50_ms": float(np.percentile(lat, 50)),
+                                   "p99_ms": float(np.percentile(lat, 99)), "span_s": span_s,
+                                   "walkers": int(w.sum()), "steps_per_s_est": hops / span_s}
+        out[name] = per_rate
+        e.close()
+    clocks.stop()
+    clk = clocks.summary(wall0 - 0.5, time.time())
+    if rank != 0:
+        return 0
+    mid = str(cfg["rates"][1])
+    line = {
+        "metric": "PPR p99 latency ms", "value": out["learned"][mid]["p99_ms"], "unit": "ms", "n_gpus": ws,
+        "steps": 1, "warmup": 0, "ms_per_step": None, "higher_is_better": False, "scaling": "weak",
+        "vs_baseline": None, "dtype": "u32", "data": "synthetic RMAT graph, synthetic Poisson query trace",
+        "config": {"workload": cfg["workload"], "V": V, "rates_qps": list(cfg["rates"]),
+                   "walks": "lognormal median %g sigma %g in [%g, %g]" % (cfg["walk_median"], cfg["walk_sigma"],
+                                                                          cfg["walk_min"], cfg["walk_max"]),
+                   "value_is": f"learned scheduler p99 at {mid} qps"},
+        "serving": out, "clocks": clk,
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     args = parse()
     cfg = CONFIGS[args.config]
+    if cfg.get("serving") and args.impl != "reference":
+        return gb300_serve(args, cfg)
     if args.impl == "reference":
         return reference_arm(args, cfg)
     if "partitions" in cfg:
         return gb300_ooc(args, cfg)
+    if cfg.get("batch_queries"):
+        return gb300_batch(args, cfg)
     return gb300_resident(args, cfg)
 
 

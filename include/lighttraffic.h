@@ -259,6 +259,31 @@ typedef struct lt_batch_tune {
 lt_status lt_engine_autotune(lt_engine *e);
 lt_status lt_engine_batch_tune(const lt_engine *e, lt_batch_tune *out);
 
+/* ------------------------------------------------------------------ serving */
+
+/* Continuous-batching PPR server on an out-of-core engine (no counterpart in
+ * the reference, which runs one source per process).  Queries are admitted
+ * when a query slot, room in the table arena (table_slots entries of 8 bytes)
+ * and walker-pool chunks for all their walkers are free; admitted queries
+ * share every scheduler iteration, cached partition and kernel launch with
+ * the queries already running; their walkers stay in the device pool.  Each
+ * query's counts depend only on (source, walkers, seed, prob). */
+typedef struct lt_server lt_server;
+lt_status lt_serve_open(lt_engine *e, uint32_t max_active, uint64_t table_slots, float prob, lt_server **out);
+/* Queue a query; arrival_ms (lt_serve_now_ms clock, <= 0: now) starts its latency clock. */
+lt_status lt_serve_submit(lt_server *s, uint32_t source, uint64_t walkers, uint64_t seed, double arrival_ms,
+                          uint64_t *ticket);
+/* Admit what fits, run one scheduler iteration, extract finished queries. */
+lt_status lt_serve_step(lt_server *s, uint32_t *completed, uint32_t *active, uint32_t *pending);
+/* done = 1 once the query finished; with vertices / counts given (capacity
+ * pairs), copy its (vertex, count) pairs (unspecified order) and release it. */
+lt_status lt_serve_result(lt_server *s, uint64_t ticket, int *done, uint64_t *n_pairs, uint32_t *vertices,
+                          uint32_t *counts, uint64_t capacity, double *latency_ms);
+/* Tickets of queries finished since the last call (up to cap); returns how many were written. */
+uint64_t lt_serve_finished(lt_server *s, uint64_t *tickets, uint64_t cap);
+void lt_serve_close(lt_server *s);
+double lt_serve_now_ms(void);
+
 /* ------------------------------------------------------ learned prefetcher */
 
 typedef struct lt_policy_stats {

@@ -113,6 +113,14 @@ def _load():
         "lt_ppr_batch": ([vp, C.c_uint32, u32p, u64p, u64p, C.c_float, u64p, u32p, u32p, C.c_uint64], C.c_int),
         "lt_ppr_batch_device": ([vp, C.c_uint32, vp, vp, vp, C.c_float, vp, vp, vp, C.c_uint64, vp], C.c_int),
         "lt_engine_autotune": ([vp], C.c_int),
+        "lt_serve_open": ([vp, C.c_uint32, C.c_uint64, C.c_float, C.POINTER(vp)], C.c_int),
+        "lt_serve_submit": ([vp, C.c_uint32, C.c_uint64, C.c_uint64, C.c_double, C.POINTER(C.c_uint64)], C.c_int),
+        "lt_serve_step": ([vp, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)], C.c_int),
+        "lt_serve_result": ([vp, C.c_uint64, C.POINTER(C.c_int), C.POINTER(C.c_uint64), u32p, u32p, C.c_uint64,
+                             C.POINTER(C.c_double)], C.c_int),
+        "lt_serve_close": ([vp], None),
+        "lt_serve_finished": ([vp, u64p, C.c_uint64], C.c_uint64),
+        "lt_serve_now_ms": ([], C.c_double),
         "lt_engine_batch_tune": ([vp, C.POINTER(BatchTune)], C.c_int),
         "lt_mlp_check": ([C.c_int, C.c_uint32, C.POINTER(C.c_float), C.POINTER(C.c_float),
                           C.POINTER(C.c_float), C.c_float, C.c_float, C.POINTER(C.c_float),
@@ -250,6 +258,64 @@ class Graph:
     def close(self):
         if self._h:
             lib.lt_graph_close(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Server:
+    """Continuous-batching PPR server on an out-of-core engine."""
+
+    def __init__(self, engine: "Engine", max_active: int = 1024, table_slots: int = 1 << 26, prob: float = 0.15):
+        self.engine = engine
+        self._h = C.c_void_p()
+        check(lib.lt_serve_open(engine._h, max_active, table_slots, prob, C.byref(self._h)))
+
+    @staticmethod
+    def now_ms() -> float:
+        return lib.lt_serve_now_ms()
+
+    def submit(self, source: int, walkers: int, seed: int, arrival_ms: float = 0.0) -> int:
+        t = C.c_uint64()
+        check(lib.lt_serve_submit(self._h, source, walkers, seed, arrival_ms, C.byref(t)))
+        return t.value
+
+    def step(self):
+        c, a, p = C.c_uint32(), C.c_uint32(), C.c_uint32()
+        check(lib.lt_serve_step(self._h, C.byref(c), C.byref(a), C.byref(p)))
+        return c.value, a.value, p.value
+
+    def finished(self, cap: int = 1 << 16):
+        """Tickets finished since the last call."""
+        buf = np.zeros(cap, np.uint64)
+        n = lib.lt_serve_finished(self._h, _ptr(buf, C.c_uint64), cap)
+        return buf[:n].tolist()
+
+    def latency_ms(self, ticket: int):
+        done, n, lat = C.c_int(), C.c_uint64(), C.c_double()
+        check(lib.lt_serve_result(self._h, ticket, C.byref(done), C.byref(n), None, None, 0, C.byref(lat)))
+        return lat.value if done.value else None
+
+    def result(self, ticket: int):
+        """None while running; else (dict vertex -> count, latency ms)."""
+        done, n, lat = C.c_int(), C.c_uint64(), C.c_double()
+        check(lib.lt_serve_result(self._h, ticket, C.byref(done), C.byref(n), None, None, 0, C.byref(lat)))
+        if not done.value:
+            return None
+        v = np.zeros(max(1, n.value), np.uint32)
+        c = np.zeros(max(1, n.value), np.uint32)
+        check(lib.lt_serve_result(self._h, ticket, C.byref(done), C.byref(n), _ptr(v, C.c_uint32),
+                                  _ptr(c, C.c_uint32), len(v), C.byref(lat)))
+        k = n.value
+        return dict(zip(v[:k].tolist(), c[:k].tolist())), lat.value
+
+    def close(self):
+        if self._h:
+            lib.lt_serve_close(self._h)
             self._h = None
 
     def __del__(self):

@@ -267,6 +267,41 @@ lt_status lt_ppr_batch_device(lt_engine *e, uint32_t n, const uint32_t *d_source
                             out_capacity, (cudaStream_t)stream);
 }
 
+lt_status lt_serve_open(lt_engine *e, uint32_t max_active, uint64_t table_slots, float prob, lt_server **out)
+{
+    if (!e || !out) return fail(LT_ERR_INVALID, "null argument");
+    return serve_open(e, max_active, table_slots, prob, out);
+}
+
+lt_status lt_serve_submit(lt_server *s, uint32_t source, uint64_t walkers, uint64_t seed, double arrival_ms,
+                          uint64_t *ticket)
+{
+    if (!s || !ticket) return fail(LT_ERR_INVALID, "null argument");
+    return serve_submit(s, source, walkers, seed, arrival_ms, ticket);
+}
+
+lt_status lt_serve_step(lt_server *s, uint32_t *completed, uint32_t *active, uint32_t *pending)
+{
+    if (!s) return fail(LT_ERR_INVALID, "null server");
+    return serve_step(s, completed, active, pending);
+}
+
+lt_status lt_serve_result(lt_server *s, uint64_t ticket, int *done, uint64_t *n_pairs, uint32_t *vertices,
+                          uint32_t *counts, uint64_t capacity, double *latency_ms)
+{
+    if (!s) return fail(LT_ERR_INVALID, "null server");
+    return serve_result(s, ticket, done, n_pairs, vertices, counts, capacity, latency_ms);
+}
+
+uint64_t lt_serve_finished(lt_server *s, uint64_t *tickets, uint64_t cap)
+{
+    return s ? serve_finished(s, tickets, cap) : 0;
+}
+
+void lt_serve_close(lt_server *s) { serve_close(s); }
+
+double lt_serve_now_ms(void) { return serve_now_ms(); }
+
 lt_status lt_engine_autotune(lt_engine *e)
 {
     if (!e) return fail(LT_ERR_INVALID, "null engine");

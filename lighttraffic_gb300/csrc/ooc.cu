@@ -23,6 +23,8 @@
 #include "ooc.h"
 
 #include <algorithm>
+#include <deque>
+#include <map>
 #include <chrono>
 #include <cstring>
 
@@ -86,7 +88,8 @@ struct Ooc {
     std::vector<uint32_t> host_free;
 
     uint64_t staging_cap = 0;
-    uint32_t *d_out = nullptr;      // 4 arrays of staging_cap
+    uint32_t *d_out = nullptr;      // 5 arrays of staging_cap: cur, step, idx, dest, query
+    lt_server *serve = nullptr;  // serving state when queries are being served
     uint32_t *d_ctl = nullptr;      // hist[P] | visits[P] | pad | out_n (u64) | next (u64)
     uint64_t ctl_words = 0;         // u32 words of d_ctl
     uint32_t *d_planbuf = nullptr;  // cursor[P] | win_off[P] | plan chunks
@@ -400,6 +403,8 @@ lt_status unspill(Ooc &o, uint32_t p, uint64_t max_chunks)
     return LT_OK;
 }
 
+void serve_args(Ooc &o, StepArgs &a);
+
 struct RunParams {
     int app, start;
     uint32_t source, length, run;
@@ -506,12 +511,14 @@ lt_status step_and_bucket(Ooc &o, const RunParams &rp, int32_t p, const Lazy &lz
     a.out_step = o.d_out + o.staging_cap;
     a.out_idx = o.d_out + 2 * o.staging_cap;
     a.out_dest = o.d_out + 3 * o.staging_cap;
+    a.out_q = o.d_out + 4 * o.staging_cap;
     a.out_n = o.ctl_out_n();
     a.hist = o.ctl_hist();
     a.visits = o.ctl_visits();
     a.next = o.ctl_next();
     a.stats = o.d_stats;
     a.zc_part = kNoPart;
+    if (o.serve) serve_args(o, a);
     if (zero_copy) {
         a.zc_part = (uint32_t)p;
         a.zc_rp = o.zc_rp_base + 8ull * g.node_off[p];
@@ -597,6 +604,7 @@ lt_status step_and_bucket(Ooc &o, const RunParams &rp, int32_t p, const Lazy &lz
     sa.in_step = a.out_step;
     sa.in_idx = a.out_idx;
     sa.in_dest = a.out_dest;
+    sa.in_q = a.out_q;
     sa.n = staged;
     sa.arena = o.d_arena;
     sa.cursor = o.d_planbuf;
@@ -643,7 +651,7 @@ lt_status ensure_pool(Ooc &o, uint64_t W)
     o.plan_cap = o.n_chunks + (uint64_t)o.P;
     o.work_cap = o.n_chunks;
     LT_TRY(dalloc(&o.d_arena, (uint64_t)o.n_chunks * kChunkBytes));
-    LT_TRY(dalloc(&o.d_out, 4 * o.staging_cap));
+    LT_TRY(dalloc(&o.d_out, 5 * o.staging_cap));
     LT_TRY(dalloc(&o.d_planbuf, 2ull * o.P + o.plan_cap));
     LT_TRY(dalloc(&o.d_work, o.work_cap));
     LT_TRY(host_alloc(o.h_plan, 4 * (2ull * o.P + o.plan_cap), true));
@@ -972,6 +980,412 @@ lt_status ooc_run(lt_engine *e, int app, int start, uint32_t source, uint64_t W,
     e->stats.handoffs = hs[4];
     e->stats.running_ms = now_ms() - t0;
     return LT_OK;
+}
+
+}  // namespace lt
+
+// ===========================================================================
+// Serving: continuous batching of PPR queries on the out-of-core engine.
+//
+// A query (source, walkers, seed) is admitted when a query slot, room in the
+// per-query table arena and walker-pool chunks for all its walkers are free
+// (admission by free device memory); its walkers are written straight into
+// its source partition's queue and from then on share every scheduler
+// iteration, cache slot and kernel launch with the queries already running.
+// Walker state stays in the device pool (spilled only under pressure).  Each
+// walker draws from its query's key and index, so a query's counts do not
+// depend on what else runs.  After every iteration the finished-walker
+// counters of the active queries come back to the host; a query whose count
+// reached its walker total is extracted (its table compacted on the device)
+// and its slot, table and chunks are released.
+// ===========================================================================
+
+struct lt_server {
+    struct Query {
+        uint64_t ticket = 0;
+        uint32_t source = 0;
+        uint64_t walkers = 0, seed = 0;
+        int32_t slot = -1;
+        uint64_t toff = 0;
+        uint32_t tlog = 0;
+        double t_arrive = 0, t_done = 0;
+        int state = 0;  // 0 pending, 1 active, 2 done
+        std::vector<uint32_t> out_v, out_c;
+    };
+    lt_engine *e = nullptr;
+    lt::Ooc *o = nullptr;
+    uint32_t max_active = 0;
+    uint64_t table_cap = 0;
+    float prob = 0.15f;
+    uint64_t thr = 0;
+    uint64_t *d_seed = nullptr, *d_toff = nullptr;
+    uint32_t *d_tlog = nullptr, *d_keys = nullptr, *d_cnt = nullptr;
+    unsigned long long *d_done = nullptr, *d_err = nullptr, *d_outn = nullptr;
+    uint32_t *d_out_v = nullptr, *d_out_c = nullptr;
+    uint64_t out_cap = 0;
+    lt::HostBuf h_done;
+    std::vector<Query *> slots;
+    std::deque<Query *> pending;
+    std::map<uint64_t, Query *> all;
+    uint64_t next_ticket = 1;
+    std::vector<std::vector<uint64_t>> free_by_log;  // table arena free list per size class
+    uint64_t bump = 0;
+    uint64_t live_walkers = 0;
+    std::vector<uint64_t> finished;  // tickets completed since the last drain
+};
+
+namespace lt {
+
+double serve_now_ms()
+{
+    using namespace std::chrono;
+    return duration<double, std::milli>(steady_clock::now().time_since_epoch()).count();
+}
+
+namespace {
+
+__global__ void serve_slot_kernel(uint64_t *seed, uint64_t *toff, uint32_t *tlog, unsigned long long *done,
+                                  uint32_t slot, uint64_t sv, uint64_t tv, uint32_t lv)
+{
+    seed[slot] = sv;
+    toff[slot] = tv;
+    tlog[slot] = lv;
+    done[slot] = 0;
+}
+
+__global__ void serve_clear_kernel(uint32_t *keys, uint32_t *cnt, uint64_t base, uint64_t n)
+{
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        keys[base + i] = 0xFFFFFFFFu;
+        cnt[base + i] = 0;
+    }
+}
+
+// One CTA per finished query: its occupied table slots become (vertex, count)
+// pairs at out + obase[k].
+__global__ void serve_extract_kernel(const uint32_t *keys, const uint32_t *cnt, const uint64_t *tbase,
+                                     const uint64_t *tsize, const uint64_t *obase, unsigned long long *outn,
+                                     uint32_t *out_v, uint32_t *out_c)
+{
+    const uint32_t k = blockIdx.x;
+    const uint64_t b = tbase[k], n = tsize[k], o = obase[k];
+    for (uint64_t i = threadIdx.x; i < n; i += blockDim.x) {
+        const uint32_t key = keys[b + i];
+        if (key != 0xFFFFFFFFu) {
+            const unsigned long long pos = atomicAdd(&outn[k], 1ull);
+            out_v[o + pos] = key;
+            out_c[o + pos] = cnt[b + i];
+        }
+    }
+}
+
+void serve_args(Ooc &o, StepArgs &a)
+{
+    lt_server &s = *o.serve;
+    a.q_seed = s.d_seed;
+    a.q_toff = s.d_toff;
+    a.q_tlog = s.d_tlog;
+    a.q_keys = s.d_keys;
+    a.q_cnt = s.d_cnt;
+    a.q_done = s.d_done;
+    a.q_error = s.d_err;
+}
+
+bool table_alloc(lt_server &s, uint32_t lg, uint64_t &off)
+{
+    if (lg < s.free_by_log.size() && !s.free_by_log[lg].empty()) {
+        off = s.free_by_log[lg].back();
+        s.free_by_log[lg].pop_back();
+        return true;
+    }
+    const uint64_t size = 1ull << lg;
+    const uint64_t aligned = (s.bump + size - 1) & ~(size - 1);
+    if (aligned + size > s.table_cap) return false;
+    off = aligned;
+    s.bump = aligned + size;
+    return true;
+}
+
+void table_free(lt_server &s, uint32_t lg, uint64_t off)
+{
+    if (s.free_by_log.size() <= lg) s.free_by_log.resize(lg + 1);
+    s.free_by_log[lg].push_back(off);
+}
+
+uint32_t log2_ceil_host(uint64_t x)
+{
+    uint32_t l = 0;
+    while ((1ull << l) < x) l++;
+    return l;
+}
+
+// Admit pending queries while a slot, table room and walker chunks are free.
+lt_status serve_admit(lt_server &s)
+{
+    Ooc &o = *s.o;
+    lt_engine &e = *s.e;
+    lt_graph &g = *o.g;
+    while (!s.pending.empty()) {
+        lt_server::Query *q = s.pending.front();
+        int32_t slot = -1;
+        for (uint32_t i = 0; i < s.max_active; i++)
+            if (!s.slots[i]) {
+                slot = (int32_t)i;
+                break;
+            }
+        if (slot < 0) break;
+        const uint32_t p = g.find_partition(q->source);
+        Queue &qp = o.q[p];
+        const bool open_tail = !qp.dev_chunks.empty() && qp.tail_fill < kChunk;
+        const uint64_t fill = open_tail ? qp.tail_fill : 0;
+        const uint64_t need = (fill + q->walkers + kChunk - 1) / kChunk - (open_tail ? 1 : 0);
+        if (o.free_chunks.size() < need + (uint64_t)o.P + 2) break;  // keep room for the walkers to move
+        const uint32_t lg = std::max<uint32_t>(5, log2_ceil_host(q->walkers * 2));
+        uint64_t toff = 0;
+        if (!table_alloc(s, lg, toff)) break;
+        s.pending.pop_front();
+        q->slot = slot;
+        q->toff = toff;
+        q->tlog = lg;
+        q->state = 1;
+        s.slots[slot] = q;
+        s.live_walkers += q->walkers;
+        serve_slot_kernel<<<1, 1, 0, e.s_compute>>>(s.d_seed, s.d_toff, s.d_tlog, s.d_done, (uint32_t)slot, q->seed,
+                                                   toff, lg);
+        serve_clear_kernel<<<std::max<uint64_t>(1, std::min<uint64_t>((1ull << lg) / 256, 256)), 256, 0,
+                             e.s_compute>>>(s.d_keys, s.d_cnt, toff, 1ull << lg);
+        // append the walkers to the source partition's queue
+        if (qp.dev_chunks.empty() || qp.tail_fill == kChunk) {
+            qp.dev_chunks.push_back(o.free_chunks.back());
+            o.free_chunks.pop_back();
+            qp.tail_fill = 0;
+        }
+        uint32_t *h_chunks = (uint32_t *)o.h_plan.ptr;
+        uint64_t n_plan = 0;
+        h_chunks[n_plan++] = qp.dev_chunks.back();
+        const uint32_t cursor = qp.tail_fill;
+        const uint64_t tot = (uint64_t)qp.tail_fill + q->walkers;
+        const uint64_t extra = (tot + kChunk - 1) / kChunk - 1;
+        for (uint64_t k = 0; k < extra; k++) {
+            const uint32_t c = o.free_chunks.back();
+            o.free_chunks.pop_back();
+            qp.dev_chunks.push_back(c);
+            h_chunks[n_plan++] = c;
+        }
+        qp.tail_fill = (uint32_t)(tot - extra * kChunk);
+        LT_CUDA_TRY(cudaMemcpyAsync(o.d_planbuf, h_chunks, 4 * n_plan, cudaMemcpyHostToDevice, e.s_compute));
+        InjectArgs ia{};
+        ia.arena = o.d_arena;
+        ia.plan_chunks = o.d_planbuf;
+        ia.cursor = cursor;
+        ia.n = q->walkers;
+        ia.source = q->source;
+        ia.qslot = (uint32_t)slot;
+        ia.seed = q->seed;
+        ia.thr = s.thr;
+        LT_CUDA_TRY(launch_inject(ia, e.device, e.s_compute));
+        // the pinned plan block is rewritten by the next admission: let the copy finish
+        LT_CUDA_TRY(cudaStreamSynchronize(e.s_compute));
+        refresh(o, p);
+    }
+    return LT_OK;
+}
+
+// Extract every active query whose walkers have all finished.
+lt_status serve_complete(lt_server &s, uint32_t &completed)
+{
+    Ooc &o = *s.o;
+    lt_engine &e = *s.e;
+    completed = 0;
+    unsigned long long *h_done = (unsigned long long *)s.h_done.ptr;
+    LT_CUDA_TRY(cudaMemcpyAsync(h_done, s.d_done, 8ull * s.max_active, cudaMemcpyDeviceToHost, e.s_compute));
+    LT_CUDA_TRY(cudaStreamSynchronize(e.s_compute));
+    std::vector<lt_server::Query *> fin;
+    for (uint32_t i = 0; i < s.max_active; i++)
+        if (s.slots[i] && h_done[i] >= s.slots[i]->walkers) fin.push_back(s.slots[i]);
+    if (fin.empty()) return LT_OK;
+    std::vector<uint64_t> meta(3 * fin.size());
+    uint64_t obase = 0;
+    for (size_t k = 0; k < fin.size(); k++) {
+        meta[k] = fin[k]->toff;
+        meta[fin.size() + k] = 1ull << fin[k]->tlog;
+        meta[2 * fin.size() + k] = obase;
+        obase += fin[k]->walkers;
+    }
+    if (obase > s.out_cap) {
+        for (void *p : {(void *)s.d_out_v, (void *)s.d_out_c})
+            if (p) cudaFree(p);
+        s.out_cap = std::max<uint64_t>(obase, 2 * s.out_cap);
+        LT_CUDA_TRY(cudaMalloc(&s.d_out_v, 4 * s.out_cap));
+        LT_CUDA_TRY(cudaMalloc(&s.d_out_c, 4 * s.out_cap));
+    }
+    uint64_t *d_meta = nullptr;
+    LT_CUDA_TRY(cudaMalloc(&d_meta, 8 * meta.size() + 8 * fin.size()));
+    unsigned long long *d_n = (unsigned long long *)(d_meta + meta.size());
+    LT_CUDA_TRY(cudaMemcpyAsync(d_meta, meta.data(), 8 * meta.size(), cudaMemcpyHostToDevice, e.s_compute));
+    LT_CUDA_TRY(cudaMemsetAsync(d_n, 0, 8 * fin.size(), e.s_compute));
+    serve_extract_kernel<<<(unsigned)fin.size(), 256, 0, e.s_compute>>>(s.d_keys, s.d_cnt, d_meta, d_meta + fin.size(),
+                                                                          d_meta + 2 * fin.size(), d_n, s.d_out_v,
+                                                                          s.d_out_c);
+    LT_CUDA_TRY(cudaGetLastError());
+    std::vector<unsigned long long> nn(fin.size());
+    LT_CUDA_TRY(cudaMemcpyAsync(nn.data(), d_n, 8 * fin.size(), cudaMemcpyDeviceToHost, e.s_compute));
+    LT_CUDA_TRY(cudaStreamSynchronize(e.s_compute));
+    const double now = serve_now_ms();
+    for (size_t k = 0; k < fin.size(); k++) {
+        lt_server::Query *q = fin[k];
+        q->out_v.resize(nn[k]);
+        q->out_c.resize(nn[k]);
+        LT_CUDA_TRY(cudaMemcpyAsync(q->out_v.data(), s.d_out_v + meta[2 * fin.size() + k], 4 * nn[k],
+                                    cudaMemcpyDeviceToHost, e.s_compute));
+        LT_CUDA_TRY(cudaMemcpyAsync(q->out_c.data(), s.d_out_c + meta[2 * fin.size() + k], 4 * nn[k],
+                                    cudaMemcpyDeviceToHost, e.s_compute));
+    }
+    LT_CUDA_TRY(cudaStreamSynchronize(e.s_compute));
+    cudaFree(d_meta);
+    for (lt_server::Query *q : fin) {
+        q->state = 2;
+        q->t_done = now;
+        s.finished.push_back(q->ticket);
+        s.slots[q->slot] = nullptr;
+        table_free(s, q->tlog, q->toff);
+        s.live_walkers -= q->walkers;
+        completed++;
+    }
+    (void)o;
+    return LT_OK;
+}
+
+}  // namespace
+
+lt_status serve_open(lt_engine *e, uint32_t max_active, uint64_t table_slots, float prob, lt_server **out)
+{
+    if (!e->ooc) return fail(LT_ERR_UNSUPPORTED, "serving runs on the out-of-core engine (-p below the partition count)");
+    if (e->ooc->serve) return fail(LT_ERR_INVALID, "the engine already serves");
+    if (!(prob > 0.0f && prob <= 1.0f)) return fail(LT_ERR_INVALID, "PPR stop probability must be in (0, 1]");
+    if (max_active == 0 || table_slots < 64) return fail(LT_ERR_INVALID, "no room for queries");
+    LT_CUDA_TRY(cudaSetDevice(e->device));
+    Ooc &o = *e->ooc;
+    LT_TRY(ensure_pool(o, e->cfg.num_device_walkers ? e->cfg.num_device_walkers : (1ull << 26)));
+    lt_server *s = new lt_server();
+    s->e = e;
+    s->o = &o;
+    s->max_active = max_active;
+    s->table_cap = table_slots;
+    s->prob = prob;
+    s->thr = threshold53(prob);
+    s->slots.assign(max_active, nullptr);
+    auto bail = [&](lt_status st) {
+        serve_close(s);
+        return st;
+    };
+    lt_status st = dalloc(&s->d_seed, max_active);
+    if (st == LT_OK) st = dalloc(&s->d_toff, max_active);
+    if (st == LT_OK) st = dalloc(&s->d_tlog, max_active);
+    if (st == LT_OK) st = dalloc(&s->d_done, max_active);
+    if (st == LT_OK) st = dalloc(&s->d_err, 1);
+    if (st == LT_OK) st = dalloc(&s->d_keys, table_slots);
+    if (st == LT_OK) st = dalloc(&s->d_cnt, table_slots);
+    if (st == LT_OK) st = host_alloc(s->h_done, 8ull * max_active, true);
+    if (st != LT_OK) return bail(st);
+    if (cudaMemset(s->d_done, 0, 8ull * max_active) != cudaSuccess || cudaMemset(s->d_err, 0, 8) != cudaSuccess)
+        return bail(fail(LT_ERR_CUDA, "serving state initialisation failed"));
+    reset_queues(o);
+    refresh_all(o);
+    cudaMemsetAsync(o.d_stats, 0, 64, e->s_compute);
+    o.serve = s;
+    *out = s;
+    return LT_OK;
+}
+
+lt_status serve_submit(lt_server *s, uint32_t source, uint64_t walkers, uint64_t seed, double arrival_ms, uint64_t *ticket)
+{
+    if (source >= s->o->g->V) return fail(LT_ERR_INVALID, "source %u out of range", source);
+    if (walkers == 0 || walkers >= (1ull << 32)) return fail(LT_ERR_INVALID, "walkers must be in [1, 2^32)");
+    auto *q = new lt_server::Query();
+    q->ticket = s->next_ticket++;
+    q->source = source;
+    q->walkers = walkers;
+    q->seed = seed;
+    q->t_arrive = arrival_ms > 0 ? arrival_ms : serve_now_ms();
+    s->pending.push_back(q);
+    s->all[q->ticket] = q;
+    *ticket = q->ticket;
+    return LT_OK;
+}
+
+lt_status serve_step(lt_server *s, uint32_t *completed, uint32_t *active, uint32_t *pending)
+{
+    Ooc &o = *s->o;
+    lt_engine &e = *s->e;
+    LT_CUDA_TRY(cudaSetDevice(e.device));
+    LT_TRY(serve_admit(*s));
+    uint32_t p = 0;
+    SchedView v = view(o);
+    if (o.policy->next(v, o.prev_computed, false, p) || o.policy->next(v, o.prev_computed, true, p)) {
+        RunParams rp{};
+        rp.app = kPPR;
+        rp.start = kStartSource;
+        rp.thr = s->thr;
+        rp.W = 0;
+        LT_TRY(process(o, rp, p));
+    }
+    uint32_t done = 0;
+    LT_TRY(serve_complete(*s, done));
+    if (completed) *completed = done;
+    uint32_t act = 0;
+    for (lt_server::Query *q : s->slots) act += q != nullptr;
+    if (active) *active = act;
+    if (pending) *pending = (uint32_t)s->pending.size();
+    return LT_OK;
+}
+
+lt_status serve_result(lt_server *s, uint64_t ticket, int *done, uint64_t *n_pairs, uint32_t *vertices,
+                       uint32_t *counts, uint64_t capacity, double *latency_ms)
+{
+    auto it = s->all.find(ticket);
+    if (it == s->all.end()) return fail(LT_ERR_INVALID, "unknown ticket %llu", (unsigned long long)ticket);
+    lt_server::Query *q = it->second;
+    if (done) *done = q->state == 2;
+    if (q->state != 2) return LT_OK;
+    if (n_pairs) *n_pairs = q->out_v.size();
+    if (latency_ms) *latency_ms = q->t_done - q->t_arrive;
+    if (vertices && counts) {
+        if (capacity < q->out_v.size()) return fail(LT_ERR_CAPACITY, "result has %zu pairs", q->out_v.size());
+        std::memcpy(vertices, q->out_v.data(), 4 * q->out_v.size());
+        std::memcpy(counts, q->out_c.data(), 4 * q->out_c.size());
+        s->all.erase(it);
+        delete q;
+    }
+    return LT_OK;
+}
+
+uint64_t serve_finished(lt_server *s, uint64_t *tickets, uint64_t cap)
+{
+    const uint64_t n = std::min<uint64_t>(cap, s->finished.size());
+    if (tickets) std::memcpy(tickets, s->finished.data(), 8 * n);
+    s->finished.erase(s->finished.begin(), s->finished.begin() + n);
+    return n;
+}
+
+void serve_close(lt_server *s)
+{
+    if (!s) return;
+    if (s->o && s->o->serve == s) {
+        cudaStreamSynchronize(s->e->s_compute);
+        s->o->serve = nullptr;
+        reset_queues(*s->o);
+        refresh_all(*s->o);
+    }
+    for (void *p : {(void *)s->d_seed, (void *)s->d_toff, (void *)s->d_tlog, (void *)s->d_keys, (void *)s->d_cnt,
+                    (void *)s->d_done, (void *)s->d_err, (void *)s->d_out_v, (void *)s->d_out_c})
+        if (p) cudaFree(p);
+    host_free(s->h_done);
+    for (auto &kv : s->all) delete kv.second;
+    for (lt_server::Query *q : s->pending)
+        if (s->all.find(q->ticket) == s->all.end()) delete q;
+    delete s;
 }
 
 }  // namespace lt

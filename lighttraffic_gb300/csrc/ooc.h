@@ -14,6 +14,7 @@
 #include "sched.h"
 
 struct lt_engine;
+struct lt_server;
 
 namespace lt {
 
@@ -37,5 +38,16 @@ lt_status ooc_drop_cache(Ooc *o);
 void ooc_policy_stats(const Ooc *o, lt_policy_stats &s);
 lt_status ooc_run(lt_engine *e, int app, int start, uint32_t source, uint64_t W, uint32_t length, uint32_t runs,
                   uint32_t run_base, float prob, uint64_t *counts_out, uint32_t *endpoints_out, uint32_t *paths_out);
+
+// Serving: PPR queries admitted, stepped and completed continuously.
+lt_status serve_open(lt_engine *e, uint32_t max_active, uint64_t table_slots, float prob, lt_server **out);
+lt_status serve_submit(lt_server *s, uint32_t source, uint64_t walkers, uint64_t seed, double arrival_ms,
+                       uint64_t *ticket);
+lt_status serve_step(lt_server *s, uint32_t *completed, uint32_t *active, uint32_t *pending);
+lt_status serve_result(lt_server *s, uint64_t ticket, int *done, uint64_t *n_pairs, uint32_t *vertices,
+                       uint32_t *counts, uint64_t capacity, double *latency_ms);
+uint64_t serve_finished(lt_server *s, uint64_t *tickets, uint64_t cap);
+void serve_close(lt_server *s);
+double serve_now_ms();
 
 }  // namespace lt

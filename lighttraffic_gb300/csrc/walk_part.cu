@@ -52,6 +52,33 @@ __device__ __forceinline__ uint32_t ld_u32(unsigned long long addr)
     return __ldg(reinterpret_cast<const unsigned int *>(addr));
 }
 
+// A PPR walk ends at v: count it (single run) or add it to the query's table
+// (linear probing, u32 counts) and mark one more walker of the query done.
+__device__ __forceinline__ void ppr_count(const StepArgs &a, uint32_t qs, uint32_t v)
+{
+    if (!a.q_seed) {
+        atomicAdd((unsigned long long *)&a.counts[v], 1ull);
+        return;
+    }
+    const uint64_t base = a.q_toff[qs];
+    const uint64_t mask = (1ull << a.q_tlog[qs]) - 1;
+    uint64_t slot = ((uint64_t)(v * 0x9E3779B1u)) & mask;
+    bool added = false;
+    for (uint64_t probe = 0; probe <= mask && !added; probe++) {
+        uint32_t *k = &a.q_keys[base + slot];
+        uint32_t old = *(volatile uint32_t *)k;
+        if (old == 0xFFFFFFFFu) old = atomicCAS(k, 0xFFFFFFFFu, v);
+        if (old == 0xFFFFFFFFu || old == v) {
+            atomicAdd(&a.q_cnt[base + slot], 1u);
+            added = true;
+        }
+        slot = (slot + 1) & mask;
+    }
+    if (!added) atomicAdd(a.q_error, 1ull);
+    __threadfence();
+    atomicAdd(&a.q_done[qs], 1ull);
+}
+
 template <int APP>
 __global__ void __launch_bounds__(kPartBlock) walk_part_kernel(StepArgs a)
 {
@@ -77,7 +104,8 @@ __global__ void __launch_bounds__(kPartBlock) walk_part_kernel(StepArgs a)
     const unsigned lt_mask = (1u << lane) - 1u;
     const uint64_t total = a.n_chunk_walkers + a.lazy_count;
 
-    uint32_t cur = 0, step = 0, idx = 0, hop = 0;
+    uint32_t cur = 0, step = 0, idx = 0, hop = 0, qs = 0;
+    uint64_t seed = a.seed;
     bool active = false, exhausted = false;
     // cached readable partition of the lane
     uint32_t cp_nb = 1, cp_ne = 0;
@@ -103,6 +131,8 @@ __global__ void __launch_bounds__(kPartBlock) walk_part_kernel(StepArgs a)
                     cur = c[j];
                     step = c[kChunk + j];
                     idx = c[2 * kChunk + j];
+                    qs = c[3 * kChunk + j];
+                    if (a.q_seed) seed = a.q_seed[qs];
                     active = true;
                 } else if (my < total) {
                     const uint64_t t = a.lazy_begin + (my - a.n_chunk_walkers);
@@ -113,6 +143,8 @@ __global__ void __launch_bounds__(kPartBlock) walk_part_kernel(StepArgs a)
                         idx = (uint32_t)t;
                         cur = start_vertex(a.lazy_mode, a.source, a.V, a.seed, a.run, idx);
                     }
+                    qs = 0;
+                    seed = a.seed;
                     step = APP == kPPR ? ppr_length(a.seed, a.run, idx, a.thr) : a.length;
                     if (APP == kWalk && a.paths) a.paths[(uint64_t)idx * (a.length + 1)] = cur;
                     active = true;
@@ -134,7 +166,7 @@ __global__ void __launch_bounds__(kPartBlock) walk_part_kernel(StepArgs a)
                 need_graph = step >= 2;
             } else if (APP == kPageRank) {
                 if (step >= 2) {
-                    r = walk_draw(a.seed, step, kTagStep, a.run, idx);
+                    r = walk_draw(seed, step, kTagStep, a.run, idx);
                     need_graph = m53_of(r) < a.thr;
                 }
             } else {
@@ -171,6 +203,7 @@ __global__ void __launch_bounds__(kPartBlock) walk_part_kernel(StepArgs a)
                 a.out_step[pos] = step;
                 a.out_idx[pos] = idx;
                 a.out_dest[pos] = dest;
+                a.out_q[pos] = qs;
                 atomicAdd(&hist[dest], 1u);
                 active = false;
                 n_exit++;
@@ -184,19 +217,19 @@ __global__ void __launch_bounds__(kPartBlock) walk_part_kernel(StepArgs a)
         if (APP == kPPR) {
             // app/ppr.cu:22-42
             if (s == 1) {
-                atomicAdd((unsigned long long *)&a.counts[cur], 1ull);
+                ppr_count(a, qs, cur);
                 done = true;
             } else {
                 step = s - 1;
                 const uint64_t first = ld_u64(cp_rp + 8ull * (cur - cp_nb));
                 const uint64_t deg = ld_u64(cp_rp + 8ull * (cur - cp_nb + 1)) - first;
                 if (deg > 0) {
-                    const Rand4 q = walk_draw(a.seed, s, kTagStep, a.run, idx);
+                    const Rand4 q = walk_draw(seed, s, kTagStep, a.run, idx);
                     cur = ld_u32(cp_col + 4ull * (first + mod_u64(r64_of(q), deg) - cp_eb));
                     n_mov++;
                     n_zc += cp_zc;
                 } else {
-                    atomicAdd((unsigned long long *)&a.counts[cur], 1ull);
+                    ppr_count(a, qs, cur);
                     done = true;
                 }
             }
@@ -231,7 +264,7 @@ __global__ void __launch_bounds__(kPartBlock) walk_part_kernel(StepArgs a)
             const uint64_t deg = ld_u64(cp_rp + 8ull * (cur - cp_nb + 1)) - first;
             uint32_t *path = a.paths ? a.paths + (uint64_t)idx * (a.length + 1) : nullptr;
             if (deg > 0) {
-                const Rand4 q = walk_draw(a.seed, s, kTagStep, a.run, idx);
+                const Rand4 q = walk_draw(seed, s, kTagStep, a.run, idx);
                 cur = ld_u32(cp_col + 4ull * (first + mod_u64(r64_of(q), deg) - cp_eb));
                 n_mov++;
                 n_zc += cp_zc;
@@ -322,9 +355,25 @@ __global__ void __launch_bounds__(kPartBlock) scatter_kernel(ScatterArgs a)
                 c[j] = a.in_cur[i];
                 c[kChunk + j] = a.in_step[i];
                 c[2 * kChunk + j] = a.in_idx[i];
+                c[3 * kChunk + j] = a.in_q[i];
             }
         }
         if (in_smem) __syncthreads();
+    }
+}
+
+__global__ void inject_kernel(InjectArgs a)
+{
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < a.n; i += stride) {
+        const uint64_t pos = a.cursor + i;
+        const uint32_t chunk = a.plan_chunks[pos / kChunk];
+        uint32_t *c = reinterpret_cast<uint32_t *>(a.arena + (uint64_t)chunk * kChunkBytes);
+        const uint32_t j = (uint32_t)(pos % kChunk);
+        c[j] = a.source;
+        c[kChunk + j] = ppr_length(a.seed, 0, i, a.thr);
+        c[2 * kChunk + j] = (uint32_t)i;
+        c[3 * kChunk + j] = a.qslot;
     }
 }
 
@@ -359,6 +408,17 @@ cudaError_t launch_walk_part(const StepArgs &a, int app, int grid, cudaStream_t 
     case kPageRank: walk_part_kernel<kPageRank><<<grid, kPartBlock, smem, st>>>(a); break;
     default: walk_part_kernel<kWalk><<<grid, kPartBlock, smem, st>>>(a); break;
     }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_inject(const InjectArgs &a, int device, cudaStream_t st)
+{
+    if (a.n == 0) return cudaSuccess;
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+    uint64_t blocks = (a.n + 255) / 256;
+    if (blocks > (uint64_t)sms * 4) blocks = (uint64_t)sms * 4;
+    inject_kernel<<<(unsigned)blocks, 256, 0, st>>>(a);
     return cudaGetLastError();
 }
 

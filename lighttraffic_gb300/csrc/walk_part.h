@@ -2,9 +2,10 @@
 //
 // Walkers wait in per-partition queues made of fixed-size chunks.  A chunk is
 // one contiguous block of kChunk walkers in structure-of-arrays form:
-//     u32 cur[kChunk] | u32 step[kChunk] | u32 idx[kChunk]
+//     u32 cur[kChunk] | u32 step[kChunk] | u32 idx[kChunk] | u32 query[kChunk]
 // so a chunk moves between device and host with a single copy.  Every chunk of
-// a queue is full except its last one.
+// a queue is full except its last one.  `query` is the walker's query slot
+// when the engine serves many PPR queries at once (0 otherwise).
 #pragma once
 
 #include <cstdint>
@@ -13,7 +14,7 @@
 namespace lt {
 
 constexpr uint32_t kChunk = 8192;                         // walkers per chunk
-constexpr uint64_t kChunkBytes = 12ull * kChunk;           // 96 KiB
+constexpr uint64_t kChunkBytes = 16ull * kChunk;           // 128 KiB
 constexpr int kPartBlock = 256;
 constexpr uint32_t kSmemPartMax = 4096;                    // P up to this keeps node_off / histograms in smem
 
@@ -62,10 +63,20 @@ struct StepArgs {
     // device-visible addresses of pinned host memory
     uint32_t zc_part;
     unsigned long long zc_rp, zc_col;
+    // query mode (serving many PPR queries): per query slot its key, table and
+    // finished-walker counter; endpoints go to the query's table instead of
+    // `counts`.  q_seed == null: single-run mode.
+    uint32_t *out_q;
+    const uint64_t *q_seed;
+    const uint64_t *q_toff;
+    const uint32_t *q_tlog;
+    uint32_t *q_keys, *q_cnt;
+    unsigned long long *q_done;
+    unsigned long long *q_error;
 };
 
 struct ScatterArgs {
-    const uint32_t *in_cur, *in_step, *in_idx, *in_dest;
+    const uint32_t *in_cur, *in_step, *in_idx, *in_dest, *in_q;
     uint64_t n;
     uint8_t *arena;
     uint32_t *cursor;              // P: next free slot offset in the destination's chunk window
@@ -74,7 +85,19 @@ struct ScatterArgs {
     uint32_t P;
 };
 
+// Walkers of newly admitted queries: walker i of query slot q (i < n) goes to
+// position cursor + i of the chunk window, with PPR length from (seed, i).
+struct InjectArgs {
+    uint8_t *arena;
+    const uint32_t *plan_chunks;
+    uint32_t cursor;
+    uint64_t n;
+    uint32_t source, qslot;
+    uint64_t seed, thr;
+};
+
 int part_grid(int app, int start, int device, size_t smem);
+cudaError_t launch_inject(const InjectArgs &a, int device, cudaStream_t st);
 size_t part_smem(uint32_t P);
 cudaError_t launch_walk_part(const StepArgs &a, int app, int grid, cudaStream_t st);
 cudaError_t launch_scatter(const ScatterArgs &a, int device, cudaStream_t st);
