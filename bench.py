@@ -661,13 +661,16 @@ def gb300_serve(args, cfg):
                 if a == 0 and p == 0 and nxt < n:
                     time.sleep(max(0.0, (t[nxt] - (lt.Server.now_ms() - t0)) / 1e3))
             span_s = (lt.Server.now_ms() - t0) / 1e3
-            hops = int(w.sum() * (1 / cfg["prob"]))  # expected hops; exact count below
             srv.close()
             st = e.stats()
             lat = np.array(lat)
+            link = link_bytes(st)
             per_rate[str(rate)] = {"queries": n, "p50_ms": float(np.percentile(lat, 50)),
                                    "p99_ms": float(np.percentile(lat, 99)), "span_s": span_s,
-                                   "walkers": int(w.sum()), "steps_per_s_est": hops / span_s}
+                                   "walkers": int(w.sum()), "steps": st["moves"],
+                                   "steps_per_s": st["moves"] / span_s,
+                                   "bytes_per_step": link / max(1, st["moves"]),
+                                   "iterations": st["iterations"], "partition_loads": st["partition_loads"]}
         out[name] = per_rate
         e.close()
     clocks.stop()

@@ -308,6 +308,11 @@ lt_status lt_engine_policy_stats(const lt_engine *e, lt_policy_stats *out);
 lt_status lt_mlp_check(int device, uint32_t n, const float *x, const float *y, const float *params, float lr,
                        float momentum, float *pred_out, float *grad_out, float *loss_out, float *params_out);
 
+/* The remainder x[i] % d[i] as the walk kernels compute it (host build of the
+ * same code), for checking it against native division.  No counterpart in
+ * the reference. */
+lt_status lt_mod_check(uint64_t n, const uint64_t *x, const uint64_t *d, uint64_t *out);
+
 #ifdef __cplusplus
 }
 #endif

@@ -23,6 +23,7 @@
 
 #include "engine.h"
 #include "lt_core.cuh"
+#include "mem.cuh"
 #include "scan.cuh"
 
 namespace lt {
@@ -203,6 +204,7 @@ __global__ void __launch_bounds__(BLOCK) batch_walk_kernel(BatchArgs a)
 
     const int lane = threadIdx.x & 31;
     const unsigned lt_mask = (1u << lane) - 1u;
+    const uint64_t keep = l2_policy_evict_last(), stream = l2_policy_evict_first();
     uint32_t cur = 0, step = 0, q = 0;
     uint64_t idx = 0, seed = 0;
     bool active = false, exhausted = false;
@@ -241,11 +243,11 @@ __global__ void __launch_bounds__(BLOCK) batch_walk_kernel(BatchArgs a)
             done = true;
         } else {
             step = s - 1;
-            const uint64_t first = __ldg((const unsigned long long *)a.rowptr + cur);
-            const uint64_t deg = __ldg((const unsigned long long *)a.rowptr + cur + 1) - first;
+            const uint64_t first = ld_nc_u64(a.rowptr + cur, keep);
+            const uint64_t deg = ld_nc_u64(a.rowptr + cur + 1, keep) - first;
             if (deg > 0) {
                 const Rand4 r = walk_draw(seed, s, kTagStep, 0, idx);
-                cur = __ldg(a.col + first + mod_u64(r64_of(r), deg));
+                cur = ld_nc_stream_u32(a.col + first + mod_u64(r64_of(r), deg), stream);
                 n_mov++;
             } else {
                 done = true;

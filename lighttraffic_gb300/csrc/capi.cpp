@@ -3,6 +3,7 @@
 #include <new>
 
 #include "engine.h"
+#include "lt_core.cuh"
 
 using namespace lt;
 
@@ -246,6 +247,16 @@ lt_status lt_engine_policy_stats(const lt_engine *e, lt_policy_stats *out)
 }
 
 size_t lt_walk_scratch_bytes(void) { return walk_scratch_bytes(); }
+
+lt_status lt_mod_check(uint64_t n, const uint64_t *x, const uint64_t *d, uint64_t *out)
+{
+    if (!x || !d || !out) return fail(LT_ERR_INVALID, "null argument");
+    for (uint64_t i = 0; i < n; i++) {
+        if (d[i] == 0) return fail(LT_ERR_INVALID, "zero divisor at %llu", (unsigned long long)i);
+        out[i] = mod_u64(x[i], d[i]);
+    }
+    return LT_OK;
+}
 
 lt_status lt_ppr_batch(lt_engine *e, uint32_t n, const uint32_t *sources, const uint64_t *walkers,
                        const uint64_t *seeds, float prob, uint64_t *out_offsets, uint32_t *out_vertices,

@@ -14,6 +14,7 @@
 //   (0, 1]; the test U > p is done exactly in integers as m53 >= floor(p 2^53).
 #pragma once
 
+#include <cmath>
 #include <cstdint>
 #include <cuda_runtime.h>
 
@@ -92,16 +93,57 @@ inline uint64_t threshold53(float p)
     return (uint64_t)(d * 9007199254740992.0);
 }
 
-// r % n for the neighbour / vertex choice.  n fits 32 bits on every graph the
-// engine accepts (degree and V are below 2^32), so the 64-by-32 remainder is
-// split into two 32-bit-divisor steps.
+// x mod d for 0 < d < 2^16: long division in base 2^16 with three 32-bit
+// remainders (every partial value stays below 2^32).
+LT_HD uint32_t mod64_small(uint64_t x, uint32_t d)
+{
+    const uint32_t hi = (uint32_t)(x >> 32), lo = (uint32_t)x;
+    uint32_t r = hi % d;
+    r = ((r << 16) | (lo >> 16)) % d;
+    r = ((r << 16) | (lo & 0xFFFFu)) % d;
+    return r;
+}
+
+LT_HD float rcp_f32(float d)
+{
+#ifdef __CUDA_ARCH__
+    return __frcp_rn(d);
+#else
+    return 1.0f / d;
+#endif
+}
+
+// x mod d for 2^16 <= d < 2^32 without 64-bit division: reduce the high word
+// (32-bit remainder), estimate the quotient of the remaining t = r1 2^32 + lo
+// (t < d 2^32) in single precision, then correct in integers.  The estimate's
+// relative error is below 2^-21, so after the first correction |r| < 1024 d;
+// a second single-precision estimate of r / d (from r >> 16) leaves |r| < 3 d,
+// which the final loops remove.  The result is exact whatever the rounding of
+// the estimates.
+LT_HD uint32_t mod64_large(uint64_t x, uint32_t d)
+{
+    const uint32_t hi = (uint32_t)(x >> 32), lo = (uint32_t)x;
+    const uint32_t r1 = hi % d;
+    const uint64_t t = ((uint64_t)r1 << 32) | lo;
+    const float rd = rcp_f32((float)d);
+    const float qf = ((float)r1 * 4294967296.0f + (float)lo) * rd;
+    const uint32_t q = qf >= 4294967040.0f ? 0xFFFFFF00u : (qf <= 0.0f ? 0u : (uint32_t)qf);
+    int64_t r = (int64_t)(t - (uint64_t)q * d);
+    const int32_t c = (int32_t)floorf((float)(int32_t)(r >> 16) * 65536.0f * rd);
+    r -= (int64_t)c * (int64_t)d;
+    while (r < 0) r += d;
+    while (r >= (int64_t)d) r -= d;
+    return (uint32_t)r;
+}
+
+// r % n for the neighbour / vertex choice, without 64-bit division (which
+// the compiler lowers through the FP64 pipe, slow on this part).  n fits 32
+// bits on every graph the engine accepts (degree and V are below 2^32).
 LT_HD uint64_t mod_u64(uint64_t r, uint64_t n)
 {
     if ((n >> 32) == 0) {
         const uint32_t d = (uint32_t)n;
-        const uint32_t hi = (uint32_t)(r >> 32);
-        const uint64_t t = ((uint64_t)(hi % d) << 32) | (uint32_t)r;
-        return t % d;
+        return d <= 0xFFFFu ? mod64_small(r, d) : mod64_large(r, d);
     }
     return r % n;
 }

@@ -413,6 +413,10 @@ public:
     const char *name() const override { return use_net_ ? "learned" : "frequency"; }
 
     bool single_pass() const override { return false; }
+    // Serving keeps few walkers in flight, so reading cold partitions zero-copy
+    // costs little and lets every admitted query finish in one step; the
+    // network then chooses which partitions hold cache slots.
+    bool serve_single_pass() const override { return true; }
 
     void stats(lt_policy_stats &st) const override
     {
@@ -431,7 +435,10 @@ public:
         st.baseline_loss = n ? b / n : 0.0;
     }
 
-    size_t swap_budget() const override { return 64; }
+    // Few walkers per batch make single scores noisy: swap rarely and only for
+    // a clearly hotter partition, so the cache settles on the hot set.
+    size_t swap_budget() const override { return 4; }
+    double swap_ratio() const override { return 4.0; }
     // Predicted visits once the predictor is trained; before that, the
     // partition's edge count (a hub-heavy RMAT prior).
     double cache_score(const SchedView &v, uint32_t p) override

@@ -95,6 +95,7 @@ struct Ooc {
     uint32_t *d_planbuf = nullptr;  // cursor[P] | win_off[P] | plan chunks
     uint64_t plan_cap = 0;
     uint32_t *d_work = nullptr;
+    uint64_t *d_work_off = nullptr;
     uint64_t work_cap = 0;
     unsigned long long *d_stats = nullptr;
 
@@ -468,22 +469,52 @@ Lazy lazy_of(Ooc &o, const RunParams &rp, int32_t p, uint64_t begin, uint64_t co
     return z;
 }
 
+lt_status step_and_bucket_parts(Ooc &o, const RunParams &rp, const std::vector<uint32_t> &parts, int32_t p,
+                                const Lazy &lz, bool zero_copy, std::vector<std::pair<uint32_t, cudaEvent_t>> *deferred);
+
 lt_status step_and_bucket(Ooc &o, const RunParams &rp, int32_t p, const Lazy &lz, bool zero_copy,
                           std::vector<std::pair<uint32_t, cudaEvent_t>> *deferred)
+{
+    std::vector<uint32_t> parts;
+    if (p >= 0) parts.push_back((uint32_t)p);
+    return step_and_bucket_parts(o, rp, parts, p, lz, zero_copy, deferred);
+}
+
+// Drain the queues of `parts` (and create lz.count lazy walkers, belonging to
+// partition p when p >= 0) in one step-kernel launch.
+lt_status step_and_bucket_parts(Ooc &o, const RunParams &rp, const std::vector<uint32_t> &parts, int32_t p,
+                                const Lazy &lz, bool zero_copy, std::vector<std::pair<uint32_t, cudaEvent_t>> *deferred)
 {
     const uint64_t G = lz.count;
     lt_engine &e = *o.e;
     lt_graph &g = *o.g;
     Queue *qp = p >= 0 ? &o.q[p] : nullptr;
-    const uint64_t n_chunk_walkers = qp ? qp->dev_count() : 0;
+    uint64_t n_chunk_walkers = 0, nw = 0;
+    for (uint32_t x : parts) {
+        n_chunk_walkers += o.q[x].dev_count();
+        nw += o.q[x].dev_chunks.size();
+    }
     if (n_chunk_walkers + G == 0) return LT_OK;
     if (n_chunk_walkers + G > o.staging_cap) return fail(LT_ERR_CAPACITY, "staging area too small");
-    const uint64_t nw = qp ? qp->dev_chunks.size() : 0;
     if (nw > o.work_cap) return fail(LT_ERR_CAPACITY, "work list too small");
     uint32_t *h_work = (uint32_t *)o.h_work.ptr;
+    uint64_t *h_woff = (uint64_t *)(h_work + o.work_cap);
+    const bool multi = parts.size() > 1;
+    {
+        uint64_t k = 0, ord = 0;
+        for (uint32_t x : parts) {
+            const Queue &qx = o.q[x];
+            for (size_t c = 0; c < qx.dev_chunks.size(); c++, k++) {
+                h_work[k] = qx.dev_chunks[c];
+                h_woff[k] = ord;
+                ord += c + 1 == qx.dev_chunks.size() ? qx.tail_fill : kChunk;
+            }
+        }
+    }
     if (nw) {
-        std::memcpy(h_work, qp->dev_chunks.data(), 4 * nw);
         LT_CUDA_TRY(cudaMemcpyAsync(o.d_work, h_work, 4 * nw, cudaMemcpyHostToDevice, e.s_compute));
+        if (multi)
+            LT_CUDA_TRY(cudaMemcpyAsync(o.d_work_off, h_woff, 8 * nw, cudaMemcpyHostToDevice, e.s_compute));
     }
     LT_CUDA_TRY(cudaMemsetAsync(o.d_ctl, 0, 4 * o.ctl_words, e.s_compute));
 
@@ -492,6 +523,8 @@ lt_status step_and_bucket(Ooc &o, const RunParams &rp, int32_t p, const Lazy &lz
     a.arena = o.d_arena;
     a.work_chunks = o.d_work;
     a.n_chunk_walkers = n_chunk_walkers;
+    a.work_off = multi && nw ? o.d_work_off : nullptr;
+    a.n_work = (uint32_t)nw;
     a.lazy_begin = lz.begin;
     a.lazy_count = G;
     a.lazy_nb = lz.nb;
@@ -546,11 +579,15 @@ lt_status step_and_bucket(Ooc &o, const RunParams &rp, int32_t p, const Lazy &lz
     LT_CUDA_TRY(cudaMemcpyAsync(h_hist, o.d_ctl, 4ull * o.hist_words() + 8, cudaMemcpyDeviceToHost, e.s_compute));
     LT_CUDA_TRY(cudaStreamSynchronize(e.s_compute));
     const uint64_t staged = *(const unsigned long long *)(h_hist + o.hist_words());
-    // p's queue is drained: its chunks return to the pool.
+    // the drained queues' chunks return to the pool
+    for (uint32_t x : parts) {
+        Queue &qx = o.q[x];
+        for (uint32_t c : qx.dev_chunks) o.free_chunks.push_back(c);
+        qx.dev_chunks.clear();
+        qx.tail_fill = 0;
+        refresh(o, x);
+    }
     if (qp) {
-        for (uint32_t c : qp->dev_chunks) o.free_chunks.push_back(c);
-        qp->dev_chunks.clear();
-        qp->tail_fill = 0;
         qp->lazy_next += G;
         refresh(o, (uint32_t)p);
     }
@@ -640,12 +677,13 @@ lt_status ensure_pool(Ooc &o, uint64_t W)
     const uint64_t want = (B + kChunk - 1) / kChunk + 2ull * o.P + 2;
     if (want > 0xFFFFFFF0ull) return fail(LT_ERR_CAPACITY, "walker pool too large");
     if (o.d_arena && o.n_chunks == want) return LT_OK;
-    for (void *p : {(void *)o.d_arena, (void *)o.d_out, (void *)o.d_planbuf, (void *)o.d_work})
+    for (void *p : {(void *)o.d_arena, (void *)o.d_out, (void *)o.d_planbuf, (void *)o.d_work, (void *)o.d_work_off})
         if (p) cudaFree(p);
     host_free(o.h_plan);
     host_free(o.h_work);
     o.d_arena = nullptr;
     o.d_out = o.d_planbuf = o.d_work = nullptr;
+    o.d_work_off = nullptr;
     o.n_chunks = (uint32_t)want;
     o.staging_cap = (uint64_t)o.n_chunks * kChunk;
     o.plan_cap = o.n_chunks + (uint64_t)o.P;
@@ -654,8 +692,9 @@ lt_status ensure_pool(Ooc &o, uint64_t W)
     LT_TRY(dalloc(&o.d_out, 5 * o.staging_cap));
     LT_TRY(dalloc(&o.d_planbuf, 2ull * o.P + o.plan_cap));
     LT_TRY(dalloc(&o.d_work, o.work_cap));
+    LT_TRY(dalloc(&o.d_work_off, o.work_cap));
     LT_TRY(host_alloc(o.h_plan, 4 * (2ull * o.P + o.plan_cap), true));
-    LT_TRY(host_alloc(o.h_work, 4 * o.work_cap, true));
+    LT_TRY(host_alloc(o.h_work, 12 * o.work_cap, true));
     return LT_OK;
 }
 
@@ -731,7 +770,7 @@ lt_status update_cache(Ooc &o, std::vector<std::pair<uint32_t, cudaEvent_t>> &de
         if (slot < 0) {
             if (swaps >= o.policy->swap_budget() || next_in >= in_set.size()) break;
             const uint32_t w = in_set[next_in];
-            if (!(sc[c] > 1.25 * sc[w] + 1.0)) break;
+            if (!(sc[c] > o.policy->swap_ratio() * sc[w] + 1.0)) break;
             next_in++;
             swaps++;
             slot = o.slot_of[w];
@@ -845,7 +884,7 @@ void ooc_destroy(Ooc *o)
     drain_timers(*o, true);
     for (void *p : {(void *)o->d_slots, (void *)o->d_node_off, (void *)o->d_edge_off, (void *)o->d_rp, (void *)o->d_col,
                     (void *)o->d_arena, (void *)o->d_out, (void *)o->d_ctl, (void *)o->d_planbuf, (void *)o->d_work,
-                    (void *)o->d_stats})
+                    (void *)o->d_work_off, (void *)o->d_stats})
         if (p) cudaFree(p);
     for (HostBuf &b : o->host_slabs) host_free(b);
     host_free(o->h_ctl);
@@ -1294,7 +1333,15 @@ lt_status serve_open(lt_engine *e, uint32_t max_active, uint64_t table_slots, fl
     reset_queues(o);
     refresh_all(o);
     cudaMemsetAsync(o.d_stats, 0, 64, e->s_compute);
+    e->stats = lt_stats{};
     o.serve = s;
+    o.single = o.policy->serve_single_pass() && o.zc_rp_base != 0;
+    if (o.single)
+        for (uint32_t p = 0; p < o.P; p++)
+            if (o.slot_of[p] < 0) {
+                uncached_entry(o, p);
+                LT_TRY(set_entry(o, p, e->s_compute));
+            }
     *out = s;
     return LT_OK;
 }
@@ -1323,7 +1370,33 @@ lt_status serve_step(lt_server *s, uint32_t *completed, uint32_t *active, uint32
     LT_TRY(serve_admit(*s));
     uint32_t p = 0;
     SchedView v = view(o);
-    if (o.policy->next(v, o.prev_computed, false, p) || o.policy->next(v, o.prev_computed, true, p)) {
+    bool spilled = false;
+    for (uint32_t i = 0; i < o.P && !spilled; i++) spilled = !o.q[i].host_chunks.empty();
+    if (o.single && !spilled) {
+        // every partition readable: drain all in-flight walkers in one launch
+        std::vector<uint32_t> parts;
+        for (uint32_t i = 0; i < o.P; i++)
+            if (!o.q[i].dev_chunks.empty()) parts.push_back(i);
+        std::vector<std::pair<uint32_t, cudaEvent_t>> deferred;
+        o.iteration++;
+        e.stats.iterations++;
+        LT_TRY(update_cache(o, deferred));
+        RunParams rp{};
+        rp.app = kPPR;
+        rp.start = kStartSource;
+        rp.thr = s->thr;
+        if (!parts.empty()) {
+            Lazy none{};
+            none.mode = kStartSource;
+            LT_TRY(step_and_bucket_parts(o, rp, parts, -1, none, false, &deferred));
+        }
+        for (auto &d : deferred) {
+            LT_CUDA_TRY(cudaStreamWaitEvent(e.s_compute, d.second, 0));
+            LT_TRY(set_entry(o, d.first, e.s_compute));
+        }
+        drain_timers(o, false);
+        o.policy->observe(view(o));
+    } else if (o.policy->next(v, o.prev_computed, false, p) || o.policy->next(v, o.prev_computed, true, p)) {
         RunParams rp{};
         rp.app = kPPR;
         rp.start = kStartSource;
@@ -1374,7 +1447,25 @@ void serve_close(lt_server *s)
     if (!s) return;
     if (s->o && s->o->serve == s) {
         cudaStreamSynchronize(s->e->s_compute);
+        unsigned long long hs[8];
+        if (cudaMemcpy(hs, s->o->d_stats, sizeof hs, cudaMemcpyDeviceToHost) == cudaSuccess) {
+            s->e->stats.updates = hs[0];
+            s->e->stats.moves = hs[1];
+            s->e->stats.teleports = hs[2];
+            s->e->stats.zerocopy_bytes = hs[3] * 256;
+            s->e->stats.handoffs = hs[4];
+        }
+        drain_timers(*s->o, true);
         s->o->serve = nullptr;
+        if (s->o->single) {
+            s->o->single = false;
+            for (uint32_t p = 0; p < s->o->P; p++)
+                if (s->o->slot_of[p] < 0) {
+                    uncached_entry(*s->o, p);
+                    set_entry(*s->o, p, s->e->s_compute);
+                }
+            cudaStreamSynchronize(s->e->s_compute);
+        }
         reset_queues(*s->o);
         refresh_all(*s->o);
     }

@@ -62,8 +62,12 @@ public:
     // which partitions hold cache slots, by cache_score (higher = keep), and
     // swaps at most swap_budget partitions per batch.
     virtual bool single_pass() const { return false; }
+    // The same while serving queries (light, latency-bound load).
+    virtual bool serve_single_pass() const { return false; }
     virtual double cache_score(const SchedView &v, uint32_t p) { return 0.0; }
     virtual size_t swap_budget() const { return 0; }
+    // a cached partition is given up only for one scoring swap_ratio() times higher
+    virtual double swap_ratio() const { return 1.25; }
     // Cache emptied (the learned state of a policy survives).
     virtual void reset() {}
     virtual void stats(lt_policy_stats &s) const

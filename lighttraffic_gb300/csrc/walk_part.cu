@@ -22,6 +22,7 @@
 // destination with one global atomic (the two-level scheme of
 // src/WalkManager.h:122-190), into chunks the host allocated beforehand.
 #include "lt_core.cuh"
+#include "mem.cuh"
 #include "walk_part.h"
 
 namespace lt {
@@ -43,13 +44,14 @@ __device__ __forceinline__ uint32_t find_part(const uint32_t *off, uint32_t P, u
     return lo;
 }
 
-__device__ __forceinline__ uint64_t ld_u64(unsigned long long addr)
+// Row offsets stay in L2 (evict-last), column entries stream (evict-first).
+__device__ __forceinline__ uint64_t ld_u64(unsigned long long addr, uint64_t keep)
 {
-    return __ldg(reinterpret_cast<const unsigned long long *>(addr));
+    return ld_nc_u64(reinterpret_cast<const void *>(addr), keep);
 }
-__device__ __forceinline__ uint32_t ld_u32(unsigned long long addr)
+__device__ __forceinline__ uint32_t ld_u32(unsigned long long addr, uint64_t stream)
 {
-    return __ldg(reinterpret_cast<const unsigned int *>(addr));
+    return ld_nc_stream_u32(reinterpret_cast<const void *>(addr), stream);
 }
 
 // A PPR walk ends at v: count it (single run) or add it to the query's table
@@ -57,7 +59,7 @@ __device__ __forceinline__ uint32_t ld_u32(unsigned long long addr)
 __device__ __forceinline__ void ppr_count(const StepArgs &a, uint32_t qs, uint32_t v)
 {
     if (!a.q_seed) {
-        atomicAdd((unsigned long long *)&a.counts[v], 1ull);
+        red_add1_u64((unsigned long long *)&a.counts[v], l2_policy_evict_last());
         return;
     }
     const uint64_t base = a.q_toff[qs];
@@ -103,6 +105,7 @@ __global__ void __launch_bounds__(kPartBlock) walk_part_kernel(StepArgs a)
     const int lane = threadIdx.x & 31;
     const unsigned lt_mask = (1u << lane) - 1u;
     const uint64_t total = a.n_chunk_walkers + a.lazy_count;
+    const uint64_t keep = l2_policy_evict_last(), stream = l2_policy_evict_first();
 
     uint32_t cur = 0, step = 0, idx = 0, hop = 0, qs = 0;
     uint64_t seed = a.seed;
@@ -125,8 +128,23 @@ __global__ void __launch_bounds__(kPartBlock) walk_part_kernel(StepArgs a)
             if (!active) {
                 const uint64_t my = base + __popc(idle & lt_mask);
                 if (my < a.n_chunk_walkers) {
-                    const uint32_t k = a.work_chunks[my / kChunk];
-                    const uint32_t j = (uint32_t)(my % kChunk);
+                    uint32_t wi, j;
+                    if (!a.work_off) {
+                        wi = (uint32_t)(my / kChunk);
+                        j = (uint32_t)(my % kChunk);
+                    } else {
+                        uint32_t lo = 0, hi = a.n_work - 1;
+                        while (lo < hi) {
+                            const uint32_t mid = lo + (hi - lo + 1) / 2;
+                            if (my < a.work_off[mid])
+                                hi = mid - 1;
+                            else
+                                lo = mid;
+                        }
+                        wi = lo;
+                        j = (uint32_t)(my - a.work_off[lo]);
+                    }
+                    const uint32_t k = a.work_chunks[wi];
                     const uint32_t *c = reinterpret_cast<const uint32_t *>(a.arena + (uint64_t)k * kChunkBytes);
                     cur = c[j];
                     step = c[kChunk + j];
@@ -221,11 +239,11 @@ __global__ void __launch_bounds__(kPartBlock) walk_part_kernel(StepArgs a)
                 done = true;
             } else {
                 step = s - 1;
-                const uint64_t first = ld_u64(cp_rp + 8ull * (cur - cp_nb));
-                const uint64_t deg = ld_u64(cp_rp + 8ull * (cur - cp_nb + 1)) - first;
+                const uint64_t first = ld_u64(cp_rp + 8ull * (cur - cp_nb), keep);
+                const uint64_t deg = ld_u64(cp_rp + 8ull * (cur - cp_nb + 1), keep) - first;
                 if (deg > 0) {
                     const Rand4 q = walk_draw(seed, s, kTagStep, a.run, idx);
-                    cur = ld_u32(cp_col + 4ull * (first + mod_u64(r64_of(q), deg) - cp_eb));
+                    cur = ld_u32(cp_col + 4ull * (first + mod_u64(r64_of(q), deg) - cp_eb), stream);
                     n_mov++;
                     n_zc += cp_zc;
                 } else {
@@ -235,7 +253,7 @@ __global__ void __launch_bounds__(kPartBlock) walk_part_kernel(StepArgs a)
             }
         } else if (APP == kPageRank) {
             // app/pagerank.cu:26-44; a vertex without out-edges teleports.
-            atomicAdd((unsigned long long *)&a.counts[cur], 1ull);
+            red_add1_u64((unsigned long long *)&a.counts[cur], keep);
             if (s == 1) {
                 done = true;
             } else {
@@ -243,10 +261,10 @@ __global__ void __launch_bounds__(kPartBlock) walk_part_kernel(StepArgs a)
                 const uint64_t r64 = r64_of(r);
                 bool tele = !need_graph;
                 if (!tele) {
-                    const uint64_t first = ld_u64(cp_rp + 8ull * (cur - cp_nb));
-                    const uint64_t deg = ld_u64(cp_rp + 8ull * (cur - cp_nb + 1)) - first;
+                    const uint64_t first = ld_u64(cp_rp + 8ull * (cur - cp_nb), keep);
+                    const uint64_t deg = ld_u64(cp_rp + 8ull * (cur - cp_nb + 1), keep) - first;
                     if (deg > 0) {
-                        cur = ld_u32(cp_col + 4ull * (first + mod_u64(r64, deg) - cp_eb));
+                        cur = ld_u32(cp_col + 4ull * (first + mod_u64(r64, deg) - cp_eb), stream);
                         n_mov++;
                         n_zc += cp_zc;
                     } else {
@@ -260,12 +278,12 @@ __global__ void __launch_bounds__(kPartBlock) walk_part_kernel(StepArgs a)
             }
         } else {
             // app/genericwalk.cu:22-32
-            const uint64_t first = ld_u64(cp_rp + 8ull * (cur - cp_nb));
-            const uint64_t deg = ld_u64(cp_rp + 8ull * (cur - cp_nb + 1)) - first;
+            const uint64_t first = ld_u64(cp_rp + 8ull * (cur - cp_nb), keep);
+            const uint64_t deg = ld_u64(cp_rp + 8ull * (cur - cp_nb + 1), keep) - first;
             uint32_t *path = a.paths ? a.paths + (uint64_t)idx * (a.length + 1) : nullptr;
             if (deg > 0) {
                 const Rand4 q = walk_draw(seed, s, kTagStep, a.run, idx);
-                cur = ld_u32(cp_col + 4ull * (first + mod_u64(r64_of(q), deg) - cp_eb));
+                cur = ld_u32(cp_col + 4ull * (first + mod_u64(r64_of(q), deg) - cp_eb), stream);
                 n_mov++;
                 n_zc += cp_zc;
                 hop++;

@@ -36,8 +36,13 @@ struct PartTable {
 struct StepArgs {
     PartTable t;
     uint8_t *arena;                // chunk arena
-    const uint32_t *work_chunks;   // chunk ids of the partition being processed
-    uint64_t n_chunk_walkers;      // walkers in those chunks ((n-1) * kChunk + tail fill)
+    const uint32_t *work_chunks;   // chunk ids of the partitions being drained
+    uint64_t n_chunk_walkers;      // walkers in those chunks
+    // null: one partition's chunks, all full except the last; otherwise the
+    // first walker ordinal of each of the n_work chunks (chunks of several
+    // partitions, each partition's last one partly filled)
+    const uint64_t *work_off;
+    uint32_t n_work;
     uint64_t lazy_begin;           // first lazy ordinal to create
     uint64_t lazy_count;           // lazy walkers to create in this pass
     uint32_t lazy_nb, lazy_n;      // per-vertex starts: vertex range [lazy_nb, lazy_nb + lazy_n)

@@ -14,8 +14,10 @@
 //    (one atomic per warp refill), keeping every lane busy despite the
 //    geometric length spread of PPR walks.
 //  * Graph reads: rowptr[cur], rowptr[cur+1] (16 B) and col[e] (4 B) through
-//    the read-only path; counters are u64 atomics resolved in L2.
+//    the read-only path; counters are u64 reductions resolved in L2.  Column
+//    loads are evict-first, row offsets and counters evict-last (mem.cuh).
 #include "lt_core.cuh"
+#include "mem.cuh"
 #include "walk_whole.h"
 
 namespace lt {
@@ -24,14 +26,19 @@ namespace {
 
 constexpr unsigned kFull = 0xFFFFFFFFu;
 
-__device__ __forceinline__ uint64_t ldg_u64(const uint64_t *p) { return __ldg((const unsigned long long *)p); }
-__device__ __forceinline__ uint32_t ldg_u32(const uint32_t *p) { return __ldg(p); }
+struct Hints {
+    uint64_t keep, stream;
+};
+__device__ __forceinline__ uint64_t ldg_u64(const uint64_t *p, const Hints &h) { return ld_nc_u64(p, h.keep); }
+__device__ __forceinline__ uint32_t ldg_u32(const uint32_t *p, const Hints &h) { return ld_nc_stream_u32(p, h.stream); }
+__device__ __forceinline__ void count1(uint64_t *c, const Hints &h) { red_add1_u64((unsigned long long *)c, h.keep); }
 
 template <int APP, int START>
 __global__ void __launch_bounds__(kWholeBlock) walk_whole_kernel(WholeArgs a)
 {
     const int lane = threadIdx.x & 31;
     const unsigned lt_mask = (1u << lane) - 1u;
+    const Hints h{l2_policy_evict_last(), l2_policy_evict_first()};
 
     uint32_t cur = 0, step = 0;
     uint64_t idx = 0;
@@ -75,24 +82,24 @@ __global__ void __launch_bounds__(kWholeBlock) walk_whole_kernel(WholeArgs a)
         if (APP == kPPR) {
             // app/ppr.cu:22-42
             if (s == 1) {
-                atomicAdd((unsigned long long *)&a.counts[cur], 1ull);
+                count1(&a.counts[cur], h);
                 active = false;
             } else {
                 step = s - 1;
-                const uint64_t first = ldg_u64(a.rowptr + cur);
-                const uint64_t deg = ldg_u64(a.rowptr + cur + 1) - first;
+                const uint64_t first = ldg_u64(a.rowptr + cur, h);
+                const uint64_t deg = ldg_u64(a.rowptr + cur + 1, h) - first;
                 if (deg > 0) {
                     const Rand4 r = walk_draw(a.seed, s, kTagStep, a.run, idx);
-                    cur = ldg_u32(a.col + first + mod_u64(r64_of(r), deg));
+                    cur = ldg_u32(a.col + first + mod_u64(r64_of(r), deg), h);
                     n_mov++;
                 } else {
-                    atomicAdd((unsigned long long *)&a.counts[cur], 1ull);
+                    count1(&a.counts[cur], h);
                     active = false;
                 }
             }
         } else if (APP == kPageRank) {
             // app/pagerank.cu:26-44; a vertex without out-edges teleports.
-            atomicAdd((unsigned long long *)&a.counts[cur], 1ull);
+            count1(&a.counts[cur], h);
             if (s == 1) {
                 active = false;
             } else {
@@ -101,10 +108,10 @@ __global__ void __launch_bounds__(kWholeBlock) walk_whole_kernel(WholeArgs a)
                 const uint64_t r64 = r64_of(r);
                 bool tele = m53_of(r) >= a.thr;
                 if (!tele) {
-                    const uint64_t first = ldg_u64(a.rowptr + cur);
-                    const uint64_t deg = ldg_u64(a.rowptr + cur + 1) - first;
+                    const uint64_t first = ldg_u64(a.rowptr + cur, h);
+                    const uint64_t deg = ldg_u64(a.rowptr + cur + 1, h) - first;
                     if (deg > 0) {
-                        cur = ldg_u32(a.col + first + mod_u64(r64, deg));
+                        cur = ldg_u32(a.col + first + mod_u64(r64, deg), h);
                         n_mov++;
                     } else {
                         tele = true;
@@ -117,12 +124,12 @@ __global__ void __launch_bounds__(kWholeBlock) walk_whole_kernel(WholeArgs a)
             }
         } else {
             // app/genericwalk.cu:22-32
-            const uint64_t first = ldg_u64(a.rowptr + cur);
-            const uint64_t deg = ldg_u64(a.rowptr + cur + 1) - first;
+            const uint64_t first = ldg_u64(a.rowptr + cur, h);
+            const uint64_t deg = ldg_u64(a.rowptr + cur + 1, h) - first;
             uint32_t *path = a.paths ? a.paths + idx * (uint64_t)(a.length + 1) : nullptr;
             if (deg > 0) {
                 const Rand4 r = walk_draw(a.seed, s, kTagStep, a.run, idx);
-                cur = ldg_u32(a.col + first + mod_u64(r64_of(r), deg));
+                cur = ldg_u32(a.col + first + mod_u64(r64_of(r), deg), h);
                 n_mov++;
                 hop++;
                 if (path) path[hop] = cur;
