@@ -289,48 +289,56 @@ def link_bytes(s):
 
 
 def gb300_ooc(args, cfg):
-    import torch
-    ws, rank, local, dist = init_dist()
+    ws, rank, local = dist_env()
+    dist = None
+    if ws > 1:
+        # torch only for the barrier and the max over ranks of a replica run
+        ws, rank, local, dist = init_dist()
     import lighttraffic_gb300 as lt
 
     g = lt.Graph.rmat(cfg["scale"], cfg["edges"], seed=SEED_GRAPH, part_bytes=cfg["part_mb"] << 20, device=local)
     V, E = g.num_nodes, g.num_edges
     W = 2 * V
-    link_peak = host_link_peak(local)
-    counts = torch.empty(V, dtype=torch.int64, pin_memory=True).numpy().view(np.uint64)
+    link_peak = lt.host_link_gbs(local)
+    counts = np.zeros(V, dtype=np.uint64)
     clocks = ClockSampler(local)
     clocks.start()
     time.sleep(0.3)
-    wall0 = time.time()
-    # both engines live side by side and their runs alternate, so drift on
-    # the box (or order effects) hits both schedulers alike
-    engines = {name: lt.Engine(g, partitions=cfg["partitions"], batch=cfg["batch"], seed=SEED_WALK, sched=sched,
-                               device=local)
-               for name, sched in [("learned", lt.SCHED_LEARNED), ("plain", lt.SCHED_PLAIN)]}
+    scheds = {"learned": lt.SCHED_LEARNED, "plain": lt.SCHED_PLAIN}
+
+    def one_run(name):
+        # a fresh engine per run (created and destroyed outside the timed
+        # region): engines left alive in the process slow each other down
+        e = lt.Engine(g, partitions=cfg["partitions"], batch=cfg["batch"], seed=SEED_WALK, sched=scheds[name],
+                      device=local)
+        e.drop_cache()
+        t0 = time.perf_counter()
+        e.ppr(0, W, cfg["prob"], out=counts)
+        t1 = time.perf_counter()
+        assert int(counts.sum()) == W, "PPR invariant (one count per walk) violated"
+        res = (t1 - t0, e.stats(), e.policy_stats())
+        e.close()
+        return res
+
     for _ in range(args.warmup):
-        for e in engines.values():
-            e.drop_cache()
-            e.ppr(0, W, cfg["prob"], out=counts)
+        for name in scheds:
+            one_run(name)
     if dist:
         dist.barrier()
-    times = {name: [] for name in engines}
-    stats = {}
-    for _ in range(args.steps):
-        for name, e in engines.items():
-            e.drop_cache()
-            torch.cuda.synchronize()
-            t0 = time.perf_counter()
-            e.ppr(0, W, cfg["prob"], out=counts)
-            t1 = time.perf_counter()
-            assert int(counts.sum()) == W, "PPR invariant (one count per walk) violated"
-            times[name].append(t1 - t0)
-            stats[name] = e.stats()
+    wall0 = time.time()
+    times = {name: [] for name in scheds}
+    stats, pstats = {}, {}
+    order = list(scheds)
+    for k in range(args.steps):
+        for name in (order if k % 2 == 0 else order[::-1]):
+            dt, st, ps = one_run(name)
+            times[name].append(dt)
+            stats[name], pstats[name] = st, ps
     results = {}
-    for name, e in engines.items():
+    for name in scheds:
         s = stats[name]
         results[name] = {"elapsed": max_over_ranks(dist, local, sum(times[name])), "stats": s,
-                         "policy": e.policy_stats(), "steps": s["moves"], "times": times[name]}
-        e.close()
+                         "policy": pstats[name], "steps": s["moves"], "times": times[name]}
     clocks.stop()
     clk = clocks.summary(wall0 - 0.5, time.time())
     if rank != 0:
@@ -627,7 +635,9 @@ def serve_trace(cfg, V, rate, seconds, seed):
 
 
 def gb300_serve(args, cfg):
-    ws, rank, local, dist = init_dist()
+    ws, rank, local = dist_env()
+    if ws > 1:
+        ws, rank, local, _ = init_dist()
     import lighttraffic_gb300 as lt
 
     g = lt.Graph.rmat(cfg["scale"], cfg["edges"], seed=SEED_GRAPH, part_bytes=cfg["part_mb"] << 20, device=local)

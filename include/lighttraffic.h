@@ -308,6 +308,11 @@ lt_status lt_engine_policy_stats(const lt_engine *e, lt_policy_stats *out);
 lt_status lt_mlp_check(int device, uint32_t n, const float *x, const float *y, const float *params, float lr,
                        float momentum, float *pred_out, float *grad_out, float *loss_out, float *params_out);
 
+/* Pinned host -> device copy bandwidth of `device` in GB/s (best of five
+ * 1 GiB copies): the host-link roofline of out-of-core runs.  No counterpart
+ * in the reference. */
+lt_status lt_host_link_gbs(int device, double *gbs);
+
 /* The remainder x[i] % d[i] as the walk kernels compute it (host build of the
  * same code), for checking it against native division.  No counterpart in
  * the reference. */

@@ -1,4 +1,5 @@
 // capi.cpp -- extern "C" entry points declared in include/lighttraffic.h.
+#include <algorithm>
 #include <cstring>
 #include <new>
 
@@ -247,6 +248,38 @@ lt_status lt_engine_policy_stats(const lt_engine *e, lt_policy_stats *out)
 }
 
 size_t lt_walk_scratch_bytes(void) { return walk_scratch_bytes(); }
+
+lt_status lt_host_link_gbs(int device, double *gbs)
+{
+    if (!gbs) return fail(LT_ERR_INVALID, "null argument");
+    LT_CUDA_TRY(cudaSetDevice(device));
+    const size_t n = size_t(1) << 30;
+    void *h = nullptr, *d = nullptr;
+    LT_CUDA_TRY(cudaHostAlloc(&h, n, cudaHostAllocDefault));
+    if (cudaMalloc(&d, n) != cudaSuccess) {
+        cudaFreeHost(h);
+        return fail(LT_ERR_NOMEM, "cudaMalloc of 1 GiB failed");
+    }
+    cudaEvent_t a, b;
+    cudaEventCreate(&a);
+    cudaEventCreate(&b);
+    double best = 0;
+    for (int i = 0; i < 5; i++) {
+        cudaEventRecord(a, 0);
+        cudaMemcpyAsync(d, h, n, cudaMemcpyHostToDevice, 0);
+        cudaEventRecord(b, 0);
+        cudaEventSynchronize(b);
+        float ms = 0;
+        cudaEventElapsedTime(&ms, a, b);
+        if (ms > 0) best = std::max(best, (double)n / (ms / 1e3) / 1e9);
+    }
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    cudaFree(d);
+    cudaFreeHost(h);
+    *gbs = best;
+    return cudaGetLastError() == cudaSuccess ? LT_OK : fail(LT_ERR_CUDA, "bandwidth probe failed");
+}
 
 lt_status lt_mod_check(uint64_t n, const uint64_t *x, const uint64_t *d, uint64_t *out)
 {

@@ -12,6 +12,12 @@ compared against; only ``tests/``, ``__graft_entry__.smoke()`` and the
     - ``.part``: ``u16 P | u64 partitionSizeBytes | u32 nodeOffset[P+1] |
       u64 edgeOffset[P+1]``, no padding (src/partition/PartitionStrategy.h:
       76-97 reads it, :325-337 writes it).
+
+Pinning: the partitioner and ``.part`` bytes are pinned to the reference's
+own ``EqualSizeStrategy`` (compiled from its sources into ``_ref/``); Philox
+to the Random123 known-answer vectors.  Walk outputs: parity unpinned against
+reference outputs (the reference's cuRAND seed is uninitialised,
+src/Rand.h:29-30); pinned to its sum invariants and hand-checked graphs.
 """
 from __future__ import annotations
 

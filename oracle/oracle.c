@@ -42,6 +42,15 @@
  *   PPR length trials: init draw t gives two trials, m53 of (x0,x1) first,
  *   then m53 of (x2,x3).
  *
+ * Pinning.  Walk semantics: parity unpinned against reference outputs (the
+ * reference cannot produce reproducible ones, see above).  The walk functions
+ * are pinned to the reference's own invariants instead: PPR counts sum to the
+ * number of walkers (app/ppr.cu:77-85), PageRank counts to walkers x length x
+ * runs (app/pagerank.cu:202-210), and hand-checkable graphs where every
+ * endpoint is known.  Philox is pinned to the Random123 known-answer
+ * vectors.  The partitioner (orc_partition) is pinned byte for byte to the
+ * reference's EqualSizeStrategy compiled from its own sources.
+ *
  * The RMAT generator (a seeded stand-in for the reference's datasets, which
  * are absent) is restated here as well so the GPU generator can be checked
  * bit-exact:
