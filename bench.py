@@ -1,7 +1,7 @@
 #!/usr/bin/env python3
 """Benchmark of the random-walk hot path on GB300.
 
-    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference] [--config c2|c1|c0]
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference] [--config c2|c2s|c1|c0|c3|c4]
 
 Workloads (synthetic RMAT graphs, a=.57 b=.19 c=.19 d=.05, seed 1, isolated
 vertices removed, stand in for the reference's datasets, which are absent):
@@ -9,10 +9,14 @@ vertices removed, stand in for the reference's datasets, which are absent):
       partitions in pinned host memory, 256 cached on the device (-p 256,
       8 GiB), walker pool 2^28 (-b), W = 2|V| walks from source 0, stop
       probability 0.15.  One step = one full run from a cold device cache,
-      through the public API (lt_run_ppr with a pinned host count buffer):
-      every partition load, zero-copy read and walker spill is inside the
-      timed region.  `value` is the learned scheduler; the plain (reference)
-      scheduler is timed beside it under "plain".
+      through the public API (lt_run_ppr with a host count buffer): every
+      partition load, zero-copy read and walker spill is inside the timed
+      region.  `value` is the learned scheduler (wave runs, cache slots by
+      predicted visits); the plain (reference) scheduler is timed beside it
+      under "plain", and wave runs with least-recently-used slots (batched)
+      or moving-average scores (frequency) under "ablations".
+  c2s: the c2 setup scaled down for profiler captures -- RMAT(2^24, 2^28),
+      16 of its 32 MiB partitions cached, walker pool 2^22.
   c1: walk-based PageRank on RMAT(2^23, 2^27) resident in HBM (32 MiB
       partitions all cached), 2|V| walkers one per vertex, l = 10, teleport
       when U > 0.85; `value` times lt_walk_device passes on device buffers,
@@ -56,6 +60,8 @@ sys.path.insert(0, ROOT)
 CONFIGS = {
     "c2": dict(workload="ppr-rmat30-e33-outofcore-p256-b2^28", app=0, scale=30, edges=1 << 33, length=0,
                start=0, prob=0.15, part_mb=32, partitions=256, batch=1 << 28),
+    "c2s": dict(workload="ppr-rmat24-e28-outofcore-p16-b2^22", app=0, scale=24, edges=1 << 28, length=0,
+                start=0, prob=0.15, part_mb=32, partitions=16, batch=1 << 22),
     "c1": dict(workload="pagerank-rmat23-e27-resident", app=1, scale=23, edges=1 << 27, length=10,
                start=2, prob=0.85, part_mb=32),
     "c0": dict(workload="ppr-rmat20-e24-resident", app=0, scale=20, edges=1 << 24, length=0,
@@ -304,7 +310,10 @@ def gb300_ooc(args, cfg):
     clocks = ClockSampler(local)
     clocks.start()
     time.sleep(0.3)
-    scheds = {"learned": lt.SCHED_LEARNED, "plain": lt.SCHED_PLAIN}
+    # learned = the headline; plain = the reference policy; batched and
+    # frequency = wave runs without predictions / with a moving average
+    scheds = {"learned": lt.SCHED_LEARNED, "plain": lt.SCHED_PLAIN, "batched": lt.SCHED_BATCHED,
+              "frequency": lt.SCHED_FREQUENCY}
 
     def one_run(name):
         # a fresh engine per run (created and destroyed outside the timed
@@ -383,6 +392,12 @@ def gb300_ooc(args, cfg):
                     "partition_loads": s["partition_loads"], "policy": L["policy"], "step_s": L["times"]},
         "learned_over_plain": {"steps_per_s": value / plain_value,
                                "bytes_per_step": (link_bytes(s) / s["moves"]) / (link_bytes(Pn["stats"]) / Pn["steps"])},
+        "ablations": {name: {"value": results[name]["steps"] * args.steps * ws / results[name]["elapsed"],
+                             "bytes_per_step": link_bytes(results[name]["stats"]) / results[name]["steps"],
+                             "iterations": results[name]["stats"]["iterations"],
+                             "partition_loads": results[name]["stats"]["partition_loads"],
+                             "step_s": results[name]["times"]}
+                      for name in ("batched", "frequency")},
         "e2e": {"value": value, "unit": "steps/s", "h2d_bytes_per_step": s["h2d_graph_bytes"] + s["h2d_walker_bytes"],
                 "d2h_bytes_per_step": 8 * V + s["d2h_walker_bytes"],
                 "note": "each step is a full run through lt_run_ppr from a cold cache with host output buffers"},

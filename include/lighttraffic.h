@@ -53,11 +53,21 @@ typedef enum lt_app { LT_APP_PPR = 0, LT_APP_PAGERANK = 1, LT_APP_WALK = 2 } lt_
  * PER_VERTEX: walker i starts at vertex i mod V. */
 typedef enum lt_start { LT_START_SOURCE = 0, LT_START_UNIFORM = 1, LT_START_PER_VERTEX = 2 } lt_start;
 
-/* PLAIN: the reference policy (src/Scheduler.h:84-171, :243-252, :368-388);
- * FIFO: its FIFO_SCHE variant (:113-127, :391-418); LEARNED: partitions scored
- * by the visits the online-trained prefetcher network predicts; FREQUENCY: the
- * same decisions scored by a moving average of visits (ablation). */
-typedef enum lt_sched { LT_SCHED_PLAIN = 0, LT_SCHED_FIFO = 1, LT_SCHED_LEARNED = 2, LT_SCHED_FREQUENCY = 3 } lt_sched;
+/* PLAIN: the reference policy, one partition per iteration
+ * (src/Scheduler.h:84-171, :243-252, :368-388); FIFO: its FIFO_SCHE variant
+ * (:113-127, :391-418).  The others run in waves: every step kernel drains
+ * every cached partition's queue while the next loads stream in.  LEARNED:
+ * cache slots go to the partitions the online-trained prefetcher network
+ * predicts the most visits for; FREQUENCY: the same, scored by a moving
+ * average of visits (ablation of the network); BATCHED: least recently used
+ * slots (ablation of the predictions).  All give identical results. */
+typedef enum lt_sched {
+    LT_SCHED_PLAIN = 0,
+    LT_SCHED_FIFO = 1,
+    LT_SCHED_LEARNED = 2,
+    LT_SCHED_FREQUENCY = 3,
+    LT_SCHED_BATCHED = 4
+} lt_sched;
 
 typedef struct lt_graph lt_graph;
 typedef struct lt_engine lt_engine;

@@ -25,7 +25,7 @@ BIN_DIR = os.path.join(PKG, "bin")
 
 APP_PPR, APP_PAGERANK, APP_WALK = 0, 1, 2
 START_SOURCE, START_UNIFORM, START_PER_VERTEX = 0, 1, 2
-SCHED_PLAIN, SCHED_FIFO, SCHED_LEARNED, SCHED_FREQUENCY = 0, 1, 2, 3
+SCHED_PLAIN, SCHED_FIFO, SCHED_LEARNED, SCHED_FREQUENCY, SCHED_BATCHED = 0, 1, 2, 3, 4
 INVALID_NODE = 0xFFFFFFFF
 
 STATUS = {0: "LT_OK", 1: "LT_ERR_INVALID", 2: "LT_ERR_IO", 3: "LT_ERR_FORMAT", 4: "LT_ERR_NOMEM",

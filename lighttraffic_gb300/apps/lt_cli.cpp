@@ -6,7 +6,7 @@
 //   -s/--partition-size MB  -l/--length L  --runs R  --trimmed T  --source v
 //   --prob p  -m/--materialized-partition
 // plus: --seed S, --start uniform|pervertex, --alpha a (PageRank teleport
-// test, default 0.85 as app/pagerank.cu:6), --sched plain|fifo|learned,
+// test, default 0.85 as app/pagerank.cu:6), --sched plain|fifo|learned|frequency|batched,
 // --no-pipeline, --zerocopy-threshold N, --counts-out FILE (u64[V] raw),
 // --endpoints-out FILE / --paths-out FILE (genericwalk, u32 raw).
 // Prints the reference's stdout lines (src/Config.h:92, src/LightTraffic.h:26,
@@ -46,7 +46,7 @@ struct Opts {
     if (msg) fprintf(stderr, "%s\n", msg);
     fprintf(stderr,
             "usage: %s -f G.bcsr [-m] [-s MB] [-p P] [-b B] [-w W] [-l L] [--runs R] [--source v] [--prob p]\n"
-            "          [--seed S] [--start uniform|pervertex] [--alpha a] [--sched plain|fifo|learned]\n"
+            "          [--seed S] [--start uniform|pervertex] [--alpha a] [--sched plain|fifo|learned|frequency|batched]\n"
             "          [--no-pipeline] [--zerocopy-threshold N] [--counts-out F] [--endpoints-out F] [--paths-out F]\n",
             argv0);
     exit(2);
@@ -106,7 +106,9 @@ Opts parse(int argc, char **argv)
             if (s == "plain") o.sched = LT_SCHED_PLAIN;
             else if (s == "fifo") o.sched = LT_SCHED_FIFO;
             else if (s == "learned") o.sched = LT_SCHED_LEARNED;
-            else usage(argv[0], "--sched takes plain, fifo or learned");
+            else if (s == "frequency") o.sched = LT_SCHED_FREQUENCY;
+            else if (s == "batched") o.sched = LT_SCHED_BATCHED;
+            else usage(argv[0], "--sched takes plain, fifo, learned, frequency or batched");
         } else if (a == "--no-pipeline") o.pipeline = 0;
         else if (a == "--zerocopy-threshold") o.zc = strtoull(next().c_str(), nullptr, 0);
         else if (a == "--counts-out") o.counts_out = next();

@@ -1,9 +1,9 @@
 // mlp.cu -- kernels and host logic of the learned prefetcher.
 //
 // No counterpart in the reference, whose scheduler (src/Scheduler.h:84-171,
-// :368-388) ranks partitions by the walkers waiting now; this policy ranks
-// them by the arrivals a small network predicts from the engine's own traces,
-// and loads the predicted partitions ahead of need.
+// :368-388) ranks partitions by the walkers waiting now; this policy runs the
+// engine in waves and gives cache slots to the partitions a small network,
+// trained online on the engine's own traces, predicts the most visits for.
 //
 // Kernels (FP32, deterministic reduction order):
 //   mlp_forward  : one warp per row; lane j owns hidden units j and j+32,
@@ -12,7 +12,10 @@
 //                  accumulate dL/dW1[:, j], dL/db1[j], dL/dW2[j] (and dL/db2,
 //                  the loss in CTA 0), then a fixed-order tree reduction;
 //                  L = mean (y - t)^2;
-//   mlp_sgd      : v = mu v + g, w -= lr v.
+//   mlp_sgd      : v = mu v + g, w -= lr v;
+//   pol_iter / pol_features / pol_labels / pol_demand: the policy's visit
+//                  ring and moving average, feature rows, residual targets
+//                  with the moving-average baseline loss, and forecasts.
 #include "mlp.h"
 
 #include <algorithm>
@@ -180,11 +183,51 @@ lt_status Mlp::get_params(float *h)
     return LT_OK;
 }
 
+namespace {
+
+__global__ void copy_f32(float *__restrict__ dst, const float *__restrict__ src, uint64_t n)
+{
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) dst[i] = src[i];
+}
+
+// Device view of pinned, mapped host memory; null for other memory.
+const float *mapped_view(const void *h)
+{
+    cudaPointerAttributes at{};
+    if (cudaPointerGetAttributes(&at, h) != cudaSuccess || at.type != cudaMemoryTypeHost || !at.devicePointer) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return (const float *)at.devicePointer;
+}
+
+}  // namespace
+
+// Host <-> device transfers of the network's rows.  Pinned, mapped buffers
+// move by a copy kernel: copies on the copy engine would queue behind the
+// partition loads of the engine that trains the network.
+lt_status Mlp::move(float *dst, const float *src, uint64_t n, cudaMemcpyKind kind)
+{
+    const float *view = mapped_view(kind == cudaMemcpyHostToDevice ? (const void *)src : (const void *)dst);
+    if (!view) {
+        LT_CUDA_TRY(cudaMemcpyAsync(dst, src, 4ull * n, kind, st_));
+        return LT_OK;
+    }
+    const unsigned blocks = (unsigned)std::min<uint64_t>((n + 255) / 256, 152);
+    if (kind == cudaMemcpyHostToDevice)
+        copy_f32<<<blocks, 256, 0, st_>>>(dst, view, n);
+    else
+        copy_f32<<<blocks, 256, 0, st_>>>(const_cast<float *>(view), src, n);
+    LT_CUDA_TRY(cudaGetLastError());
+    return LT_OK;
+}
+
 lt_status Mlp::upload(const float *h_x, const float *h_y, uint32_t n)
 {
     if (n > cap_) return fail(LT_ERR_CAPACITY, "MLP batch of %u rows exceeds %u", n, cap_);
-    LT_CUDA_TRY(cudaMemcpyAsync(d_x_, h_x, 4ull * n * F, cudaMemcpyHostToDevice, st_));
-    if (h_y) LT_CUDA_TRY(cudaMemcpyAsync(d_y_, h_y, 4ull * n, cudaMemcpyHostToDevice, st_));
+    LT_TRY(move(d_x_, h_x, (uint64_t)n * F, cudaMemcpyHostToDevice));
+    if (h_y) LT_TRY(move(d_y_, h_y, n, cudaMemcpyHostToDevice));
     return LT_OK;
 }
 
@@ -217,25 +260,21 @@ lt_status Mlp::train(const float *h_x, const float *h_y, uint32_t n, float lr, f
     return LT_OK;
 }
 
-lt_status Mlp::train_async(const float *h_x, const float *h_y, uint32_t n, float lr, float momentum, float *h_loss)
+lt_status Mlp::train_dev(const float *d_x, const float *d_y, uint32_t n, float lr, float momentum, float *d_loss)
 {
-    LT_CUDA_TRY(cudaSetDevice(device_));
-    LT_TRY(upload(h_x, h_y, n));
-    mlp_forward<<<(n * 32 + 255) / 256, 256, 0, st_>>>(d_x_, n, d_params_, d_h_, d_pred_);
-    mlp_backward<<<H, kBwdThreads, 0, st_>>>(d_x_, d_y_, n, d_params_, d_h_, d_pred_, d_grad_, d_loss_);
+    if (n > cap_) return fail(LT_ERR_CAPACITY, "MLP batch of %u rows exceeds %u", n, cap_);
+    mlp_forward<<<(n * 32 + 255) / 256, 256, 0, st_>>>(d_x, n, d_params_, d_h_, d_pred_);
+    mlp_backward<<<H, kBwdThreads, 0, st_>>>(d_x, d_y, n, d_params_, d_h_, d_pred_, d_grad_, d_loss);
     mlp_sgd<<<(kMlpParams + 255) / 256, 256, 0, st_>>>(d_params_, d_grad_, d_mom_, lr, momentum);
     LT_CUDA_TRY(cudaGetLastError());
-    if (h_loss) LT_CUDA_TRY(cudaMemcpyAsync(h_loss, d_loss_, 4, cudaMemcpyDeviceToHost, st_));
     return LT_OK;
 }
 
-lt_status Mlp::forward_async(const float *h_x, uint32_t n, float *h_pred)
+lt_status Mlp::forward_dev(const float *d_x, uint32_t n, float *d_pred)
 {
-    LT_CUDA_TRY(cudaSetDevice(device_));
-    LT_TRY(upload(h_x, nullptr, n));
-    mlp_forward<<<(n * 32 + 255) / 256, 256, 0, st_>>>(d_x_, n, d_params_, nullptr, d_pred_);
+    if (n > cap_) return fail(LT_ERR_CAPACITY, "MLP batch of %u rows exceeds %u", n, cap_);
+    mlp_forward<<<(n * 32 + 255) / 256, 256, 0, st_>>>(d_x, n, d_params_, nullptr, d_pred);
     LT_CUDA_TRY(cudaGetLastError());
-    LT_CUDA_TRY(cudaMemcpyAsync(h_pred, d_pred_, 4ull * n, cudaMemcpyDeviceToHost, st_));
     return LT_OK;
 }
 
@@ -250,55 +289,151 @@ lt_status Mlp::record(cudaEvent_t ev)
 namespace {
 
 constexpr int kHist = 8;
-constexpr int kEvery = 8;  // features, training and prediction every kEvery iterations
+constexpr int kEvery = 2;  // features, training and prediction every kEvery iterations
 constexpr float kLearningRate = 0.02f;
 constexpr float kMomentum = 0.9f;
+constexpr float kEmaKeep = 0.95f;
 constexpr int kRing = kHist + kLabelHorizon + 1;    // visit history ring (iterations)
 constexpr int kSnaps = kLabelHorizon / kEvery + 2;  // feature snapshots awaiting labels
+constexpr int kStage = 4;                           // host staging slots (iterations in flight)
 
-// Scores are predicted visits (walkers entering the partition, cached or not)
-// over the next kLabelHorizon iterations plus the walkers already waiting.
-// Cache decisions only trade a cached partition for one predicted clearly
-// busier (twice the score plus the zero-copy threshold), so noise in the
-// predictions does not turn into load / evict churn.
+// ---- device side of the policy: features, labels and forecasts.  The host
+// stages per iteration the visits of every partition (u32) and, every kEvery
+// iterations, its waiting walkers, residency and iterations since last use
+// (f32); everything else lives on the device.
+
+// ring[slot] = visits; ema = kEmaKeep ema + (1 - kEmaKeep) visits.
+__global__ void pol_iter(uint32_t *ring, float *ema, const uint32_t *visits, uint32_t P, uint32_t slot)
+{
+    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < P; p += gridDim.x * blockDim.x) {
+        const uint32_t v = visits[p];
+        ring[(uint64_t)slot * P + p] = v;
+        ema[p] = kEmaKeep * ema[p] + (1.0f - kEmaKeep) * (float)v;
+    }
+}
+
+// Feature rows of iteration t (layout in mlp.h).  dyn = waiting | resident | gap.
+__global__ void pol_features(float *X, const uint32_t *ring, const float *ema, const float *stat, const float *dyn,
+                             uint32_t P, uint64_t t)
+{
+    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < P; p += gridDim.x * blockDim.x) {
+        float *x = X + (uint64_t)p * kMlpIn;
+        x[0] = log1pf(dyn[p]) / 16.0f;
+        for (int k = 0; k < kHist; k++)
+            x[1 + k] = (uint64_t)k < t ? log1pf((float)ring[(uint64_t)((t - k) % kRing) * P + p]) / 16.0f : 0.0f;
+        x[9] = stat[p];
+        x[10] = stat[P + p];
+        x[11] = dyn[P + p];
+        x[12] = log1pf(dyn[2 * P + p]) / 16.0f;
+        x[13] = log1pf(ema[p]) / 16.0f;
+        x[14] = (float)p / (float)P;
+        x[15] = log1pf(ema[p] * (float)kLabelHorizon) / 16.0f;  // moving-average forecast
+    }
+}
+
+// Targets for the snapshot taken kLabelHorizon iterations before t: the
+// visits since then, as a correction to the snapshot's moving-average
+// forecast; base = the mean squared error of that forecast alone (one CTA,
+// fixed reduction order).
+__global__ void __launch_bounds__(256) pol_labels(float *Y, float *base, const float *Xold, const uint32_t *ring,
+                                                  uint32_t P, uint64_t t)
+{
+    __shared__ float sh[256];
+    float acc = 0.f;
+    for (uint32_t p = threadIdx.x; p < P; p += 256) {
+        float sum = 0.f;
+        for (int k = 0; k < kLabelHorizon; k++) sum += (float)ring[(uint64_t)((t - k) % kRing) * P + p];
+        const float y = log1pf(sum) / 16.0f - Xold[(uint64_t)p * kMlpIn + 15];
+        Y[p] = y;
+        acc = fmaf(y, y, acc);
+    }
+    sh[threadIdx.x] = acc;
+    __syncthreads();
+    for (int s = 128; s > 0; s >>= 1) {
+        if ((int)threadIdx.x < s) sh[threadIdx.x] += sh[threadIdx.x + s];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *base = sh[0] / (float)P;
+}
+
+// demand = predicted visits over the label horizon.
+__global__ void pol_demand(float *demand, const float *pred, const float *X, uint32_t P)
+{
+    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < P; p += gridDim.x * blockDim.x)
+        demand[p] = expm1f(fmaxf(0.f, X[(uint64_t)p * kMlpIn + 15] + pred[p]) * 16.0f);
+}
+
+__global__ void pol_copy(float *dst, const float *src, uint32_t n)
+{
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) dst[i] = src[i];
+}
+
+// Eviction scores are predicted visits (walkers entering the partition,
+// cached or not) over the next kLabelHorizon iterations plus the walkers
+// already waiting.  The network runs on its own stream; the host stages a few
+// kilobytes per iteration and picks up the forecasts of the previous round
+// when they are ready, never waiting for them.
 class LearnedPolicy : public Policy {
 public:
     // use_net = false: the same decisions from a moving average of visits
-    // instead of the network (the ablation baseline).
+    // instead of the network (the ablation baseline), kept on the host.
     LearnedPolicy(const lt_graph &g, bool use_net) : P_(g.P()), use_net_(use_net)
     {
-        edge_feat_.resize(P_);
-        node_feat_.resize(P_);
         static_mass_.resize(P_);
-        for (uint32_t p = 0; p < P_; p++) {
-            static_mass_[p] = g.edge_off[p + 1] - g.edge_off[p];
-            edge_feat_[p] = std::log1p((float)(g.edge_off[p + 1] - g.edge_off[p])) / 24.0f;
-            node_feat_[p] = std::log1p((float)(g.node_off[p + 1] - g.node_off[p])) / 24.0f;
-        }
-        ring_.assign((size_t)kRing * P_, 0u);
+        for (uint32_t p = 0; p < P_; p++) static_mass_[p] = g.edge_off[p + 1] - g.edge_off[p];
         ema_.assign(P_, 0.f);
         demand_.assign(P_, 0.0);
         snap_t_.assign(kSnaps, 0);
+        stat_.resize(2ull * P_);
+        for (uint32_t p = 0; p < P_; p++) {
+            stat_[p] = std::log1p((float)(g.edge_off[p + 1] - g.edge_off[p])) / 24.0f;
+            stat_[P_ + p] = std::log1p((float)(g.node_off[p + 1] - g.node_off[p])) / 24.0f;
+        }
     }
 
     ~LearnedPolicy() override
     {
         if (ev_) cudaEventDestroy(ev_);
-        host_free(h_loss_);
-        host_free(h_x_);
-        host_free(h_y_);
-        host_free(h_pred_);
+        for (cudaEvent_t e : stage_ev_)
+            if (e) cudaEventDestroy(e);
+        for (void *q : {(void *)d_ring_, (void *)d_ema_, (void *)d_stat_, (void *)d_X_, (void *)d_Y_, (void *)d_out_,
+                        (void *)d_pred_})
+            if (q) cudaFree(q);
+        host_free(h_stage_);
+        host_free(h_out_);
     }
 
     lt_status init(int device)
     {
         if (!use_net_) return LT_OK;
         LT_TRY(net_.init(device, P_, 0x5EEDull));
-        LT_TRY(host_alloc(h_x_, 4ull * kSnaps * P_ * kMlpIn, true));
-        LT_TRY(host_alloc(h_y_, 4ull * P_, true));
-        LT_TRY(host_alloc(h_pred_, 4ull * P_, true));
-        LT_TRY(host_alloc(h_loss_, 16, true));
+        // the network learns a correction to the moving-average forecast:
+        // a zero output layer starts it exactly at that forecast
+        std::vector<float> w(kMlpParams);
+        LT_TRY(net_.get_params(w.data()));
+        for (int j = 0; j <= kMlpHidden; j++) w[kMlpIn * kMlpHidden + kMlpHidden + j] = 0.f;
+        LT_TRY(net_.set_params(w.data()));
+        LT_CUDA_TRY(cudaMalloc(&d_ring_, 4ull * kRing * P_));
+        LT_CUDA_TRY(cudaMalloc(&d_ema_, 4ull * P_));
+        LT_CUDA_TRY(cudaMalloc(&d_stat_, 8ull * P_));
+        LT_CUDA_TRY(cudaMalloc(&d_X_, 4ull * kSnaps * P_ * kMlpIn));
+        LT_CUDA_TRY(cudaMalloc(&d_Y_, 4ull * P_));
+        LT_CUDA_TRY(cudaMalloc(&d_out_, 4ull * (P_ + 2)));
+        LT_CUDA_TRY(cudaMalloc(&d_pred_, 4ull * P_));
+        LT_CUDA_TRY(cudaMemset(d_ring_, 0, 4ull * kRing * P_));
+        LT_CUDA_TRY(cudaMemset(d_ema_, 0, 4ull * P_));
+        LT_CUDA_TRY(cudaMemset(d_out_, 0, 4ull * (P_ + 2)));
+        LT_CUDA_TRY(cudaMemcpy(d_stat_, stat_.data(), 8ull * P_, cudaMemcpyHostToDevice));
+        LT_TRY(host_alloc(h_stage_, 16ull * P_ * kStage, true));
+        LT_TRY(host_alloc(h_out_, 4ull * (P_ + 2), true));
+        if (!h_stage_.pinned || !h_out_.pinned) return fail(LT_ERR_NOMEM, "pinned staging for the prefetcher");
+        void *dv = nullptr;
+        LT_CUDA_TRY(cudaHostGetDevicePointer(&dv, h_stage_.ptr, 0));
+        stage_dev_ = (uint8_t *)dv;
+        LT_CUDA_TRY(cudaHostGetDevicePointer(&dv, h_out_.ptr, 0));
+        out_dev_ = (float *)dv;
         LT_CUDA_TRY(cudaEventCreateWithFlags(&ev_, cudaEventDisableTiming));
+        for (cudaEvent_t &e : stage_ev_) LT_CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
         return LT_OK;
     }
 
@@ -315,104 +450,86 @@ public:
         return best;
     }
 
-    // Zero-copy follows the reference threshold on waiting walkers.
-
-    // Look-ahead: while p computes, load the non-cached partitions with the
-    // most waiting walkers, but only into slots whose partitions are
-    // predicted to be far less busy.
-    void prefetch_order(const SchedView &v, uint32_t exclude, std::vector<uint32_t> &out) override
-    {
-        out.clear();
-        if (!ready_) return;
-        for (uint32_t i = 0; i < v.P; i++)
-            if (i != exclude && v.slot_of[i] < 0 && v.waiting[i] >= v.zc_threshold) out.push_back(i);
-        const size_t k = std::min<size_t>(out.size(), 4);
-        std::partial_sort(out.begin(), out.begin() + k, out.end(), [&](uint32_t a, uint32_t b) {
-            return v.waiting[a] != v.waiting[b] ? v.waiting[a] > v.waiting[b] : a < b;
-        });
-        out.resize(k);
-    }
-
-    // Look-ahead loads measured as a net loss on the 2^33-edge graph (each one
-    // displaced a partition that was needed again); kept available, off.
-    size_t prefetch_depth(const SchedView &) override { return 0; }
-
-    int32_t victim_for_prefetch(const SchedView &v, int32_t computing, uint32_t c) override
-    {
-        const int32_t w = victim(v, computing, c);
-        if (w < 0) return -1;
-        return score(v, c) > 4.0 * score(v, (uint32_t)w) + (double)v.zc_threshold ? w : -1;
-    }
-
     void observe(const SchedView &v) override
     {
         t_++;
-        std::memcpy(&ring_[(size_t)(t_ % kRing) * P_], v.visits, 4ull * P_);
-        for (uint32_t p = 0; p < P_; p++) ema_[p] = 0.95f * ema_[p] + 0.05f * (float)v.visits[p];
-        if (t_ % kEvery) return;
         if (!use_net_) {
+            for (uint32_t p = 0; p < P_; p++) ema_[p] = kEmaKeep * ema_[p] + (1.0f - kEmaKeep) * (float)v.visits[p];
+            if (t_ % kEvery) return;
             for (uint32_t p = 0; p < P_; p++) demand_[p] = (double)ema_[p] * kLabelHorizon;
             ready_ = t_ >= (uint64_t)kLabelHorizon;
             return;
         }
-        // the work enqueued kEvery iterations ago has long finished: take its
-        // predictions, and its host buffers are free again
+        if (failed_) return;
+        // stage this iteration's visits (slot reused kStage iterations later)
+        const int slot = (int)(t_ % kStage);
+        if (cudaEventSynchronize(stage_ev_[slot]) != cudaSuccess) return fail_net();
+        uint8_t *stage = (uint8_t *)h_stage_.ptr + 16ull * P_ * slot;
+        const uint8_t *stage_dev = stage_dev_ + 16ull * P_ * slot;
+        std::memcpy(stage, v.visits, 4ull * P_);
+        cudaStream_t st = net_.stream();
+        const unsigned blocks = (P_ + 255) / 256;
+        pol_iter<<<blocks, 256, 0, st>>>(d_ring_, d_ema_, (const uint32_t *)stage_dev, P_, (uint32_t)(t_ % kRing));
+        if (t_ % kEvery) {
+            if (cudaEventRecord(stage_ev_[slot], st) != cudaSuccess) fail_net();
+            return;
+        }
+        // pick up the previous round if it has finished; never wait for it
         if (inflight_) {
-            cudaEventSynchronize(ev_);
+            if (cudaEventQuery(ev_) != cudaSuccess) {
+                cudaGetLastError();
+                skipped_++;
+                if (cudaEventRecord(stage_ev_[slot], st) != cudaSuccess) fail_net();
+                return;
+            }
             inflight_ = false;
+            const float *out = (const float *)h_out_.ptr;
             if (train_enqueued_) {
-                losses_.push_back({*(const float *)h_loss_.ptr, pending_baseline_});
+                losses_.push_back({out[P_], out[P_ + 1]});
                 train_enqueued_ = false;
             }
             if (pred_enqueued_) {
-                const float *pred = (const float *)h_pred_.ptr;
-                for (uint32_t p = 0; p < P_; p++) demand_[p] = std::expm1(std::max(0.f, pred[p]) * 16.0f);
+                for (uint32_t p = 0; p < P_; p++) demand_[p] = out[p];
                 pred_enqueued_ = false;
                 ready_ = true;
                 predictions_++;
             }
         }
+        float *dyn = (float *)(stage + 4ull * P_);
+        for (uint32_t p = 0; p < P_; p++) {
+            dyn[p] = (float)v.waiting[p];
+            dyn[P_ + p] = v.slot_of[p] >= 0 ? 1.0f : 0.0f;
+            dyn[2 * P_ + p] = (float)(v.iteration - std::min<uint64_t>(v.iteration, v.last_used[p]));
+        }
         const int s = (int)((t_ / kEvery) % kSnaps);
-        float *xs = (float *)h_x_.ptr + (size_t)s * P_ * kMlpIn;
-        features(v, xs);
+        float *Xs = d_X_ + (uint64_t)s * P_ * kMlpIn;
+        pol_features<<<blocks, 256, 0, st>>>(Xs, d_ring_, d_ema_, d_stat_, (const float *)(stage_dev + 4ull * P_), P_,
+                                             t_);
         snap_t_[s] = t_;
         // train on the snapshot whose label horizon has passed
         const int old = (int)(((t_ / kEvery) + kSnaps - (kLabelHorizon / kEvery)) % kSnaps);
-        bool enq = false;
         if (t_ >= (uint64_t)kLabelHorizon + kEvery && snap_t_[old] + kLabelHorizon == t_) {
-            float *y = (float *)h_y_.ptr;
-            for (uint32_t p = 0; p < P_; p++) {
-                float sum = 0.f;
-                for (int k = 0; k < kLabelHorizon; k++) sum += (float)ring_[(size_t)((t_ - k) % kRing) * P_ + p];
-                y[p] = std::log1p(sum) / 16.0f;
-            }
-            const float *xo = (const float *)h_x_.ptr + (size_t)old * P_ * kMlpIn;
-            // the predictor the network replaces: the visit moving average of
-            // the snapshot, scaled to the label horizon
-            double base = 0.0;
-            for (uint32_t p = 0; p < P_; p++) {
-                const float ema = std::expm1(xo[(size_t)p * kMlpIn + 13] * 16.0f);
-                const float yb = std::log1p(ema * (float)kLabelHorizon) / 16.0f;
-                base += (double)(yb - y[p]) * (yb - y[p]);
-            }
-            pending_baseline_ = base / P_;
-            if (net_.train_async(xo, y, P_, kLearningRate, kMomentum, (float *)h_loss_.ptr) == LT_OK) {
-                trained_++;
-                train_enqueued_ = true;
-                enq = true;
-            }
+            const float *Xo = d_X_ + (uint64_t)old * P_ * kMlpIn;
+            pol_labels<<<1, 256, 0, st>>>(d_Y_, d_out_ + P_ + 1, Xo, d_ring_, P_, t_);
+            if (net_.train_dev(Xo, d_Y_, P_, kLearningRate, kMomentum, d_out_ + P_) != LT_OK) return fail_net();
+            trained_++;
+            train_enqueued_ = true;
         }
-        if (trained_ >= 4 && net_.forward_async(xs, P_, (float *)h_pred_.ptr) == LT_OK) {
+        if (trained_ >= 4) {
+            if (net_.forward_dev(Xs, P_, d_pred_) != LT_OK) return fail_net();
+            pol_demand<<<blocks, 256, 0, st>>>(d_out_, d_pred_, Xs, P_);
             pred_enqueued_ = true;
-            enq = true;
         }
-        if (enq && net_.record(ev_) == LT_OK) inflight_ = true;
-        cudaGetLastError();
+        pol_copy<<<blocks, 256, 0, st>>>(out_dev_, d_out_, P_ + 2);
+        if (cudaEventRecord(ev_, st) != cudaSuccess || cudaEventRecord(stage_ev_[slot], st) != cudaSuccess)
+            return fail_net();
+        inflight_ = true;
     }
 
     const char *name() const override { return use_net_ ? "learned" : "frequency"; }
 
     bool single_pass() const override { return false; }
+    bool wave() const override { return true; }
     // Serving keeps few walkers in flight, so reading cold partitions zero-copy
     // costs little and lets every admitted query finish in one step; the
     // network then chooses which partitions hold cache slots.
@@ -449,42 +566,29 @@ public:
 private:
     double score(const SchedView &v, uint32_t p) const { return (double)v.waiting[p] + demand_[p]; }
 
-    float hist(uint32_t p, int k) const
+    // A CUDA error in the policy's own work: keep the last forecasts and stop
+    // training (scheduling decisions never affect results).
+    void fail_net()
     {
-        if ((uint64_t)k >= t_) return 0.f;
-        return std::log1p((float)ring_[(size_t)((t_ - k) % kRing) * P_ + p]) / 16.0f;
-    }
-
-    void features(const SchedView &v, float *xs) const
-    {
-        for (uint32_t p = 0; p < P_; p++) {
-            float *x = xs + (size_t)p * kMlpIn;
-            x[0] = std::log1p((float)v.waiting[p]) / 16.0f;
-            for (int k = 0; k < kHist; k++) x[1 + k] = hist(p, k);
-            x[9] = edge_feat_[p];
-            x[10] = node_feat_[p];
-            x[11] = v.slot_of[p] >= 0 ? 1.0f : 0.0f;
-            x[12] = std::log1p((float)(v.iteration - std::min<uint64_t>(v.iteration, v.last_used[p]))) / 16.0f;
-            x[13] = std::log1p(ema_[p]) / 16.0f;
-            x[14] = (float)p / (float)P_;
-            x[15] = 0.0f;
-        }
+        cudaGetLastError();
+        failed_ = true;
     }
 
     uint32_t P_;
     bool use_net_;
     Mlp net_;
-    uint64_t t_ = 0, trained_ = 0;
-    bool ready_ = false, inflight_ = false, pred_enqueued_ = false, train_enqueued_ = false;
-    double pending_baseline_ = 0.0;
-    uint64_t predictions_ = 0;
+    uint64_t t_ = 0, trained_ = 0, skipped_ = 0, predictions_ = 0;
+    bool ready_ = false, inflight_ = false, pred_enqueued_ = false, train_enqueued_ = false, failed_ = false;
     std::vector<std::pair<double, double>> losses_;  // (network, moving average) per training batch
-    HostBuf h_loss_;
     cudaEvent_t ev_ = nullptr;
-    HostBuf h_x_, h_y_, h_pred_;
-    std::vector<uint32_t> ring_;
+    cudaEvent_t stage_ev_[kStage] = {};
+    HostBuf h_stage_, h_out_;
+    uint8_t *stage_dev_ = nullptr;
+    float *out_dev_ = nullptr;
+    uint32_t *d_ring_ = nullptr;
+    float *d_ema_ = nullptr, *d_stat_ = nullptr, *d_X_ = nullptr, *d_Y_ = nullptr, *d_out_ = nullptr, *d_pred_ = nullptr;
     std::vector<uint64_t> snap_t_, static_mass_;
-    std::vector<float> edge_feat_, node_feat_, ema_;
+    std::vector<float> ema_, stat_;
     std::vector<double> demand_;
 };
 

@@ -102,6 +102,8 @@ struct Ooc {
     HostBuf h_ctl;   // pinned mirror of d_ctl's hist + out_n
     HostBuf h_plan;  // pinned plan block
     HostBuf h_work;  // pinned work list
+    // device views of h_plan / h_work (null: not mapped, upload by copy)
+    uint8_t *h_plan_dev = nullptr, *h_work_dev = nullptr;
     std::vector<uint32_t> arrivals, visits;
     std::vector<uint64_t> waiting, lazy_left;
 
@@ -112,6 +114,9 @@ struct Ooc {
     uint64_t zc_threshold = 0;
     unsigned long long zc_rp_base = 0, zc_col_base = 0;  // device view of the pinned host CSR
     bool single = false;  // single-pass run: partitions outside the cache are read zero-copy
+    // zero-copy set of the next step kernel (wave runs)
+    uint32_t zc_mask[kZcMaskWords] = {};
+    bool zc_mask_any = false;
     int grid[3] = {0, 0, 0};
 
     std::vector<cudaEvent_t> ev_free;
@@ -188,6 +193,32 @@ lt_status set_entry(Ooc &o, uint32_t p, cudaStream_t st)
     set_entry_kernel<<<1, 1, 0, st>>>(o.d_rp, o.d_col, p, o.h_rp[p], o.h_col[p]);
     LT_CUDA_TRY(cudaGetLastError());
     o.e->stats.kernel_launches++;
+    return LT_OK;
+}
+
+__global__ void upload_kernel(uint32_t *dst, const uint32_t *src, uint64_t n)
+{
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) dst[i] = src[i];
+}
+
+// Copy `words` u32 words at h_src (inside the pinned buffer hb, whose device
+// view is hb_dev) to d_dst on the compute stream.  A kernel reading the mapped
+// host buffer does it: an H2D copy on the compute stream would wait on the
+// copy engine behind the partition loads queued on the copy stream.
+lt_status upload(Ooc &o, void *d_dst, const HostBuf &hb, uint8_t *hb_dev, const void *h_src, uint64_t words)
+{
+    lt_engine &e = *o.e;
+    if (words == 0) return LT_OK;
+    if (!hb_dev) {
+        LT_CUDA_TRY(cudaMemcpyAsync(d_dst, h_src, 4 * words, cudaMemcpyHostToDevice, e.s_compute));
+        return LT_OK;
+    }
+    const uint32_t *src = (const uint32_t *)(hb_dev + ((const uint8_t *)h_src - (const uint8_t *)hb.ptr));
+    const uint64_t blocks = std::min<uint64_t>((words + 255) / 256, 304);
+    upload_kernel<<<(unsigned)blocks, 256, 0, e.s_compute>>>((uint32_t *)d_dst, src, words);
+    LT_CUDA_TRY(cudaGetLastError());
+    e.stats.kernel_launches++;
     return LT_OK;
 }
 
@@ -498,7 +529,7 @@ lt_status step_and_bucket_parts(Ooc &o, const RunParams &rp, const std::vector<u
     if (n_chunk_walkers + G > o.staging_cap) return fail(LT_ERR_CAPACITY, "staging area too small");
     if (nw > o.work_cap) return fail(LT_ERR_CAPACITY, "work list too small");
     uint32_t *h_work = (uint32_t *)o.h_work.ptr;
-    uint64_t *h_woff = (uint64_t *)(h_work + o.work_cap);
+    uint64_t *h_woff = (uint64_t *)(h_work + ((o.work_cap + 1) & ~1ull));
     const bool multi = parts.size() > 1;
     {
         uint64_t k = 0, ord = 0;
@@ -512,9 +543,8 @@ lt_status step_and_bucket_parts(Ooc &o, const RunParams &rp, const std::vector<u
         }
     }
     if (nw) {
-        LT_CUDA_TRY(cudaMemcpyAsync(o.d_work, h_work, 4 * nw, cudaMemcpyHostToDevice, e.s_compute));
-        if (multi)
-            LT_CUDA_TRY(cudaMemcpyAsync(o.d_work_off, h_woff, 8 * nw, cudaMemcpyHostToDevice, e.s_compute));
+        LT_TRY(upload(o, o.d_work, o.h_work, o.h_work_dev, h_work, nw));
+        if (multi) LT_TRY(upload(o, o.d_work_off, o.h_work, o.h_work_dev, h_woff, 2 * nw));
     }
     LT_CUDA_TRY(cudaMemsetAsync(o.d_ctl, 0, 4 * o.ctl_words, e.s_compute));
 
@@ -551,6 +581,9 @@ lt_status step_and_bucket_parts(Ooc &o, const RunParams &rp, const std::vector<u
     a.next = o.ctl_next();
     a.stats = o.d_stats;
     a.zc_part = kNoPart;
+    a.zc_rp_base = o.zc_rp_base;
+    a.zc_col_base = o.zc_col_base;
+    if (o.zc_mask_any) std::memcpy(a.zc_mask, o.zc_mask, sizeof a.zc_mask);
     if (o.serve) serve_args(o, a);
     if (zero_copy) {
         a.zc_part = (uint32_t)p;
@@ -558,12 +591,13 @@ lt_status step_and_bucket_parts(Ooc &o, const RunParams &rp, const std::vector<u
         a.zc_col = o.zc_col_base + 4ull * g.edge_off[p];
     }
 
-    Ooc::Timed t{ev_get(o), ev_get(o), zero_copy ? kTZero : kTCompute};
+    const bool zc_launch = zero_copy || o.zc_mask_any;
+    Ooc::Timed t{ev_get(o), ev_get(o), zc_launch ? kTZero : kTCompute};
     LT_CUDA_TRY(cudaEventRecord(t.a, e.s_compute));
     LT_CUDA_TRY(launch_walk_part(a, rp.app, o.grid[rp.app], e.s_compute));
     LT_CUDA_TRY(cudaEventRecord(t.b, e.s_compute));
     o.timed.push_back(t);
-    if (zero_copy)
+    if (zc_launch)
         e.stats.zerocopy_calls++;
     else
         e.stats.computing_calls++;
@@ -635,7 +669,7 @@ lt_status step_and_bucket_parts(Ooc &o, const RunParams &rp, const std::vector<u
         refresh(o, d);
     }
     if (n_plan > o.plan_cap) return fail(LT_ERR_CAPACITY, "plan buffer too small");
-    LT_CUDA_TRY(cudaMemcpyAsync(o.d_planbuf, h_cursor, 4ull * (2ull * o.P + n_plan), cudaMemcpyHostToDevice, e.s_compute));
+    LT_TRY(upload(o, o.d_planbuf, o.h_plan, o.h_plan_dev, h_cursor, 2ull * o.P + n_plan));
     ScatterArgs sa{};
     sa.in_cur = a.out_cur;
     sa.in_step = a.out_step;
@@ -694,7 +728,12 @@ lt_status ensure_pool(Ooc &o, uint64_t W)
     LT_TRY(dalloc(&o.d_work, o.work_cap));
     LT_TRY(dalloc(&o.d_work_off, o.work_cap));
     LT_TRY(host_alloc(o.h_plan, 4 * (2ull * o.P + o.plan_cap), true));
-    LT_TRY(host_alloc(o.h_work, 12 * o.work_cap, true));
+    LT_TRY(host_alloc(o.h_work, 12 * o.work_cap + 8, true));
+    o.h_plan_dev = o.h_work_dev = nullptr;
+    void *dv = nullptr;
+    if (o.h_plan.pinned && cudaHostGetDevicePointer(&dv, o.h_plan.ptr, 0) == cudaSuccess) o.h_plan_dev = (uint8_t *)dv;
+    if (o.h_work.pinned && cudaHostGetDevicePointer(&dv, o.h_work.ptr, 0) == cudaSuccess) o.h_work_dev = (uint8_t *)dv;
+    cudaGetLastError();
     return LT_OK;
 }
 
@@ -807,6 +846,192 @@ lt_status single_pass_run(Ooc &o, const RunParams &rp, uint64_t W)
     return LT_OK;
 }
 
+// Walkers that can be created in a kernel that drains `chunks` chunks holding
+// `walkers` walkers (the multi-partition form of lazy_budget).
+uint64_t wave_lazy_budget(Ooc &o, uint64_t chunks, uint64_t walkers, uint64_t left)
+{
+    const uint64_t avail = o.free_chunks.size() + chunks;
+    if (avail <= (uint64_t)o.P + 1) return 0;
+    uint64_t g = (avail - o.P - 1) * kChunk;
+    g = g > walkers ? g - walkers : 0;
+    if (g + walkers > o.staging_cap) g = o.staging_cap > walkers ? o.staging_cap - walkers : 0;
+    return std::min(g, left);
+}
+
+constexpr uint64_t kSweepWalkers = 1ull << 18;    // about one walker per resident lane
+constexpr uint64_t kZcGroupBytes = 64ull << 20;   // zero-copy group: about half the L2
+
+// Wave run.  Iteration i: publish the loads started in iteration i-1; drain,
+// in one step kernel, the queues of every cached partition (the ones just
+// loaded hold the walkers that queued for them) and create new walkers into
+// the room the pool has; start the loads for iteration i+1 -- the partitions
+// not cached with the most waiting walkers, at least the zero-copy threshold
+// -- on the copy stream, so they overlap this kernel, their slots taken from
+// idle cached partitions with the lowest cache_score.  When nothing is worth a
+// load and no walker can be created, every partition outside the cache is
+// read zero-copy in one kernel (the final phase).  Results are those of the
+// reference loop: every draw is keyed by walker and step.
+lt_status wave_run(Ooc &o, const RunParams &rp)
+{
+    lt_engine &e = *o.e;
+    const bool zc_ok = o.zc_rp_base != 0 && o.P <= kSmemPartMax && o.zc_threshold > 0;
+    const uint64_t load_min = zc_ok ? o.zc_threshold : 1;
+    const uint64_t reserve = (uint64_t)o.P + 2;
+    std::vector<std::pair<uint32_t, cudaEvent_t>> inflight;
+    std::vector<uint32_t> parts, cand, idle;
+    std::vector<char> draining(o.P, 0), loading(o.P, 0);
+    int stalls = 0;
+    while (true) {
+        for (auto &d : inflight) {
+            LT_CUDA_TRY(cudaStreamWaitEvent(e.s_compute, d.second, 0));
+            LT_TRY(set_entry(o, d.first, e.s_compute));
+            loading[d.first] = 0;
+        }
+        inflight.clear();
+        refresh_all(o);
+        bool any = false;
+        for (uint32_t p = 0; p < o.P && !any; p++) any = o.waiting[p] > 0;
+        if (!any) break;
+        o.iteration++;
+        e.stats.iterations++;
+
+        // drain set: cached partitions with queued walkers; spilled ones come back first
+        parts.clear();
+        for (uint32_t p = 0; p < o.P; p++) {
+            draining[p] = 0;
+            if (o.slot_of[p] < 0) continue;
+            Queue &qp = o.q[p];
+            if (!qp.host_chunks.empty()) {
+                const uint64_t room = o.free_chunks.size() > reserve ? o.free_chunks.size() - reserve : 0;
+                if (room) LT_TRY(unspill(o, p, std::min<uint64_t>(qp.host_chunks.size(), room)));
+            }
+            if (!qp.dev_chunks.empty()) {
+                parts.push_back(p);
+                draining[p] = 1;
+                o.last_used[p] = o.iteration;
+            }
+        }
+
+        // loads for the next kernel
+        SchedView v = view(o);
+        cand.clear();
+        for (uint32_t p = 0; p < o.P; p++)
+            if (o.slot_of[p] < 0 && o.waiting[p] >= load_min) cand.push_back(p);
+        std::sort(cand.begin(), cand.end(), [&](uint32_t a, uint32_t b) {
+            return o.waiting[a] != o.waiting[b] ? o.waiting[a] > o.waiting[b] : a < b;
+        });
+        idle.clear();
+        for (uint32_t p = 0; p < o.P; p++)
+            if (o.slot_of[p] >= 0 && !draining[p] && o.waiting[p] == 0) idle.push_back(p);
+        std::vector<double> sc(o.P, 0.0);
+        for (uint32_t p : idle) sc[p] = o.policy->cache_score(v, p);
+        std::sort(idle.begin(), idle.end(), [&](uint32_t a, uint32_t b) {
+            if (sc[a] != sc[b]) return sc[a] < sc[b];
+            return o.last_used[a] != o.last_used[b] ? o.last_used[a] < o.last_used[b] : a < b;
+        });
+        size_t n_idle = 0, started = 0;
+        const size_t m = std::max<size_t>(1, o.policy->wave_loads());
+        for (uint32_t c : cand) {
+            if (started >= m) break;
+            int32_t slot = free_slot(o);
+            if (slot < 0) {
+                if (n_idle >= idle.size()) break;
+                const uint32_t w = idle[n_idle++];
+                slot = o.slot_of[w];
+                LT_TRY(evict_partition(o, w));
+            }
+            LT_TRY(start_load(o, c, slot, &inflight));
+            loading[c] = 1;
+            o.last_used[c] = o.iteration;
+            started++;
+        }
+        if (started) e.stats.explicit_iterations++;
+
+        // walkers to create: into a readable partition if one has them
+        uint64_t chunks = 0, walkers = 0;
+        for (uint32_t p : parts) {
+            chunks += o.q[p].dev_chunks.size();
+            walkers += o.q[p].dev_count();
+        }
+        int32_t lazy_p = -1;
+        for (int pass = 0; pass < 2 && lazy_p < 0; pass++)
+            for (uint32_t p = 0; p < o.P; p++) {
+                if (o.lazy_left[p] == 0 || loading[p]) continue;
+                if (pass == 0 && o.slot_of[p] < 0) continue;
+                if (lazy_p < 0 || o.lazy_left[p] > o.lazy_left[lazy_p]) lazy_p = (int32_t)p;
+            }
+        uint64_t G = lazy_p >= 0 ? wave_lazy_budget(o, chunks, walkers, o.lazy_left[lazy_p]) : 0;
+
+        // Nothing worth a load and no room for new walkers: read partitions
+        // outside the cache zero-copy.  Zero-copy hops are fast only while
+        // the host lines they touch stay in L2, so the partitions go in groups
+        // of about half the L2, most waiting walkers first; once few walkers
+        // are left, one sweep makes every partition readable and finishes
+        // them in a single, latency-bound kernel.
+        std::memset(o.zc_mask, 0, sizeof o.zc_mask);
+        o.zc_mask_any = false;
+        bool lazy_left = false;
+        for (uint32_t p = 0; p < o.P && !lazy_left; p++) lazy_left = o.lazy_left[p] > 0;
+        if (zc_ok && cand.empty() && inflight.empty() && (G == 0 || !lazy_left)) {
+            uint64_t outside = 0;
+            std::vector<uint32_t> group;
+            for (uint32_t p = 0; p < o.P; p++)
+                if (o.slot_of[p] < 0 && o.waiting[p] > 0) {
+                    outside += o.waiting[p];
+                    group.push_back(p);
+                }
+            const bool sweep = outside <= kSweepWalkers;
+            if (!sweep) {
+                std::sort(group.begin(), group.end(), [&](uint32_t a, uint32_t b) {
+                    return o.waiting[a] != o.waiting[b] ? o.waiting[a] > o.waiting[b] : a < b;
+                });
+                uint64_t bytes = 0;
+                size_t n = 0;
+                while (n < group.size() && (n == 0 || bytes + o.g->slot_bytes(group[n]) <= kZcGroupBytes))
+                    bytes += o.g->slot_bytes(group[n++]);
+                group.resize(n);
+            } else {
+                group.clear();
+                for (uint32_t p = 0; p < o.P; p++)
+                    if (o.slot_of[p] < 0) group.push_back(p);
+            }
+            for (uint32_t p : group) {
+                o.zc_mask[p >> 5] |= 1u << (p & 31);
+                o.zc_mask_any = true;
+                Queue &qp = o.q[p];
+                if (!qp.host_chunks.empty()) {
+                    const uint64_t room = o.free_chunks.size() > reserve ? o.free_chunks.size() - reserve : 0;
+                    if (room) LT_TRY(unspill(o, p, std::min<uint64_t>(qp.host_chunks.size(), room)));
+                }
+                if (!qp.dev_chunks.empty()) {
+                    parts.push_back(p);
+                    chunks += qp.dev_chunks.size();
+                    walkers += qp.dev_count();
+                }
+            }
+            if (lazy_p >= 0) G = wave_lazy_budget(o, chunks, walkers, o.lazy_left[lazy_p]);
+        }
+        if (parts.empty() && G == 0 && inflight.empty()) {
+            // Nothing readable holds walkers, none can be created and nothing
+            // is loading: the pool is full of walkers queued outside the cache
+            // while the cached partitions wait for spilled or uncreated ones.
+            // Spill to make room, then try again.
+            o.zc_mask_any = false;
+            if (++stalls > 2)
+                return fail(LT_ERR_CAPACITY, "wave scheduler cannot make progress (walker pool or cache too small)");
+            LT_TRY(spill_until(o, std::min<uint64_t>(o.n_chunks, reserve + 64), -1));
+            continue;
+        }
+        stalls = 0;
+        const Lazy lz = lazy_p >= 0 ? lazy_of(o, rp, lazy_p, o.q[lazy_p].lazy_next, G) : Lazy{};
+        LT_TRY(step_and_bucket_parts(o, rp, parts, lazy_p, lz, false, nullptr));
+        o.zc_mask_any = false;
+        drain_timers(o, false);
+        o.policy->observe(view(o));
+    }
+    return LT_OK;
+}
+
 }  // namespace
 
 lt_status ooc_create(lt_engine *e, Ooc **out)
@@ -852,6 +1077,8 @@ lt_status ooc_create(lt_engine *e, Ooc **out)
     o->q.assign(o->P, Queue{});
     if (e->cfg.sched == LT_SCHED_FIFO) {
         o->policy.reset(new FifoPolicy());
+    } else if (e->cfg.sched == LT_SCHED_BATCHED) {
+        o->policy.reset(new BatchedPolicy());
     } else if (e->cfg.sched == LT_SCHED_LEARNED || e->cfg.sched == LT_SCHED_FREQUENCY) {
         Policy *lp = nullptr;
         s = make_learned_policy(g, e->device, e->cfg.sched == LT_SCHED_LEARNED, &lp);
@@ -989,6 +1216,10 @@ lt_status ooc_run(lt_engine *e, int app, int start, uint32_t source, uint64_t W,
             }
         }
         refresh_all(o);
+        if (o.policy->wave()) {
+            LT_TRY(wave_run(o, rp));
+            continue;
+        }
         // Scheduler::start (src/Scheduler.h:425-438)
         bool sync = false;
         uint32_t p = 0;

@@ -68,6 +68,15 @@ public:
     virtual size_t swap_budget() const { return 0; }
     // a cached partition is given up only for one scoring swap_ratio() times higher
     virtual double swap_ratio() const { return 1.25; }
+    // Wave runs: each step kernel drains every readable queue (all cached
+    // partitions with walkers, plus a zero-copy set in the final phase) while
+    // the loads for the next kernel run on the copy stream.  At most
+    // wave_loads() loads start per kernel: the partitions not cached with the
+    // most waiting walkers (at least the zero-copy threshold), into the slots
+    // of idle cached partitions with the lowest cache_score (ties: least
+    // recently used).
+    virtual bool wave() const { return false; }
+    virtual size_t wave_loads() const { return 8; }
     // Cache emptied (the learned state of a policy survives).
     virtual void reset() {}
     virtual void stats(lt_policy_stats &s) const
@@ -76,6 +85,14 @@ public:
         std::strncpy(s.name, name(), sizeof s.name - 1);
     }
     virtual const char *name() const { return "plain"; }
+};
+
+// The plain policy's rules executed as wave runs (least recently used
+// victims): separates what wave execution gains from what predictions gain.
+class BatchedPolicy : public Policy {
+public:
+    bool wave() const override { return true; }
+    const char *name() const override { return "batched"; }
 };
 
 class FifoPolicy : public Policy {

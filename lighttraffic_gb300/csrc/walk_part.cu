@@ -90,12 +90,14 @@ __global__ void __launch_bounds__(kPartBlock) walk_part_kernel(StepArgs a)
     uint32_t *s_off = smem;
     uint32_t *s_hist = smem + (P + 1);
     uint32_t *s_visit = s_hist + P;
+    uint32_t *s_zc = s_visit + P;
     if (in_smem) {
         for (uint32_t i = threadIdx.x; i <= P; i += blockDim.x) s_off[i] = a.t.node_off[i];
         for (uint32_t i = threadIdx.x; i < P; i += blockDim.x) {
             s_hist[i] = 0;
             s_visit[i] = 0;
         }
+        for (uint32_t i = threadIdx.x; i < (P + 31) / 32; i += blockDim.x) s_zc[i] = a.zc_mask[i];
     }
     __syncthreads();
     const uint32_t *off = in_smem ? s_off : a.t.node_off;
@@ -193,9 +195,19 @@ __global__ void __launch_bounds__(kPartBlock) walk_part_kernel(StepArgs a)
             if (need_graph && (cur < cp_nb || cur >= cp_ne)) {
                 const uint32_t p = find_part(off, P, cur);
                 atomicAdd(&visit[p], 1u);
-                const bool zc = p == a.zc_part;
-                const unsigned long long rp = zc ? (a.zc_rp | 1ull)
-                                                 : *(volatile const unsigned long long *)&a.t.rp_addr[p];
+                unsigned long long rp, col = 0;
+                if (p == a.zc_part) {
+                    rp = a.zc_rp | 1ull;
+                    col = a.zc_col;
+                } else {
+                    rp = *(volatile const unsigned long long *)&a.t.rp_addr[p];
+                    if (rp != 0ull) {
+                        col = *(volatile const unsigned long long *)&a.t.col_addr[p];
+                    } else if (in_smem && ((s_zc[p >> 5] >> (p & 31)) & 1u)) {
+                        rp = (a.zc_rp_base + 8ull * off[p]) | 1ull;
+                        col = a.zc_col_base + 4ull * a.t.edge_off[p];
+                    }
+                }
                 if (rp == 0ull) {
                     emit = true;
                     dest = p;
@@ -203,7 +215,7 @@ __global__ void __launch_bounds__(kPartBlock) walk_part_kernel(StepArgs a)
                     cp_nb = off[p];
                     cp_ne = off[p + 1];
                     cp_rp = rp & ~1ull;
-                    cp_col = zc ? a.zc_col : *(volatile const unsigned long long *)&a.t.col_addr[p];
+                    cp_col = col;
                     cp_eb = a.t.edge_off[p];
                     cp_zc = (rp & 1ull) != 0;
                 }
@@ -407,7 +419,7 @@ int occ_part(size_t smem)
 
 }  // namespace
 
-size_t part_smem(uint32_t P) { return P <= kSmemPartMax ? sizeof(uint32_t) * (3ull * P + 1) : 0; }
+size_t part_smem(uint32_t P) { return P <= kSmemPartMax ? sizeof(uint32_t) * (3ull * P + 1 + (P + 31) / 32) : 0; }
 
 int part_grid(int app, int /*start*/, int device, size_t smem)
 {

@@ -17,6 +17,7 @@ constexpr uint32_t kChunk = 8192;                         // walkers per chunk
 constexpr uint64_t kChunkBytes = 16ull * kChunk;           // 128 KiB
 constexpr int kPartBlock = 256;
 constexpr uint32_t kSmemPartMax = 4096;                    // P up to this keeps node_off / histograms in smem
+constexpr uint32_t kZcMaskWords = kSmemPartMax / 32;       // zero-copy set of one launch, one bit per partition
 
 // Device view of the partition table: node / edge ranges of every partition
 // and, for readable partitions, the addresses of their rowptr slice (n+1
@@ -68,6 +69,11 @@ struct StepArgs {
     // device-visible addresses of pinned host memory
     uint32_t zc_part;
     unsigned long long zc_rp, zc_col;
+    // further partitions read zero-copy in this launch (wave runs): bit p of
+    // zc_mask (P <= kSmemPartMax only), read at zc_rp_base + 8 node_off[p]
+    // and zc_col_base + 4 edge_off[p] when the table marks p unreadable
+    unsigned long long zc_rp_base, zc_col_base;
+    uint32_t zc_mask[kZcMaskWords];
     // query mode (serving many PPR queries): per query slot its key, table and
     // finished-walker counter; endpoints go to the query's table instead of
     // `counts`.  q_seed == null: single-run mode.

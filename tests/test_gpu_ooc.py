@@ -31,8 +31,12 @@ CASES = [
     (4, 0, None, 0),         # default threshold partitionSize/128/2
     (3, 20000, 0, 0),        # tiny walker pool: host spills
     (5, 0, 0, 1),            # FIFO policy
-    (4, 0, None, 2),         # learned: cache by predicted visits, the rest zero-copy
-    (2, 20000, None, 3),     # frequency ablation
+    (4, 0, None, 2),         # learned (wave runs): cache by predicted visits
+    (2, 20000, None, 3),     # frequency ablation, host spills
+    (4, 0, None, 4),         # batched: wave runs, least recently used slots
+    (1, 0, 0, 4),            # wave runs through a single slot, no zero-copy
+    (3, 20000, 0, 2),        # learned, tiny walker pool, no zero-copy
+    (4, 0, 1 << 40, 4),      # wave runs with every cold partition read zero-copy
 ]
 
 
@@ -49,13 +53,11 @@ def test_ppr_ooc(lt, require_gpu, g16, case):
     s = e.stats()
     assert s["moves"] == st[1]
     assert s["iterations"] >= 1
-    if sched >= 2:
-        return                                   # single pass: no queues, no spills
     if zc == 0:
         assert s["h2d_graph_bytes"] > 0 and s["zerocopy_calls"] == 0
     if zc == 1 << 40:
         assert s["zerocopy_calls"] > 0
-    if B:
+    if B and sched < 2:
         assert s["d2h_walker_bytes"] > 0 and s["h2d_walker_bytes"] > 0
 
 
@@ -116,3 +118,15 @@ def test_c0_ooc_full_size(lt, require_gpu):
     assert (got == want).all()
     s = e.stats()
     assert s["partition_loads"] >= 2
+
+
+def test_wave_runs_take_fewer_iterations(lt, require_gpu, g16):
+    """A wave drains every cached queue per kernel: far fewer iterations than
+    the one-partition-per-iteration reference loop, same counts."""
+    rp, col = g16
+    res = {}
+    for sched in (0, 4):
+        g, e = _eng(lt, rp, col, 256 << 10, partitions=4, sched=sched, seed=9)
+        res[sched] = (e.ppr(0, 300000, 0.15), e.stats())
+    assert (res[0][0] == res[4][0]).all()
+    assert res[4][1]["iterations"] < res[0][1]["iterations"]
