@@ -1,7 +1,7 @@
 #!/usr/bin/env python3
 """Benchmark of the random-walk hot path on GB300.
 
-    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference] [--config c2|c2s|c1|c0|c3|c4]
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference] [--config c2|c2s|c1|c0|c3|c3s|c4]
 
 Workloads (synthetic RMAT graphs, a=.57 b=.19 c=.19 d=.05, seed 1, isolated
 vertices removed, stand in for the reference's datasets, which are absent):
@@ -29,6 +29,7 @@ vertices removed, stand in for the reference's datasets, which are absent):
       u32 sparse counts; `value` times lt_ppr_batch_device (the captured
       batch pipeline) on device buffers after the autotuner, `e2e` lt_ppr_batch
       with host buffers.
+  c3s: c3 scaled down for profiler captures -- RMAT(2^22, 2^26), 256 sources.
   c4: serving PPR on the c2 graph and cache: Poisson arrivals at 100, 1 000
       and 10 000 queries/s, uniform random sources, lognormal walk counts
       (median 1e4, sigma 1.0 -- left open by the workload) clipped to
@@ -73,6 +74,9 @@ CONFIGS = {
     "c3": dict(workload="ppr-batch4096-zipf1.1-lognormal-rmat26-e30", app=0, scale=26, edges=1 << 30, length=0,
                start=0, prob=0.15, part_mb=32, queries=4096, zipf=1.1, walk_median=1e4, walk_sigma=1.5,
                walk_min=1e3, walk_max=1e6, batch_queries=True),
+    "c3s": dict(workload="ppr-batch256-zipf1.1-lognormal-rmat22-e26", app=0, scale=22, edges=1 << 26, length=0,
+                start=0, prob=0.15, part_mb=32, queries=256, zipf=1.1, walk_median=1e4, walk_sigma=1.5,
+                walk_min=1e3, walk_max=1e6, batch_queries=True),
 }
 SEED_GRAPH = 1
 SEED_WALK = 1

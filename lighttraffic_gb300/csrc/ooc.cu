@@ -859,7 +859,7 @@ uint64_t wave_lazy_budget(Ooc &o, uint64_t chunks, uint64_t walkers, uint64_t le
 }
 
 constexpr uint64_t kSweepWalkers = 1ull << 18;    // about one walker per resident lane
-constexpr uint64_t kZcGroupBytes = 64ull << 20;   // zero-copy group: about half the L2
+constexpr uint64_t kZcGroupBytes = 128ull << 20;  // zero-copy group: host bytes touched, about the L2
 
 // Wave run.  Iteration i: publish the loads started in iteration i-1; drain,
 // in one step kernel, the queues of every cached partition (the ones just
@@ -965,9 +965,9 @@ lt_status wave_run(Ooc &o, const RunParams &rp)
         // Nothing worth a load and no room for new walkers: read partitions
         // outside the cache zero-copy.  Zero-copy hops are fast only while
         // the host lines they touch stay in L2, so the partitions go in groups
-        // of about half the L2, most waiting walkers first; once few walkers
-        // are left, one sweep makes every partition readable and finishes
-        // them in a single, latency-bound kernel.
+        // whose estimated footprint is about the L2, most waiting walkers
+        // first; once few walkers are left, one sweep makes every partition
+        // readable and finishes them in a single, latency-bound kernel.
         std::memset(o.zc_mask, 0, sizeof o.zc_mask);
         o.zc_mask_any = false;
         bool lazy_left = false;
@@ -985,10 +985,13 @@ lt_status wave_run(Ooc &o, const RunParams &rp)
                 std::sort(group.begin(), group.end(), [&](uint32_t a, uint32_t b) {
                     return o.waiting[a] != o.waiting[b] ? o.waiting[a] > o.waiting[b] : a < b;
                 });
+                // host bytes a partition's walkers touch: at most the partition,
+                // else about two 128-byte lines per hop, two hops per walker
+                auto footprint = [&](uint32_t p) { return std::min<uint64_t>(o.g->slot_bytes(p), 512 * o.waiting[p]); };
                 uint64_t bytes = 0;
                 size_t n = 0;
-                while (n < group.size() && (n == 0 || bytes + o.g->slot_bytes(group[n]) <= kZcGroupBytes))
-                    bytes += o.g->slot_bytes(group[n++]);
+                while (n < group.size() && (n == 0 || bytes + footprint(group[n]) <= kZcGroupBytes))
+                    bytes += footprint(group[n++]);
                 group.resize(n);
             } else {
                 group.clear();
