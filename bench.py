@@ -436,45 +436,69 @@ def gb300_resident(args, cfg):
     d_st = torch.zeros(3, dtype=torch.int64, device=dev)
     stream = torch.cuda.current_stream()
     app, start, length, prob = cfg["app"], cfg["start"], cfg["length"], cfg["prob"]
+    # compact layout (u32 row offsets and counters), what the engine runs when
+    # E and the pass's counter updates fit 32 bits; the u64 layout beside it
+    compact_ok = E < (1 << 32) and (W * max(1, length) if app == 1 else W) < (1 << 32)
+    d_rp32 = torch.zeros(V + 1, dtype=torch.int32, device=dev)
+    d_cnt32 = torch.zeros(V, dtype=torch.int32, device=dev)
+    if compact_ok:
+        lt.check(lt.lib.lt_rowptr_narrow(d_rp.data_ptr(), d_rp32.data_ptr(), V, stream.cuda_stream))
 
-    def launch():
+    def launch_std():
+        d_cnt.zero_()
         lt.check(lt.lib.lt_walk_device(app, start, d_rp.data_ptr(), d_col.data_ptr(), V, 0, W, length,
                                        ctypes.c_float(prob), 0, SEED_WALK, d_cnt.data_ptr(), None, None,
                                        d_scr.data_ptr(), d_st.data_ptr(), stream.cuda_stream))
 
+    def launch_compact():
+        d_cnt32.zero_()
+        lt.check(lt.lib.lt_walk_device_compact(app, start, d_rp32.data_ptr(), d_col.data_ptr(), V, 0, W, length,
+                                               ctypes.c_float(prob), 0, SEED_WALK, d_cnt32.data_ptr(), None, None,
+                                               d_scr.data_ptr(), d_st.data_ptr(), stream.cuda_stream))
+
+    def timed(launch):
+        for _ in range(args.warmup):
+            launch()
+        torch.cuda.synchronize()
+        d_st.zero_()
+        starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+        ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+        t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize()
+        t0.record()
+        for i in range(args.steps):
+            starts[i].record()
+            launch()
+            ends[i].record()
+        t1.record()
+        torch.cuda.synchronize()
+        el = max_over_ranks(dist, local, t0.elapsed_time(t1))
+        st = d_st.cpu().numpy().astype(np.uint64) // np.uint64(args.steps)
+        return el, [x.elapsed_time(y) for x, y in zip(starts, ends)], st
+
     clocks = ClockSampler(local)
     clocks.start()
     time.sleep(0.3)
-    for _ in range(args.warmup):
-        d_cnt.zero_()
-        launch()
-    torch.cuda.synchronize()
-    d_st.zero_()
-    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    t_all0, t_all1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    if dist:
-        dist.barrier()
-    torch.cuda.synchronize()
     wall0 = time.time()
-    t_all0.record()
-    for i in range(args.steps):
-        d_cnt.zero_()
-        starts[i].record()
-        launch()
-        ends[i].record()
-    t_all1.record()
-    torch.cuda.synchronize()
-    elapsed_ms = max_over_ranks(dist, local, t_all0.elapsed_time(t_all1))
-    kern_ms = [a.elapsed_time(b) for a, b in zip(starts, ends)]
-    st = d_st.cpu().numpy().astype(np.uint64) // np.uint64(args.steps)
+    std_ms, std_kern, std_st = timed(launch_std)
+    std_total = int(d_cnt.sum().item())
+    if compact_ok:
+        elapsed_ms, kern_ms, st = timed(launch_compact)
+        total = int(d_cnt32.to(torch.int64).sum().item())
+        assert (std_st == st).all(), "compact and u64 layouts took different steps"
+    else:
+        elapsed_ms, kern_ms, st, total = std_ms, std_kern, std_st, std_total
     updates, moves, tele = (int(x) for x in st)
     steps_per_pass = updates if app == 1 else moves
-    total = int(d_cnt.sum().item())
-    assert total == (W * length if app == 1 else W), "invariant violated in the timed pass"
+    assert total == (W * length if app == 1 else W) == std_total, "invariant violated in the timed pass"
     value = steps_per_pass * args.steps * ws / (elapsed_ms / 1e3)
     counter_updates = updates if app == 1 else W
-    alg_bytes = 20 * moves + 16 * counter_updates
+    # algorithmic bytes: row-offset pair + column entry per hop, counter
+    # read-modify-write per update, at the width of the layout timed
+    ob, cb = (4, 4) if compact_ok else (8, 8)
+    alg_bytes = (2 * ob + 4) * moves + 2 * cb * counter_updates
     mean_kern_s = statistics.mean(kern_ms) / 1e3
     peak, peak_src = measured_peak("hbm_gbs", 6800.0)
     achieved = alg_bytes / mean_kern_s / 1e9
@@ -510,9 +534,13 @@ def gb300_resident(args, cfg):
                    "l2": "inputs larger than L2 (graph %d MiB > 129 MB L2), no flush" % ((8 * (V + 1) + 4 * E) >> 20),
                    "parallelism": "replicas" if ws > 1 else "1 GPU"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": profiled_traffic(cfg["workload"]), "kernel": "walk_whole_kernel",
+                     "traffic": profiled_traffic(cfg["workload"] + ("-compact" if compact_ok else "")),
+                     "kernel": "walk_whole_kernel" + (" (compact layout)" if compact_ok else ""),
                      "alg_bytes_per_launch": alg_bytes, "mean_launch_ms": mean_kern_s * 1e3,
                      "peak_source": peak_src},
+        "layout": "compact (u32 row offsets and counters)" if compact_ok else "u64 row offsets and counters",
+        "u64_layout": {"value": steps_per_pass * args.steps * ws / (std_ms / 1e3), "ms_per_step": std_ms / args.steps,
+                       "mean_launch_ms": statistics.mean(std_kern)},
         "e2e": {"value": steps_per_pass * ws / e2e_s, "unit": "steps/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": 8 * V, "ms_per_step": e2e_s * 1e3},
         "gpu_launches": args.steps,

@@ -221,6 +221,24 @@ lt_status lt_walk_device(int app, int start_mode, const uint64_t *d_rowptr, cons
                          uint64_t *d_counts, uint32_t *d_endpoints, uint32_t *d_paths,
                          void *d_scratch, uint64_t *d_stats, void *stream);
 
+/* lt_walk_device on the compact layout: u32 row offsets (any graph with
+ * E < 2^32; lt_rowptr_narrow makes them from the u64 ones) and u32 counters.
+ * Same step kernel (src/WalkManager.h:229-246) and identical results; the two
+ * arrays every update reuses take half the bytes, so they stay in L2.
+ *   d_counts32 : u32[V], added to (PPR / PageRank); a call is rejected with
+ *                LT_ERR_INVALID when its counter updates (W for PPR,
+ *                W * length for PageRank) reach 2^32.  Counters that start at
+ *                zero therefore cannot wrap within one call.
+ * Other arguments as lt_walk_device. */
+lt_status lt_walk_device_compact(int app, int start_mode, const uint32_t *d_rowptr32, const uint32_t *d_col,
+                                 uint32_t num_nodes, uint32_t source, uint64_t num_walkers,
+                                 uint32_t length, float prob, uint32_t run, uint64_t seed,
+                                 uint32_t *d_counts32, uint32_t *d_endpoints, uint32_t *d_paths,
+                                 void *d_scratch, uint64_t *d_stats, void *stream);
+/* d_rowptr32[i] = d_rowptr[i] for i <= num_nodes (edge offsets below 2^32),
+ * on `stream`. */
+lt_status lt_rowptr_narrow(const uint64_t *d_rowptr, uint32_t *d_rowptr32, uint32_t num_nodes, void *stream);
+
 /* lt_walk_device without the scratch argument, for callers that cannot
  * allocate device memory (inside a stream capture, or when a host framework
  * owns every device allocation and hands over only inputs and outputs).  No

@@ -129,6 +129,9 @@ def _load():
                           C.POINTER(C.c_float), C.POINTER(C.c_float), C.POINTER(C.c_float)], C.c_int),
         "lt_walk_device": ([C.c_int, C.c_int, vp, vp, C.c_uint32, C.c_uint32, C.c_uint64, C.c_uint32,
                             C.c_float, C.c_uint32, C.c_uint64, vp, vp, vp, vp, vp, vp], C.c_int),
+        "lt_walk_device_compact": ([C.c_int, C.c_int, vp, vp, C.c_uint32, C.c_uint32, C.c_uint64, C.c_uint32,
+                                    C.c_float, C.c_uint32, C.c_uint64, vp, vp, vp, vp, vp, vp], C.c_int),
+        "lt_rowptr_narrow": ([vp, vp, C.c_uint32, vp], C.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)

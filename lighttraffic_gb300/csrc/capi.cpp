@@ -372,4 +372,19 @@ lt_status lt_walk_device(int app, int start_mode, const uint64_t *d_rowptr, cons
                        d_counts, d_endpoints, d_paths, d_scratch, d_stats, (cudaStream_t)stream, 0);
 }
 
+lt_status lt_walk_device_compact(int app, int start_mode, const uint32_t *d_rowptr32, const uint32_t *d_col,
+                                 uint32_t num_nodes, uint32_t source, uint64_t num_walkers, uint32_t length,
+                                 float prob, uint32_t run, uint64_t seed, uint32_t *d_counts32,
+                                 uint32_t *d_endpoints, uint32_t *d_paths, void *d_scratch, uint64_t *d_stats,
+                                 void *stream)
+{
+    return walk_device_compact(app, start_mode, d_rowptr32, d_col, num_nodes, source, num_walkers, length, prob, run,
+                               seed, d_counts32, d_endpoints, d_paths, d_scratch, d_stats, (cudaStream_t)stream, 0);
+}
+
+lt_status lt_rowptr_narrow(const uint64_t *d_rowptr, uint32_t *d_rowptr32, uint32_t num_nodes, void *stream)
+{
+    return rowptr_narrow(d_rowptr, d_rowptr32, num_nodes, (cudaStream_t)stream);
+}
+
 }  // extern "C"

@@ -41,16 +41,44 @@ constexpr size_t kScratchBytes = 256;
 
 size_t walk_scratch_bytes() { return kScratchBytes; }
 
-lt_status walk_device(int app, int start, const uint64_t *d_rowptr, const uint32_t *d_col, uint32_t V,
-                      uint32_t source, uint64_t W, uint32_t length, float prob, uint32_t run, uint64_t seed,
-                      uint64_t *d_counts, uint32_t *d_endpoints, uint32_t *d_paths, void *d_scratch,
-                      uint64_t *d_stats, cudaStream_t st, int ctas_per_sm)
+namespace {
+
+__global__ void narrow_kernel(uint32_t *dst, const uint64_t *src, uint64_t n)
 {
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) dst[i] = (uint32_t)src[i];
+}
+
+__global__ void widen_kernel(uint64_t *dst, const uint32_t *src, uint64_t n)
+{
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) dst[i] = src[i];
+}
+
+unsigned stream_blocks(uint64_t n, int sms) { return (unsigned)std::min<uint64_t>((n + 255) / 256, (uint64_t)sms * 8); }
+
+// Counter updates of one launch: one per walk (PPR), one per step (PageRank).
+uint64_t count_updates(int app, uint64_t W, uint32_t length)
+{
+    if (app == kPPR) return W;
+    if (app == kPageRank) return length && W > UINT64_MAX / length ? UINT64_MAX : W * length;
+    return 0;
+}
+
+// One launch of the resident step kernel, standard (u64 row offsets and
+// counters) or compact (u32, when d_rowptr32 is given).
+lt_status walk_launch(int app, int start, const uint64_t *d_rowptr, const uint32_t *d_rowptr32, const uint32_t *d_col,
+                      uint32_t V, uint32_t source, uint64_t W, uint32_t length, float prob, uint32_t run,
+                      uint64_t seed, uint64_t *d_counts, uint32_t *d_counts32, uint32_t *d_endpoints,
+                      uint32_t *d_paths, void *d_scratch, uint64_t *d_stats, cudaStream_t st, int ctas_per_sm)
+{
+    const bool compact = d_rowptr32 != nullptr;
     if (app < kPPR || app > kWalk) return fail(LT_ERR_INVALID, "unknown app %d", app);
     if (start < kStartSource || start > kStartPerVertex) return fail(LT_ERR_INVALID, "unknown start mode %d", start);
-    if (!d_rowptr || !d_col || V == 0) return fail(LT_ERR_INVALID, "empty graph");
+    if ((!compact && !d_rowptr) || !d_col || V == 0) return fail(LT_ERR_INVALID, "empty graph");
     if (!d_scratch) return fail(LT_ERR_INVALID, "scratch buffer is required");
-    if (app != kWalk && !d_counts) return fail(LT_ERR_INVALID, "counts buffer is required for PPR and PageRank");
+    if (app != kWalk && !(compact ? (void *)d_counts32 : (void *)d_counts))
+        return fail(LT_ERR_INVALID, "counts buffer is required for PPR and PageRank");
     if (app == kPPR && !(prob > 0.0f && prob <= 1.0f)) return fail(LT_ERR_INVALID, "PPR stop probability must be in (0, 1]");
     if (app != kPPR && length == 0) return fail(LT_ERR_INVALID, "walk length must be positive");
     if (start == kStartSource && source >= V) return fail(LT_ERR_INVALID, "source %u out of range (V=%u)", source, V);
@@ -61,6 +89,8 @@ lt_status walk_device(int app, int start, const uint64_t *d_rowptr, const uint32
     LT_CUDA_TRY(cudaGetDevice(&device));
     WholeArgs a{};
     a.rowptr = d_rowptr;
+    a.rowptr32 = d_rowptr32;
+    a.counts32 = d_counts32;
     a.col = d_col;
     a.V = V;
     a.source = source;
@@ -75,8 +105,44 @@ lt_status walk_device(int app, int start, const uint64_t *d_rowptr, const uint32
     a.next = (uint64_t *)d_scratch;
     a.stats = d_stats;
     LT_CUDA_TRY(cudaMemsetAsync(d_scratch, 0, kScratchBytes, st));
-    const int grid = whole_grid(app, start, device, ctas_per_sm);
-    LT_CUDA_TRY(launch_walk_whole(a, app, start, grid, st));
+    const int grid = whole_grid(app, start, device, ctas_per_sm, compact);
+    LT_CUDA_TRY(launch_walk_whole(a, app, start, grid, st, compact));
+    return LT_OK;
+}
+
+}  // namespace
+
+lt_status walk_device(int app, int start, const uint64_t *d_rowptr, const uint32_t *d_col, uint32_t V,
+                      uint32_t source, uint64_t W, uint32_t length, float prob, uint32_t run, uint64_t seed,
+                      uint64_t *d_counts, uint32_t *d_endpoints, uint32_t *d_paths, void *d_scratch,
+                      uint64_t *d_stats, cudaStream_t st, int ctas_per_sm)
+{
+    return walk_launch(app, start, d_rowptr, nullptr, d_col, V, source, W, length, prob, run, seed, d_counts, nullptr,
+                       d_endpoints, d_paths, d_scratch, d_stats, st, ctas_per_sm);
+}
+
+lt_status walk_device_compact(int app, int start, const uint32_t *d_rowptr32, const uint32_t *d_col, uint32_t V,
+                              uint32_t source, uint64_t W, uint32_t length, float prob, uint32_t run, uint64_t seed,
+                              uint32_t *d_counts32, uint32_t *d_endpoints, uint32_t *d_paths, void *d_scratch,
+                              uint64_t *d_stats, cudaStream_t st, int ctas_per_sm)
+{
+    if (!d_rowptr32) return fail(LT_ERR_INVALID, "empty graph");
+    if (count_updates(app, W, length) >= (1ull << 32))
+        return fail(LT_ERR_INVALID, "%s updates of %llu walkers overflow u32 counters: use lt_walk_device",
+                    app == kPPR ? "PPR" : "PageRank", (unsigned long long)W);
+    return walk_launch(app, start, nullptr, d_rowptr32, d_col, V, source, W, length, prob, run, seed, nullptr,
+                       d_counts32, d_endpoints, d_paths, d_scratch, d_stats, st, ctas_per_sm);
+}
+
+lt_status rowptr_narrow(const uint64_t *d_rowptr, uint32_t *d_rowptr32, uint32_t V, cudaStream_t st)
+{
+    if (!d_rowptr || !d_rowptr32) return fail(LT_ERR_INVALID, "null buffer");
+    int device = 0, sms = 0;
+    LT_CUDA_TRY(cudaGetDevice(&device));
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+    const uint64_t n = (uint64_t)V + 1;
+    narrow_kernel<<<stream_blocks(n, sms), 256, 0, st>>>(d_rowptr32, d_rowptr, n);
+    LT_CUDA_TRY(cudaGetLastError());
     return LT_OK;
 }
 
@@ -115,6 +181,14 @@ lt_status engine_create(lt_graph *g, const lt_engine_cfg &cfg, lt_engine **out)
         cudaGetLastError();
         return bail(fail(LT_ERR_NOMEM, "device allocation for the resident graph failed"));
     }
+    // compact layout of the resident graph: u32 row offsets and counters
+    if (e->resident && g->E < (1ull << 32)) {
+        if (cudaMalloc(&e->d_rowptr32, 4ull * ((uint64_t)g->V + 1)) != cudaSuccess ||
+            cudaMalloc(&e->d_counts32, 4ull * g->V) != cudaSuccess) {
+            cudaGetLastError();
+            return bail(fail(LT_ERR_NOMEM, "device allocation for the compact row offsets failed"));
+        }
+    }
     if (!e->resident) {
         lt_status s = ooc_create(e, &e->ooc);
         if (s != LT_OK) return bail(s);
@@ -131,7 +205,7 @@ void engine_destroy(lt_engine *e)
     if (e->ooc) ooc_destroy(e->ooc);
     if (e->batch) batch_destroy(e->batch);
     for (void *p : {(void *)e->d_rowptr, (void *)e->d_col, (void *)e->d_counts, e->d_scratch, (void *)e->d_stats,
-                    (void *)e->d_endpoints, (void *)e->d_paths})
+                    (void *)e->d_endpoints, (void *)e->d_paths, (void *)e->d_rowptr32, (void *)e->d_counts32})
         if (p) cudaFree(p);
     if (e->ev_k0) cudaEventDestroy(e->ev_k0);
     if (e->ev_k1) cudaEventDestroy(e->ev_k1);
@@ -172,6 +246,7 @@ lt_status load_all(lt_engine *e)
         e->stats.partition_loads++;
         e->stats.graph_loading_calls++;
     }
+    if (e->d_rowptr32) LT_TRY(rowptr_narrow(e->d_rowptr, e->d_rowptr32, g.V, e->s_copy));
     LT_CUDA_TRY(cudaEventRecord(b, e->s_copy));
     LT_CUDA_TRY(cudaEventSynchronize(b));
     float ms = 0;
@@ -205,17 +280,33 @@ lt_status engine_run(lt_engine *e, int app, int start, uint32_t source, uint64_t
     const double t0 = now_ms();
     LT_TRY(load_all(e));
     cudaStream_t st = e->s_compute;
-    if (app != kWalk) LT_CUDA_TRY(cudaMemsetAsync(e->d_counts, 0, 8ull * g.V, st));
+    // compact layout while every counter total of the call fits 32 bits
+    const uint64_t upd = count_updates(app, W, length);
+    const bool compact = e->d_rowptr32 && (upd == 0 || upd <= (((1ull << 32) - 1) / runs));
+    if (app != kWalk) {
+        if (compact)
+            LT_CUDA_TRY(cudaMemsetAsync(e->d_counts32, 0, 4ull * g.V, st));
+        else
+            LT_CUDA_TRY(cudaMemsetAsync(e->d_counts, 0, 8ull * g.V, st));
+    }
     LT_CUDA_TRY(cudaMemsetAsync(e->d_stats, 0, 64, st));
     if (endpoints_out) LT_TRY(grow((void **)&e->d_endpoints, e->endpoints_cap, 4 * W));
     if (paths_out) LT_TRY(grow((void **)&e->d_paths, e->paths_cap, 4 * W * ((uint64_t)length + 1)));
     LT_CUDA_TRY(cudaEventRecord(e->ev_k0, st));
     for (uint32_t r = 0; r < runs; r++) {
-        LT_TRY(walk_device(app, start, e->d_rowptr, e->d_col, g.V, source, W, length, prob, run_base + r,
-                           e->cfg.seed, app != kWalk ? e->d_counts : nullptr, endpoints_out ? e->d_endpoints : nullptr,
-                           paths_out ? e->d_paths : nullptr, e->d_scratch, e->d_stats, st, e->cfg.ctas_per_sm));
+        const bool cnt = app != kWalk;
+        LT_TRY(walk_launch(app, start, compact ? nullptr : e->d_rowptr, compact ? e->d_rowptr32 : nullptr, e->d_col,
+                           g.V, source, W, length, prob, run_base + r, e->cfg.seed,
+                           cnt && !compact ? e->d_counts : nullptr, cnt && compact ? e->d_counts32 : nullptr,
+                           endpoints_out ? e->d_endpoints : nullptr, paths_out ? e->d_paths : nullptr, e->d_scratch,
+                           e->d_stats, st, e->cfg.ctas_per_sm));
         e->stats.kernel_launches++;
         e->stats.computing_calls++;
+    }
+    if (compact && app != kWalk) {
+        widen_kernel<<<stream_blocks(g.V, e->sms), 256, 0, st>>>(e->d_counts, e->d_counts32, g.V);
+        LT_CUDA_TRY(cudaGetLastError());
+        e->stats.kernel_launches++;
     }
     LT_CUDA_TRY(cudaEventRecord(e->ev_k1, st));
     if (counts_out) LT_CUDA_TRY(cudaMemcpyAsync(counts_out, e->d_counts, 8ull * g.V, cudaMemcpyDeviceToHost, st));

@@ -29,6 +29,10 @@ struct lt_engine {
     uint64_t *d_rowptr = nullptr;
     uint32_t *d_col = nullptr;
     bool loaded = false;
+    // compact layout (E < 2^32): u32 row offsets, and u32 counters for calls
+    // whose counter updates stay below 2^32, widened to d_counts at the end
+    uint32_t *d_rowptr32 = nullptr;
+    uint32_t *d_counts32 = nullptr;
 
     uint64_t *d_counts = nullptr;  // u64[V]
     void *d_scratch = nullptr;     // lt_walk_scratch_bytes()
@@ -58,4 +62,9 @@ lt_status walk_device(int app, int start, const uint64_t *d_rowptr, const uint32
                       uint64_t *d_counts, uint32_t *d_endpoints, uint32_t *d_paths, void *d_scratch,
                       uint64_t *d_stats, cudaStream_t st, int block_ctas);
 size_t walk_scratch_bytes();
+lt_status walk_device_compact(int app, int start, const uint32_t *d_rowptr32, const uint32_t *d_col, uint32_t V,
+                              uint32_t source, uint64_t W, uint32_t length, float prob, uint32_t run, uint64_t seed,
+                              uint32_t *d_counts32, uint32_t *d_endpoints, uint32_t *d_paths, void *d_scratch,
+                              uint64_t *d_stats, cudaStream_t st, int ctas_per_sm);
+lt_status rowptr_narrow(const uint64_t *d_rowptr, uint32_t *d_rowptr32, uint32_t V, cudaStream_t st);
 }  // namespace lt

@@ -35,6 +35,13 @@ __device__ __forceinline__ uint64_t ld_nc_u64(const void *a, uint64_t pol)
     return v;
 }
 
+__device__ __forceinline__ uint32_t ld_nc_u32(const void *a, uint64_t pol)
+{
+    uint32_t v;
+    asm volatile("ld.global.nc.L2::cache_hint.u32 %0, [%1], %2;" : "=r"(v) : "l"(a), "l"(pol));
+    return v;
+}
+
 // Read-only streaming load: not kept in L1, L2 policy as given.
 __device__ __forceinline__ uint32_t ld_nc_stream_u32(const void *a, uint64_t pol)
 {
@@ -47,6 +54,12 @@ __device__ __forceinline__ uint32_t ld_nc_stream_u32(const void *a, uint64_t pol
 __device__ __forceinline__ void red_add1_u64(unsigned long long *a, uint64_t pol)
 {
     asm volatile("red.global.add.L2::cache_hint.u64 [%0], 1, %1;" ::"l"(a), "l"(pol) : "memory");
+}
+
+// counts[i] += 1 on a u32 counter, with an L2 policy.
+__device__ __forceinline__ void red_add1_u32(unsigned int *a, uint64_t pol)
+{
+    asm volatile("red.global.add.L2::cache_hint.u32 [%0], 1, %1;" ::"l"(a), "l"(pol) : "memory");
 }
 
 }  // namespace lt

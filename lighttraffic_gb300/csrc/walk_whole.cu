@@ -29,11 +29,33 @@ constexpr unsigned kFull = 0xFFFFFFFFu;
 struct Hints {
     uint64_t keep, stream;
 };
-__device__ __forceinline__ uint64_t ldg_u64(const uint64_t *p, const Hints &h) { return ld_nc_u64(p, h.keep); }
 __device__ __forceinline__ uint32_t ldg_u32(const uint32_t *p, const Hints &h) { return ld_nc_stream_u32(p, h.stream); }
-__device__ __forceinline__ void count1(uint64_t *c, const Hints &h) { red_add1_u64((unsigned long long *)c, h.keep); }
 
-template <int APP, int START>
+// first edge and degree of v
+template <bool C>
+__device__ __forceinline__ void row_range(const WholeArgs &a, uint32_t v, const Hints &h, uint64_t &first,
+                                          uint64_t &deg)
+{
+    if (C) {
+        const uint32_t f = ld_nc_u32(a.rowptr32 + v, h.keep);
+        first = f;
+        deg = ld_nc_u32(a.rowptr32 + v + 1, h.keep) - f;
+    } else {
+        first = ld_nc_u64(a.rowptr + v, h.keep);
+        deg = ld_nc_u64(a.rowptr + v + 1, h.keep) - first;
+    }
+}
+
+template <bool C>
+__device__ __forceinline__ void count1(const WholeArgs &a, uint32_t v, const Hints &h)
+{
+    if (C)
+        red_add1_u32(a.counts32 + v, h.keep);
+    else
+        red_add1_u64((unsigned long long *)(a.counts + v), h.keep);
+}
+
+template <int APP, int START, bool C>
 __global__ void __launch_bounds__(kWholeBlock) walk_whole_kernel(WholeArgs a)
 {
     const int lane = threadIdx.x & 31;
@@ -82,24 +104,24 @@ __global__ void __launch_bounds__(kWholeBlock) walk_whole_kernel(WholeArgs a)
         if (APP == kPPR) {
             // app/ppr.cu:22-42
             if (s == 1) {
-                count1(&a.counts[cur], h);
+                count1<C>(a, cur, h);
                 active = false;
             } else {
                 step = s - 1;
-                const uint64_t first = ldg_u64(a.rowptr + cur, h);
-                const uint64_t deg = ldg_u64(a.rowptr + cur + 1, h) - first;
+                uint64_t first, deg;
+                row_range<C>(a, cur, h, first, deg);
                 if (deg > 0) {
                     const Rand4 r = walk_draw(a.seed, s, kTagStep, a.run, idx);
                     cur = ldg_u32(a.col + first + mod_u64(r64_of(r), deg), h);
                     n_mov++;
                 } else {
-                    count1(&a.counts[cur], h);
+                    count1<C>(a, cur, h);
                     active = false;
                 }
             }
         } else if (APP == kPageRank) {
             // app/pagerank.cu:26-44; a vertex without out-edges teleports.
-            count1(&a.counts[cur], h);
+            count1<C>(a, cur, h);
             if (s == 1) {
                 active = false;
             } else {
@@ -108,8 +130,8 @@ __global__ void __launch_bounds__(kWholeBlock) walk_whole_kernel(WholeArgs a)
                 const uint64_t r64 = r64_of(r);
                 bool tele = m53_of(r) >= a.thr;
                 if (!tele) {
-                    const uint64_t first = ldg_u64(a.rowptr + cur, h);
-                    const uint64_t deg = ldg_u64(a.rowptr + cur + 1, h) - first;
+                    uint64_t first, deg;
+                    row_range<C>(a, cur, h, first, deg);
                     if (deg > 0) {
                         cur = ldg_u32(a.col + first + mod_u64(r64, deg), h);
                         n_mov++;
@@ -124,8 +146,8 @@ __global__ void __launch_bounds__(kWholeBlock) walk_whole_kernel(WholeArgs a)
             }
         } else {
             // app/genericwalk.cu:22-32
-            const uint64_t first = ldg_u64(a.rowptr + cur, h);
-            const uint64_t deg = ldg_u64(a.rowptr + cur + 1, h) - first;
+            uint64_t first, deg;
+            row_range<C>(a, cur, h, first, deg);
             uint32_t *path = a.paths ? a.paths + idx * (uint64_t)(a.length + 1) : nullptr;
             if (deg > 0) {
                 const Rand4 r = walk_draw(a.seed, s, kTagStep, a.run, idx);
@@ -159,60 +181,72 @@ __global__ void __launch_bounds__(kWholeBlock) walk_whole_kernel(WholeArgs a)
     }
 }
 
-template <int APP, int START>
+template <int APP, int START, bool C>
 cudaError_t launch_t(const WholeArgs &a, int grid, cudaStream_t st)
 {
-    walk_whole_kernel<APP, START><<<grid, kWholeBlock, 0, st>>>(a);
+    walk_whole_kernel<APP, START, C><<<grid, kWholeBlock, 0, st>>>(a);
     return cudaGetLastError();
 }
 
-template <int APP>
+template <int APP, bool C>
 cudaError_t launch_app(const WholeArgs &a, int start, int grid, cudaStream_t st)
 {
     switch (start) {
-    case kStartSource: return launch_t<APP, kStartSource>(a, grid, st);
-    case kStartUniform: return launch_t<APP, kStartUniform>(a, grid, st);
-    default: return launch_t<APP, kStartPerVertex>(a, grid, st);
+    case kStartSource: return launch_t<APP, kStartSource, C>(a, grid, st);
+    case kStartUniform: return launch_t<APP, kStartUniform, C>(a, grid, st);
+    default: return launch_t<APP, kStartPerVertex, C>(a, grid, st);
     }
 }
 
-template <int APP, int START>
+template <int APP, int START, bool C>
 int occupancy_t()
 {
     int n = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, walk_whole_kernel<APP, START>, kWholeBlock, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, walk_whole_kernel<APP, START, C>, kWholeBlock, 0);
     return n;
+}
+
+template <bool C>
+int occupancy_c(int app, int start)
+{
+    switch (app * 3 + start) {
+    case 0: return occupancy_t<kPPR, kStartSource, C>();
+    case 1: return occupancy_t<kPPR, kStartUniform, C>();
+    case 2: return occupancy_t<kPPR, kStartPerVertex, C>();
+    case 3: return occupancy_t<kPageRank, kStartSource, C>();
+    case 4: return occupancy_t<kPageRank, kStartUniform, C>();
+    case 5: return occupancy_t<kPageRank, kStartPerVertex, C>();
+    case 6: return occupancy_t<kWalk, kStartSource, C>();
+    case 7: return occupancy_t<kWalk, kStartUniform, C>();
+    default: return occupancy_t<kWalk, kStartPerVertex, C>();
+    }
 }
 
 }  // namespace
 
-int whole_grid(int app, int start, int device, int ctas_per_sm)
+int whole_grid(int app, int start, int device, int ctas_per_sm, bool compact)
 {
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
-    int occ = 0;
-    switch (app * 3 + start) {
-    case 0: occ = occupancy_t<kPPR, kStartSource>(); break;
-    case 1: occ = occupancy_t<kPPR, kStartUniform>(); break;
-    case 2: occ = occupancy_t<kPPR, kStartPerVertex>(); break;
-    case 3: occ = occupancy_t<kPageRank, kStartSource>(); break;
-    case 4: occ = occupancy_t<kPageRank, kStartUniform>(); break;
-    case 5: occ = occupancy_t<kPageRank, kStartPerVertex>(); break;
-    case 6: occ = occupancy_t<kWalk, kStartSource>(); break;
-    case 7: occ = occupancy_t<kWalk, kStartUniform>(); break;
-    default: occ = occupancy_t<kWalk, kStartPerVertex>(); break;
-    }
+    int occ = compact ? occupancy_c<true>(app, start) : occupancy_c<false>(app, start);
     if (occ < 1) occ = 1;
     if (ctas_per_sm > 0 && ctas_per_sm < occ) occ = ctas_per_sm;
     return sms * occ;
 }
 
-cudaError_t launch_walk_whole(const WholeArgs &a, int app, int start, int grid, cudaStream_t st)
+cudaError_t launch_walk_whole(const WholeArgs &a, int app, int start, int grid, cudaStream_t st, bool compact)
 {
+    if (compact) {
+        switch (app) {
+        case kPPR: return launch_app<kPPR, true>(a, start, grid, st);
+        case kPageRank: return launch_app<kPageRank, true>(a, start, grid, st);
+        default: return launch_app<kWalk, true>(a, start, grid, st);
+        }
+    }
     switch (app) {
-    case kPPR: return launch_app<kPPR>(a, start, grid, st);
-    case kPageRank: return launch_app<kPageRank>(a, start, grid, st);
-    default: return launch_app<kWalk>(a, start, grid, st);
+    case kPPR: return launch_app<kPPR, false>(a, start, grid, st);
+    case kPageRank: return launch_app<kPageRank, false>(a, start, grid, st);
+    default: return launch_app<kWalk, false>(a, start, grid, st);
     }
 }
 

@@ -23,10 +23,16 @@ struct WholeArgs {
     uint32_t *paths;         // u32[W*(length+1)] or null (walk app)
     uint64_t *next;          // scratch: next walker index (zeroed before launch)
     uint64_t *stats;         // u64[3] or null: updates, moves, teleports
+    // Compact layout (launch with compact = true): u32 row offsets (E < 2^32)
+    // and u32 counters (fewer than 2^32 counter updates in the launch)
+    // replace rowptr and counts.  Half the bytes for the two arrays every
+    // update reuses, so that they stay in L2 against the column stream.
+    const uint32_t *rowptr32;
+    uint32_t *counts32;
 };
 
 // Persistent grid size: SMs x resident CTAs (capped by ctas_per_sm when > 0).
-int whole_grid(int app, int start, int device, int ctas_per_sm);
-cudaError_t launch_walk_whole(const WholeArgs &a, int app, int start, int grid, cudaStream_t st);
+int whole_grid(int app, int start, int device, int ctas_per_sm, bool compact = false);
+cudaError_t launch_walk_whole(const WholeArgs &a, int app, int start, int grid, cudaStream_t st, bool compact = false);
 
 }  // namespace lt

@@ -55,3 +55,15 @@ def test_cli_requires_file(lt):
     assert r.returncode == 2 and "-f option must be given" in r.stderr
     r = subprocess.run([exe, "-f", "/nonexistent.bcsr", "-m"], capture_output=True, text=True)
     assert r.returncode == 1 and "cannot open" in r.stderr
+
+
+def test_compact_rejects_counter_overflow(lt):
+    """u32 counters: a call whose updates reach 2^32 is refused before any
+    device work (W * length for PageRank, W for PPR)."""
+    fake = ctypes.c_void_p(0x1000)
+    rc = lt.lib.lt_walk_device_compact(1, 1, fake, fake, 10, 0, 1 << 29, 8, ctypes.c_float(0.85), 0, 1, fake,
+                                       None, None, fake, None, None)
+    assert rc == 1 and b"overflow u32" in lt.lib.lt_last_error()
+    rc = lt.lib.lt_walk_device_compact(0, 0, fake, fake, 10, 0, 1 << 32, 0, ctypes.c_float(0.15), 0, 1, fake,
+                                       None, None, fake, None, None)
+    assert rc == 1 and b"overflow u32" in lt.lib.lt_last_error()

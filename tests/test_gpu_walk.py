@@ -161,3 +161,45 @@ def test_device_entry_point(lt, require_gpu, rmat16):
         torch.cuda.synchronize()
         want, _, _ = oracle.ppr(rp, col, 3, 50000, prob=0.15, seed=99)
         assert (d_cnt.cpu().numpy().view(np.uint64) == want).all()
+
+
+@pytest.mark.parametrize("app,start,length", [(0, 0, 0), (1, 1, 7), (1, 2, 10), (2, 1, 6)])
+def test_compact_entry_point(lt, require_gpu, rmat16, app, start, length):
+    """lt_walk_device_compact (u32 row offsets from lt_rowptr_narrow, u32
+    counters) gives the oracle's counts, endpoints and paths bit for bit."""
+    import ctypes
+    import torch
+    rp, col = rmat16
+    V = len(rp) - 1
+    W = 2 * V + 13
+    d_rp = torch.from_numpy(rp.view(np.int64)).cuda()
+    d_rp32 = torch.zeros(V + 1, dtype=torch.int32, device="cuda")
+    d_col = torch.from_numpy(col.view(np.int32)).cuda()
+    d_cnt = torch.zeros(V, dtype=torch.int32, device="cuda")
+    d_ep = torch.zeros(W, dtype=torch.int32, device="cuda")
+    d_pa = torch.zeros(W * (length + 1) if app == 2 else 1, dtype=torch.int32, device="cuda")
+    d_scr = torch.zeros(lt.lib.lt_walk_scratch_bytes() // 8, dtype=torch.int64, device="cuda")
+    d_st = torch.zeros(3, dtype=torch.int64, device="cuda")
+    s = torch.cuda.current_stream().cuda_stream
+    lt.check(lt.lib.lt_rowptr_narrow(d_rp.data_ptr(), d_rp32.data_ptr(), V, s))
+    for rep in range(2):
+        d_cnt.zero_()
+        d_st.zero_()
+        lt.check(lt.lib.lt_walk_device_compact(app, start, d_rp32.data_ptr(), d_col.data_ptr(), V, 5, W, length,
+                                               ctypes.c_float(0.15 if app == 0 else 0.85), 3, 77,
+                                               d_cnt.data_ptr() if app != 2 else None, d_ep.data_ptr(),
+                                               d_pa.data_ptr() if app == 2 else None, d_scr.data_ptr(),
+                                               d_st.data_ptr(), s))
+        torch.cuda.synchronize()
+        ep = d_ep.cpu().numpy().view(np.uint32)
+        if app != 2:
+            want, wep, _, st = oracle.walk_batch(app, rp, col, start_mode=start, source=5, walkers=W, length=length,
+                                                 prob=0.15 if app == 0 else 0.85, run=3, seed=77, endpoints=True)
+            assert (d_cnt.cpu().numpy().view(np.uint32).astype(np.uint64) == want).all()
+            assert (ep == wep).all()
+            assert tuple(int(x) for x in d_st.cpu().numpy()) == tuple(int(x) for x in st)
+        else:
+            wep, wpa, _ = oracle.generic_walk(rp, col, W, length=length, start_mode=start, run=3, seed=77,
+                                              paths=True)
+            assert (ep == wep).all()
+            assert (d_pa.cpu().numpy().view(np.uint32) == wpa.ravel()).all()
