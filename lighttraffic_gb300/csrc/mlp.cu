@@ -530,10 +530,6 @@ public:
 
     bool single_pass() const override { return false; }
     bool wave() const override { return true; }
-    // Serving keeps few walkers in flight, so reading cold partitions zero-copy
-    // costs little and lets every admitted query finish in one step; the
-    // network then chooses which partitions hold cache slots.
-    bool serve_single_pass() const override { return true; }
 
     void stats(lt_policy_stats &st) const override
     {

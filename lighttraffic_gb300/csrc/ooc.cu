@@ -871,17 +871,29 @@ constexpr uint64_t kZcGroupBytes = 128ull << 20;  // zero-copy group: host bytes
 // load and no walker can be created, every partition outside the cache is
 // read zero-copy in one kernel (the final phase).  Results are those of the
 // reference loop: every draw is keyed by walker and step.
-lt_status wave_run(Ooc &o, const RunParams &rp)
+struct WaveState {
+    explicit WaveState(uint32_t P) : draining(P, 0), loading(P, 0) {}
+    std::vector<std::pair<uint32_t, cudaEvent_t>> inflight;  // loads started, entries not yet published
+    std::vector<uint32_t> parts, cand, idle;
+    std::vector<char> draining, loading;
+    int stalls = 0;
+};
+
+// One wave iteration (see wave_run); done = nothing waits and nothing loads.
+lt_status wave_step(Ooc &o, const RunParams &rp, WaveState &w, bool &done)
 {
     lt_engine &e = *o.e;
     const bool zc_ok = o.zc_rp_base != 0 && o.P <= kSmemPartMax && o.zc_threshold > 0;
     const uint64_t load_min = zc_ok ? o.zc_threshold : 1;
     const uint64_t reserve = (uint64_t)o.P + 2;
-    std::vector<std::pair<uint32_t, cudaEvent_t>> inflight;
-    std::vector<uint32_t> parts, cand, idle;
-    std::vector<char> draining(o.P, 0), loading(o.P, 0);
-    int stalls = 0;
-    while (true) {
+    auto &inflight = w.inflight;
+    auto &parts = w.parts;
+    auto &cand = w.cand;
+    auto &idle = w.idle;
+    auto &draining = w.draining;
+    auto &loading = w.loading;
+    done = false;
+    {
         for (auto &d : inflight) {
             LT_CUDA_TRY(cudaStreamWaitEvent(e.s_compute, d.second, 0));
             LT_TRY(set_entry(o, d.first, e.s_compute));
@@ -891,7 +903,10 @@ lt_status wave_run(Ooc &o, const RunParams &rp)
         refresh_all(o);
         bool any = false;
         for (uint32_t p = 0; p < o.P && !any; p++) any = o.waiting[p] > 0;
-        if (!any) break;
+        if (!any) {
+            done = true;
+            return LT_OK;
+        }
         o.iteration++;
         e.stats.iterations++;
 
@@ -1020,18 +1035,26 @@ lt_status wave_run(Ooc &o, const RunParams &rp)
             // while the cached partitions wait for spilled or uncreated ones.
             // Spill to make room, then try again.
             o.zc_mask_any = false;
-            if (++stalls > 2)
+            if (++w.stalls > 2)
                 return fail(LT_ERR_CAPACITY, "wave scheduler cannot make progress (walker pool or cache too small)");
             LT_TRY(spill_until(o, std::min<uint64_t>(o.n_chunks, reserve + 64), -1));
-            continue;
+            return LT_OK;
         }
-        stalls = 0;
+        w.stalls = 0;
         const Lazy lz = lazy_p >= 0 ? lazy_of(o, rp, lazy_p, o.q[lazy_p].lazy_next, G) : Lazy{};
         LT_TRY(step_and_bucket_parts(o, rp, parts, lazy_p, lz, false, nullptr));
         o.zc_mask_any = false;
         drain_timers(o, false);
         o.policy->observe(view(o));
     }
+    return LT_OK;
+}
+
+lt_status wave_run(Ooc &o, const RunParams &rp)
+{
+    WaveState w(o.P);
+    bool done = false;
+    while (!done) LT_TRY(wave_step(o, rp, w, done));
     return LT_OK;
 }
 
@@ -1286,6 +1309,7 @@ struct lt_server {
         std::vector<uint32_t> out_v, out_c;
     };
     lt_engine *e = nullptr;
+    lt::WaveState *wave = nullptr;  // wave-run policies: one wave iteration per serving step
     lt::Ooc *o = nullptr;
     uint32_t max_active = 0;
     uint64_t table_cap = 0;
@@ -1569,7 +1593,8 @@ lt_status serve_open(lt_engine *e, uint32_t max_active, uint64_t table_slots, fl
     cudaMemsetAsync(o.d_stats, 0, 64, e->s_compute);
     e->stats = lt_stats{};
     o.serve = s;
-    o.single = o.policy->serve_single_pass() && o.zc_rp_base != 0;
+    if (o.policy->wave()) s->wave = new WaveState(o.P);
+    o.single = !s->wave && o.policy->serve_single_pass() && o.zc_rp_base != 0;
     if (o.single)
         for (uint32_t p = 0; p < o.P; p++)
             if (o.slot_of[p] < 0) {
@@ -1606,7 +1631,16 @@ lt_status serve_step(lt_server *s, uint32_t *completed, uint32_t *active, uint32
     SchedView v = view(o);
     bool spilled = false;
     for (uint32_t i = 0; i < o.P && !spilled; i++) spilled = !o.q[i].host_chunks.empty();
-    if (o.single && !spilled) {
+    if (s->wave) {
+        // light load: every step is a final sweep that finishes the admitted
+        // walkers in one kernel; heavy load: waves with overlapped loads
+        RunParams rp{};
+        rp.app = kPPR;
+        rp.start = kStartSource;
+        rp.thr = s->thr;
+        bool idle = false;
+        LT_TRY(wave_step(o, rp, *s->wave, idle));
+    } else if (o.single && !spilled) {
         // every partition readable: drain all in-flight walkers in one launch
         std::vector<uint32_t> parts;
         for (uint32_t i = 0; i < o.P; i++)
@@ -1689,6 +1723,12 @@ void serve_close(lt_server *s)
             s->e->stats.zerocopy_bytes = hs[3] * 256;
             s->e->stats.handoffs = hs[4];
         }
+        if (s->wave) {
+            // loads still in flight: let them land and publish them
+            cudaStreamSynchronize(s->e->s_copy);
+            for (auto &d : s->wave->inflight) set_entry(*s->o, d.first, s->e->s_compute);
+            cudaStreamSynchronize(s->e->s_compute);
+        }
         drain_timers(*s->o, true);
         s->o->serve = nullptr;
         if (s->o->single) {
@@ -1707,6 +1747,7 @@ void serve_close(lt_server *s)
                     (void *)s->d_done, (void *)s->d_err, (void *)s->d_out_v, (void *)s->d_out_c})
         if (p) cudaFree(p);
     host_free(s->h_done);
+    delete s->wave;
     for (auto &kv : s->all) delete kv.second;
     for (lt_server::Query *q : s->pending)
         if (s->all.find(q->ticket) == s->all.end()) delete q;

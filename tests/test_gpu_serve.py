@@ -36,7 +36,7 @@ def _drain(srv, tickets, max_steps=200000):
     raise AssertionError("queries did not finish")
 
 
-@pytest.mark.parametrize("sched", [0, 2])
+@pytest.mark.parametrize("sched", [0, 2, 4])
 def test_serve_alone_and_in_mix(lt, require_gpu, graph16, sched):
     rp, col = graph16
     V = len(rp) - 1
@@ -63,6 +63,10 @@ def test_serve_alone_and_in_mix(lt, require_gpu, graph16, sched):
         assert res[t][0] == _oracle(rp, col, *spec)
     assert all(r[1] >= 0 for r in res.values())
     srv.close()
+    # the engine runs regular calls again after serving (cache state intact)
+    got = e.ppr(3, 40000, 0.15)
+    want, _, _ = oracle.ppr(rp, col, 3, 40000, prob=0.15, seed=1)
+    assert (got == want).all()
 
 
 def test_serve_admission_limits(lt, require_gpu, graph16):
