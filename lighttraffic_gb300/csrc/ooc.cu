@@ -960,6 +960,31 @@ lt_status wave_step(Ooc &o, const RunParams &rp, WaveState &w, bool &done)
             o.last_used[c] = o.iteration;
             started++;
         }
+        // Nothing worth a load but slots are free (light load, e.g. serving
+        // from a cold cache): fill them with the partitions scoring highest
+        // (policy score plus waiting walkers) -- no eviction, and the copies
+        // overlap the kernel.
+        if (cand.empty() && free_slot(o) >= 0) {
+            std::vector<std::pair<double, uint32_t>> fill;
+            for (uint32_t p = 0; p < o.P; p++) {
+                if (o.slot_of[p] >= 0 || loading[p]) continue;
+                const double sc = o.policy->cache_score(v, p) + (double)o.waiting[p];
+                if (sc > 0.0) fill.push_back({sc, p});
+            }
+            std::sort(fill.begin(), fill.end(), [](const std::pair<double, uint32_t> &a,
+                                                   const std::pair<double, uint32_t> &b) {
+                return a.first != b.first ? a.first > b.first : a.second < b.second;
+            });
+            for (const auto &f : fill) {
+                if (started >= m) break;
+                const int32_t slot = free_slot(o);
+                if (slot < 0) break;
+                LT_TRY(start_load(o, f.second, slot, &inflight));
+                loading[f.second] = 1;
+                o.last_used[f.second] = o.iteration;
+                started++;
+            }
+        }
         if (started) e.stats.explicit_iterations++;
 
         // walkers to create: into a readable partition if one has them
@@ -987,7 +1012,7 @@ lt_status wave_step(Ooc &o, const RunParams &rp, WaveState &w, bool &done)
         o.zc_mask_any = false;
         bool lazy_left = false;
         for (uint32_t p = 0; p < o.P && !lazy_left; p++) lazy_left = o.lazy_left[p] > 0;
-        if (zc_ok && cand.empty() && inflight.empty() && (G == 0 || !lazy_left)) {
+        if (zc_ok && cand.empty() && (G == 0 || !lazy_left)) {
             uint64_t outside = 0;
             std::vector<uint32_t> group;
             for (uint32_t p = 0; p < o.P; p++)
