@@ -49,6 +49,7 @@ struct BatchArgs {
     const uint32_t *n_dev;   // queries in the batch (written by the host before each launch)
     uint32_t smem_queries;   // walker offsets kept in shared memory when n <= smem_queries
     const uint64_t *rowptr;
+    const uint32_t *rowptr32;  // compact row offsets when E < 2^32 (else null)
     const uint32_t *col;
     uint32_t V;
     uint64_t thr;
@@ -243,8 +244,15 @@ __global__ void __launch_bounds__(BLOCK) batch_walk_kernel(BatchArgs a)
             done = true;
         } else {
             step = s - 1;
-            const uint64_t first = ld_nc_u64(a.rowptr + cur, keep);
-            const uint64_t deg = ld_nc_u64(a.rowptr + cur + 1, keep) - first;
+            uint64_t first, deg;
+            if (a.rowptr32) {
+                const uint32_t f = ld_nc_u32(a.rowptr32 + cur, keep);
+                first = f;
+                deg = ld_nc_u32(a.rowptr32 + cur + 1, keep) - f;
+            } else {
+                first = ld_nc_u64(a.rowptr + cur, keep);
+                deg = ld_nc_u64(a.rowptr + cur + 1, keep) - first;
+            }
             if (deg > 0) {
                 const Rand4 r = walk_draw(seed, s, kTagStep, 0, idx);
                 cur = ld_nc_stream_u32(a.col + first + mod_u64(r64_of(r), deg), stream);
@@ -435,6 +443,7 @@ BatchArgs args_of(lt_engine *e, BatchState &b, uint64_t thr)
     a.n_dev = b.d_n;
     a.smem_queries = std::min<uint32_t>(b.qcap, kSmemQueries);
     a.rowptr = e->d_rowptr;
+    a.rowptr32 = e->d_rowptr32;
     a.col = e->d_col;
     a.V = e->g->V;
     a.thr = thr;
