@@ -257,13 +257,16 @@ def reference_arm(args, cfg):
 # ------------------------------------------------------------ GB300 arm
 
 def init_dist():
+    """One process per GPU (replicas): the process group exists only for the
+    barrier around the timed region and the max over ranks of its time."""
     import torch
     ws, rank, local = dist_env()
     dist = None
     if ws > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
-    torch.cuda.set_device(local)
+    if torch.cuda.is_available():
+        torch.cuda.set_device(local)
     return ws, rank, local, dist
 
 
@@ -271,27 +274,10 @@ def max_over_ranks(dist, local, x):
     if not dist:
         return x
     import torch
-    t = torch.tensor([x], dtype=torch.float64, device=f"cuda:{local}")
+    dev = f"cuda:{local}" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
-
-
-def host_link_peak(local):
-    """Pinned host -> device copy bandwidth, best of 5 (GB/s)."""
-    import torch
-    n = 1 << 30
-    src = torch.empty(n, dtype=torch.uint8, pin_memory=True)
-    dst = torch.empty(n, dtype=torch.uint8, device=f"cuda:{local}")
-    best = 0.0
-    for _ in range(5):
-        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        a.record()
-        dst.copy_(src, non_blocking=True)
-        b.record()
-        torch.cuda.synchronize()
-        best = max(best, n / (a.elapsed_time(b) / 1e3) / 1e9)
-    del src, dst
-    return best
 
 
 def link_bytes(s):
