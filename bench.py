@@ -372,8 +372,13 @@ def gb300_ooc(args, cfg):
                      "alg_bytes_per_launch": alg / max(1, launches),
                      "mean_launch_ms": s["step_kernel_ms"] / max(1, launches), "launches": launches,
                      "peak_source": peak_src},
-        "host_link": {"bytes_per_step": link_bytes(s) / s["moves"], "achieved_gbs": link_bytes(s) / (L["elapsed"] / args.steps) / 1e9,
-                      "peak_gbs": link_peak, "peak_source": "measured pinned H2D copy in this run",
+        # the resource that bounds an out-of-core run: host-link bytes (graph
+        # loads, modelled zero-copy lines, walker spills) over the run time,
+        # against the measured pinned H2D bandwidth
+        "host_link": {"bytes_per_step": link_bytes(s) / s["moves"],
+                      "achieved_gbs": link_bytes(s) / (L["elapsed"] / args.steps) / 1e9,
+                      "peak_gbs": link_peak, "frac": link_bytes(s) / (L["elapsed"] / args.steps) / 1e9 / link_peak,
+                      "peak_source": "measured pinned H2D copy in this run",
                       "zerocopy_bytes_model": "256 B per zero-copy hop (two 128 B host lines)"},
         "plain": {"value": plain_value, "bytes_per_step": link_bytes(Pn["stats"]) / Pn["steps"],
                   "iterations": Pn["stats"]["iterations"], "partition_loads": Pn["stats"]["partition_loads"],
