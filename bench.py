@@ -19,8 +19,11 @@ vertices removed, stand in for the reference's datasets, which are absent):
       16 of its 32 MiB partitions cached, walker pool 2^22.
   c1: walk-based PageRank on RMAT(2^23, 2^27) resident in HBM (32 MiB
       partitions all cached), 2|V| walkers one per vertex, l = 10, teleport
-      when U > 0.85; `value` times lt_walk_device passes on device buffers,
-      `e2e` the public API with the graph re-copied from pinned host memory.
+      when U > 0.85; `value` times lt_walk_device_compact passes (u32 row
+      offsets and counters, the layout the engine uses while E and a call's
+      counter updates fit 32 bits) on device buffers, with lt_walk_device
+      (u64 layout) timed beside it under "u64_layout"; `e2e` is the public
+      API with the graph re-copied from pinned host memory.
   c0: PPR on RMAT(2^20, 2^24) resident in HBM, source 0, W = 2|V|.
   c3: batched multi-source PPR on RMAT(2^26, 2^30) resident in HBM: 4096
       sources drawn Zipf(s = 1.1) over the out-degree rank, walks per source
