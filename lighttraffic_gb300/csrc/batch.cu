@@ -62,7 +62,9 @@ struct BatchArgs {
     uint32_t *tlog;      // n: log2 table capacity
     uint32_t *keys;      // T
     uint32_t *cnt;       // T
-    uint32_t *qcount;    // n: occupied slots per query
+    uint32_t *ccount;    // occupied slots per compaction chunk (nch)
+    uint64_t *cbase;     // nch+1: exclusive scan of ccount
+    uint64_t nch;        // compaction chunks of the table arena
     uint64_t *qout;      // n+1: output offsets
     uint32_t *out_v;
     uint32_t *out_c;
@@ -288,36 +290,35 @@ __device__ unsigned block_count(unsigned v, unsigned *sh)
     return t;
 }
 
-// One CTA per query (grid-stride over queries): occupied slots.
-__global__ void __launch_bounds__(kRowThreads) count_kernel(BatchArgs a, uint32_t qcap)
+// Compaction in fixed chunks of the table arena, so that one large table
+// (a Zipf-heavy query) is spread over many CTAs: count the occupied slots of
+// every chunk, scan the counts, then every CTA writes its chunk's pairs in
+// slot order; a query's output offset is the chunk base of its first slot
+// plus the occupied slots between that chunk's start and the table.
+constexpr uint64_t kCompactChunk = 4096;
+
+__global__ void __launch_bounds__(kRowThreads) chunk_count_kernel(BatchArgs a)
 {
     __shared__ unsigned sh[kRowThreads / 32];
-    const uint32_t n = (uint32_t)a.hdr->n;
-    for (uint32_t q = blockIdx.x; q < qcap; q += gridDim.x) {
-        if (q >= n) {
-            if (threadIdx.x == 0) a.qcount[q] = 0;
-            continue;
-        }
-        const uint64_t b = a.toff[q], e = a.toff[q + 1];
-        unsigned c = 0;
-        for (uint64_t i = b + threadIdx.x; i < e; i += kRowThreads) c += a.keys[i] != kEmpty;
-        const unsigned t = block_count(c, sh);
-        if (threadIdx.x == 0) a.qcount[q] = t;
+    const uint64_t T = a.toff[(uint32_t)a.hdr->n];
+    for (uint64_t c = blockIdx.x; c < a.nch; c += gridDim.x) {
+        const uint64_t b = c * kCompactChunk, e = b + kCompactChunk < T ? b + kCompactChunk : T;
+        unsigned cnt = 0;
+        for (uint64_t i = b + threadIdx.x; i < e; i += kRowThreads) cnt += a.keys[i] != kEmpty;
+        const unsigned t = block_count(cnt, sh);
+        if (threadIdx.x == 0) a.ccount[c] = t;
         __syncthreads();
     }
 }
 
-// One CTA per query: pairs in slot order.
-__global__ void __launch_bounds__(kRowThreads) compact_kernel(BatchArgs a)
+__global__ void __launch_bounds__(kRowThreads) chunk_compact_kernel(BatchArgs a)
 {
     __shared__ unsigned sh[kRowThreads / 32];
-    __shared__ unsigned long long s_base;
-    const uint32_t n = (uint32_t)a.hdr->n;
+    const uint64_t T = a.toff[(uint32_t)a.hdr->n];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    for (uint32_t q = blockIdx.x; q < n; q += gridDim.x) {
-        const uint64_t b = a.toff[q], e = a.toff[q + 1];
-        if (threadIdx.x == 0) s_base = a.qout[q];
-        __syncthreads();
+    for (uint64_t c = blockIdx.x; c < a.nch && c * kCompactChunk < T; c += gridDim.x) {
+        const uint64_t b = c * kCompactChunk, e = b + kCompactChunk < T ? b + kCompactChunk : T;
+        uint64_t base = a.cbase[c];
         for (uint64_t t0 = b; t0 < e; t0 += kRowThreads) {
             const uint64_t i = t0 + threadIdx.x;
             const bool occ = i < e && a.keys[i] != kEmpty;
@@ -330,14 +331,29 @@ __global__ void __launch_bounds__(kRowThreads) compact_kernel(BatchArgs a)
                 total += sh[w];
             }
             if (occ) {
-                const uint64_t pos = s_base + before + __popc(m & ((1u << lane) - 1u));
+                const uint64_t pos = base + before + __popc(m & ((1u << lane) - 1u));
                 a.out_v[pos] = a.keys[i];
                 a.out_c[pos] = a.cnt[i];
             }
-            __syncthreads();
-            if (threadIdx.x == 0) s_base += total;
+            base += total;
             __syncthreads();
         }
+    }
+}
+
+// One warp per query q (and q = n): qout[q] = occupied slots before toff[q].
+__global__ void query_offsets_kernel(BatchArgs a)
+{
+    const uint32_t n = (uint32_t)a.hdr->n;
+    const int lane = threadIdx.x & 31;
+    const uint64_t warp = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) / 32;
+    const uint64_t nwarps = (uint64_t)gridDim.x * blockDim.x / 32;
+    for (uint64_t q = warp; q <= n; q += nwarps) {
+        const uint64_t s = a.toff[q], c = s / kCompactChunk;
+        unsigned cnt = 0;
+        for (uint64_t i = c * kCompactChunk + lane; i < s; i += 32) cnt += a.keys[i] != kEmpty;
+        for (int o = 16; o > 0; o >>= 1) cnt += __shfl_down_sync(kFull, cnt, o);
+        if (lane == 0) a.qout[q] = a.cbase[c] + cnt;
     }
 }
 
@@ -356,10 +372,11 @@ struct BatchState {
     uint32_t qcap = 0;
     uint64_t wcap = 0, tcap = 0;
     Header *d_hdr = nullptr;
-    uint32_t *d_src = nullptr, *d_tlog = nullptr, *d_keys = nullptr, *d_cnt = nullptr, *d_qcount = nullptr;
+    uint32_t *d_src = nullptr, *d_tlog = nullptr, *d_keys = nullptr, *d_cnt = nullptr, *d_ccount = nullptr;
     uint32_t *d_n = nullptr;
     uint64_t *d_walkers = nullptr, *d_seeds = nullptr, *d_woff = nullptr, *d_toff = nullptr, *d_qout = nullptr;
-    uint64_t *d_scan_tmp = nullptr;
+    uint64_t *d_scan_tmp = nullptr, *d_cbase = nullptr;
+    uint64_t nch = 0;  // compaction chunks of the table arena
     uint32_t *d_out_v = nullptr, *d_out_c = nullptr;
     BatchTune tune;
     cudaGraph_t graph = nullptr;
@@ -375,13 +392,13 @@ namespace {
 void free_buffers(BatchState &b)
 {
     for (void *p : {(void *)b.d_hdr, (void *)b.d_n, (void *)b.d_src, (void *)b.d_tlog, (void *)b.d_keys, (void *)b.d_cnt,
-                    (void *)b.d_qcount, (void *)b.d_walkers, (void *)b.d_seeds, (void *)b.d_woff, (void *)b.d_toff,
-                    (void *)b.d_qout, (void *)b.d_scan_tmp, (void *)b.d_out_v, (void *)b.d_out_c})
+                    (void *)b.d_ccount, (void *)b.d_walkers, (void *)b.d_seeds, (void *)b.d_woff, (void *)b.d_toff,
+                    (void *)b.d_qout, (void *)b.d_scan_tmp, (void *)b.d_cbase, (void *)b.d_out_v, (void *)b.d_out_c})
         if (p) cudaFree(p);
     b.d_hdr = nullptr;
     b.d_n = nullptr;
-    b.d_src = b.d_tlog = b.d_keys = b.d_cnt = b.d_qcount = b.d_out_v = b.d_out_c = nullptr;
-    b.d_walkers = b.d_seeds = b.d_woff = b.d_toff = b.d_qout = b.d_scan_tmp = nullptr;
+    b.d_src = b.d_tlog = b.d_keys = b.d_cnt = b.d_ccount = b.d_out_v = b.d_out_c = nullptr;
+    b.d_walkers = b.d_seeds = b.d_woff = b.d_toff = b.d_qout = b.d_scan_tmp = b.d_cbase = nullptr;
     if (b.exec) cudaGraphExecDestroy(b.exec);
     if (b.graph) cudaGraphDestroy(b.graph);
     b.exec = nullptr;
@@ -423,13 +440,15 @@ lt_status ensure(BatchState &b, uint32_t n, uint64_t W, uint64_t T)
     LT_TRY(dalloc(&b.d_n, 1));
     LT_TRY(dalloc(&b.d_src, qcap));
     LT_TRY(dalloc(&b.d_tlog, qcap));
-    LT_TRY(dalloc(&b.d_qcount, qcap));
+    b.nch = tcap / kCompactChunk + 1;
+    LT_TRY(dalloc(&b.d_ccount, b.nch));
+    LT_TRY(dalloc(&b.d_cbase, b.nch + 1));
     LT_TRY(dalloc(&b.d_walkers, qcap));
     LT_TRY(dalloc(&b.d_seeds, qcap));
     LT_TRY(dalloc(&b.d_woff, qcap + 1));
     LT_TRY(dalloc(&b.d_toff, qcap + 1));
     LT_TRY(dalloc(&b.d_qout, qcap + 1));
-    LT_TRY(dalloc(&b.d_scan_tmp, scan_tmp_elems(qcap)));
+    LT_TRY(dalloc(&b.d_scan_tmp, scan_tmp_elems(b.nch)));
     LT_TRY(dalloc(&b.d_keys, tcap));
     LT_TRY(dalloc(&b.d_cnt, tcap));
     LT_TRY(dalloc(&b.d_out_v, wcap));
@@ -456,7 +475,9 @@ BatchArgs args_of(lt_engine *e, BatchState &b, uint64_t thr)
     a.tlog = b.d_tlog;
     a.keys = b.d_keys;
     a.cnt = b.d_cnt;
-    a.qcount = b.d_qcount;
+    a.ccount = b.d_ccount;
+    a.cbase = b.d_cbase;
+    a.nch = b.nch;
     a.qout = b.d_qout;
     a.out_v = b.d_out_v;
     a.out_c = b.d_out_c;
@@ -492,11 +513,13 @@ lt_status enqueue_pipeline(lt_engine *e, BatchState &b, uint64_t thr, cudaStream
     clear_kernel<<<e->sms * 8, 256, 0, st>>>(a);
     LT_CUDA_TRY(cudaGetLastError());
     LT_CUDA_TRY(launch_walk(a, b.tune, e->sms, st));
-    const uint32_t rows = std::min<uint32_t>(b.qcap, (uint32_t)e->sms * 16);
-    count_kernel<<<rows, kRowThreads, 0, st>>>(a, b.qcap);
+    const unsigned chunk_ctas = (unsigned)std::min<uint64_t>(b.nch, (uint64_t)e->sms * 16);
+    chunk_count_kernel<<<chunk_ctas, kRowThreads, 0, st>>>(a);
     LT_CUDA_TRY(cudaGetLastError());
-    LT_CUDA_TRY((exclusive_scan<uint32_t, uint64_t>(b.d_qcount, b.qcap, b.d_qout, b.d_scan_tmp, st)));
-    compact_kernel<<<rows, kRowThreads, 0, st>>>(a);
+    LT_CUDA_TRY((exclusive_scan<uint32_t, uint64_t>(b.d_ccount, b.nch, b.d_cbase, b.d_scan_tmp, st)));
+    chunk_compact_kernel<<<chunk_ctas, kRowThreads, 0, st>>>(a);
+    const unsigned qblocks = (unsigned)std::min<uint64_t>(((uint64_t)b.qcap + 1) * 32 / 256 + 1, (uint64_t)e->sms * 16);
+    query_offsets_kernel<<<qblocks, 256, 0, st>>>(a);
     LT_CUDA_TRY(cudaGetLastError());
     return LT_OK;
 }
