@@ -30,6 +30,10 @@ namespace lt {
 namespace {
 
 constexpr unsigned kFull = 0xFFFFFFFFu;
+// idle lanes a warp waits for before refilling them (all lanes: always): the
+// refill sits on the warp's critical path and PPR's geometric walk lengths
+// would otherwise trigger one nearly every iteration
+constexpr int kRefillMin = 24;
 
 __device__ __forceinline__ uint32_t find_part(const uint32_t *off, uint32_t P, uint32_t v)
 {
@@ -121,7 +125,7 @@ __global__ void __launch_bounds__(kPartBlock) walk_part_kernel(StepArgs a)
 
     while (true) {
         const unsigned idle = __ballot_sync(kFull, !active);
-        if (idle != 0u && !exhausted) {
+        if (idle != 0u && !exhausted && (__popc(idle) >= kRefillMin || idle == kFull)) {
             const int leader = __ffs(idle) - 1;
             unsigned long long base = 0;
             if (lane == leader) base = atomicAdd(a.next, (unsigned long long)__popc(idle));

@@ -25,6 +25,10 @@ namespace lt {
 namespace {
 
 constexpr unsigned kFull = 0xFFFFFFFFu;
+// idle lanes a warp waits for before refilling them (all lanes: always): the
+// refill sits on the warp's critical path and PPR's geometric walk lengths
+// would otherwise trigger one nearly every iteration
+constexpr int kRefillMin = 24;
 
 struct Hints {
     uint64_t keep, stream;
@@ -71,7 +75,7 @@ __global__ void __launch_bounds__(kWholeBlock) walk_whole_kernel(WholeArgs a)
 
     while (true) {
         const unsigned idle = __ballot_sync(kFull, !active);
-        if (idle != 0u && !exhausted) {
+        if (idle != 0u && !exhausted && (__popc(idle) >= kRefillMin || idle == kFull)) {
             const int leader = __ffs(idle) - 1;
             unsigned long long base = 0;
             if (lane == leader) base = atomicAdd((unsigned long long *)a.next, (unsigned long long)__popc(idle));
