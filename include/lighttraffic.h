@@ -86,7 +86,8 @@ typedef struct lt_engine_cfg {
     uint32_t num_device_partitions;  /* -p: partitions cached on the device (0 = all) */
     uint64_t num_device_walkers;     /* -b: walkers held on the device (0 = all) */
     int sched;                       /* lt_sched */
-    int pipeline;                    /* overlap partition loads with stepping (1 = on) */
+    int pipeline;                    /* wave-run policies: overlap the next partition loads with the
+                                        current step kernel (1 = on; 0 = loads finish first) */
     uint64_t zerocopy_threshold;     /* walkers below which a cold partition is read zero-copy;
                                         UINT64_MAX = default partitionSize/128/2 (src/Scheduler.h:295) */
     uint64_t seed;                   /* Philox key */

@@ -437,19 +437,6 @@ public:
         return LT_OK;
     }
 
-    int32_t victim(const SchedView &v, int32_t except, uint32_t incoming) override
-    {
-        if (!ready_) return Policy::victim(v, except, incoming);
-        int32_t best = -1;
-        for (uint32_t i = 0; i < v.P; i++) {
-            if (v.slot_of[i] < 0 || (int32_t)i == except || i == incoming) continue;
-            if (best < 0 || score(v, i) < score(v, best) ||
-                (score(v, i) == score(v, best) && v.last_used[i] < v.last_used[best]))
-                best = (int32_t)i;
-        }
-        return best;
-    }
-
     void observe(const SchedView &v) override
     {
         t_++;
@@ -528,7 +515,6 @@ public:
 
     const char *name() const override { return use_net_ ? "learned" : "frequency"; }
 
-    bool single_pass() const override { return false; }
     bool wave() const override { return true; }
 
     void stats(lt_policy_stats &st) const override
@@ -548,10 +534,6 @@ public:
         st.baseline_loss = n ? b / n : 0.0;
     }
 
-    // Few walkers per batch make single scores noisy: swap rarely and only for
-    // a clearly hotter partition, so the cache settles on the hot set.
-    size_t swap_budget() const override { return 4; }
-    double swap_ratio() const override { return 4.0; }
     // Predicted visits once the predictor is trained; before that, the
     // partition's edge count (a hub-heavy RMAT prior).
     double cache_score(const SchedView &v, uint32_t p) override
@@ -560,7 +542,6 @@ public:
     }
 
 private:
-    double score(const SchedView &v, uint32_t p) const { return (double)v.waiting[p] + demand_[p]; }
 
     // A CUDA error in the policy's own work: keep the last forecasts and stop
     // training (scheduling decisions never affect results).

@@ -113,7 +113,6 @@ struct Ooc {
     uint64_t iteration = 0;
     uint64_t zc_threshold = 0;
     unsigned long long zc_rp_base = 0, zc_col_base = 0;  // device view of the pinned host CSR
-    bool single = false;  // single-pass run: partitions outside the cache are read zero-copy
     // zero-copy set of the next step kernel (wave runs)
     uint32_t zc_mask[kZcMaskWords] = {};
     bool zc_mask_any = false;
@@ -249,20 +248,16 @@ SchedView view(Ooc &o)
     return v;
 }
 
-// Clear v's table entry on the compute stream.  Kernels enqueued before this
-// point may still read the slot; loads into the slot wait for this point.
-// Table entry of a partition outside the cache: unreadable, or in a
-// single-pass run its pinned host slices (bit 0 marks zero-copy).
+// Table entry of a partition outside the cache: unreadable (zero-copy reads
+// go through the per-launch zc_part / zc_mask instead).
 void uncached_entry(Ooc &o, uint32_t p)
 {
-    if (o.single) {
-        o.h_rp[p] = (o.zc_rp_base + 8ull * o.g->node_off[p]) | 1ull;
-        o.h_col[p] = o.zc_col_base + 4ull * o.g->edge_off[p];
-    } else {
-        o.h_rp[p] = 0;
-        o.h_col[p] = 0;
-    }
+    o.h_rp[p] = 0;
+    o.h_col[p] = 0;
 }
+
+// Clear v's table entry on the compute stream.  Kernels enqueued before this
+// point may still read the slot; loads into the slot wait for this point.
 
 lt_status evict_partition(Ooc &o, uint32_t v)
 {
@@ -444,34 +439,6 @@ struct RunParams {
     uint64_t *counts;
     uint32_t *endpoints, *paths;
 };
-
-// Loads the policy wants started before the step kernel of partition p.
-// Victims are cleared from the table before the kernel is enqueued, so the
-// kernel never reads a slot that is being overwritten; the new entries are
-// published after the kernel.
-lt_status prefetch(Ooc &o, uint32_t p, std::vector<std::pair<uint32_t, cudaEvent_t>> &deferred)
-{
-    lt_engine &e = *o.e;
-    if (!e.cfg.pipeline) return LT_OK;
-    SchedView v = view(o);
-    std::vector<uint32_t> order;
-    o.policy->prefetch_order(v, p, order);
-    const size_t depth = o.policy->prefetch_depth(v);
-    for (size_t i = 0; i < order.size() && i < depth; i++) {
-        const uint32_t c = order[i];
-        if (o.slot_of[c] >= 0) continue;
-        int32_t slot = free_slot(o);
-        if (slot < 0) {
-            v = view(o);
-            const int32_t victim = o.policy->victim_for_prefetch(v, (int32_t)p, c);
-            if (victim < 0) break;
-            slot = o.slot_of[victim];
-            LT_TRY(evict_partition(o, (uint32_t)victim));
-        }
-        LT_TRY(start_load(o, c, slot, &deferred));
-    }
-    return LT_OK;
-}
 
 // Launch the step kernel over p's device chunks plus G lazily created walkers
 // (ordinals lazy_begin..), then bucket the walkers that left.  p < 0: the
@@ -781,68 +748,10 @@ lt_status process(Ooc &o, const RunParams &rp, uint32_t p)
         LT_TRY(spill_until(o, (uint64_t)o.P + 2 + 1, (int32_t)p));
         G = lazy_budget(o, (int32_t)p, qp.lazy_left());
     }
-    std::vector<std::pair<uint32_t, cudaEvent_t>> deferred;
-    LT_TRY(prefetch(o, p, deferred));
-    LT_TRY(step_and_bucket(o, rp, (int32_t)p, lazy_of(o, rp, (int32_t)p, qp.lazy_next, G), zero_copy, &deferred));
+    LT_TRY(step_and_bucket(o, rp, (int32_t)p, lazy_of(o, rp, (int32_t)p, qp.lazy_next, G), zero_copy, nullptr));
     drain_timers(o, false);
     SchedView v = view(o);
     o.policy->observe(v);
-    return LT_OK;
-}
-
-// Single-pass cache update: fill free slots with the best-scored partitions,
-// then swap the worst cached partition for a clearly better one, at most
-// swap_budget times per batch.  Loads are published after the next kernel.
-lt_status update_cache(Ooc &o, std::vector<std::pair<uint32_t, cudaEvent_t>> &deferred)
-{
-    SchedView v = view(o);
-    std::vector<double> sc(o.P);
-    for (uint32_t p = 0; p < o.P; p++) sc[p] = o.policy->cache_score(v, p);
-    std::vector<uint32_t> out_set, in_set;
-    for (uint32_t p = 0; p < o.P; p++) (o.slot_of[p] < 0 ? out_set : in_set).push_back(p);
-    std::sort(out_set.begin(), out_set.end(), [&](uint32_t a, uint32_t b) { return sc[a] != sc[b] ? sc[a] > sc[b] : a < b; });
-    std::sort(in_set.begin(), in_set.end(), [&](uint32_t a, uint32_t b) { return sc[a] != sc[b] ? sc[a] < sc[b] : a < b; });
-    size_t next_in = 0, swaps = 0;
-    for (uint32_t c : out_set) {
-        if (sc[c] <= 0.0) break;
-        int32_t slot = free_slot(o);
-        if (slot < 0) {
-            if (swaps >= o.policy->swap_budget() || next_in >= in_set.size()) break;
-            const uint32_t w = in_set[next_in];
-            if (!(sc[c] > o.policy->swap_ratio() * sc[w] + 1.0)) break;
-            next_in++;
-            swaps++;
-            slot = o.slot_of[w];
-            LT_TRY(evict_partition(o, w));
-        }
-        LT_TRY(start_load(o, c, slot, &deferred));
-    }
-    return LT_OK;
-}
-
-// Single-pass run: every partition readable, walkers created in batches and
-// walked to completion; between batches the policy reshapes the cache.
-lt_status single_pass_run(Ooc &o, const RunParams &rp, uint64_t W)
-{
-    lt_engine &e = *o.e;
-    for (uint32_t p = 0; p < o.P; p++)
-        if (o.slot_of[p] < 0) {
-            uncached_entry(o, p);
-            LT_TRY(set_entry(o, p, e.s_compute));
-        }
-    const uint64_t batch = std::max<uint64_t>(uint64_t(1) << 22, W / 48);
-    uint64_t made = 0;
-    std::vector<std::pair<uint32_t, cudaEvent_t>> deferred;
-    while (made < W) {
-        const uint64_t G = std::min(batch, W - made);
-        o.iteration++;
-        e.stats.iterations++;
-        LT_TRY(update_cache(o, deferred));
-        LT_TRY(step_and_bucket(o, rp, -1, lazy_of(o, rp, -1, made, G), false, &deferred));
-        made += G;
-        drain_timers(o, false);
-        o.policy->observe(view(o));
-    }
     return LT_OK;
 }
 
@@ -986,6 +895,16 @@ lt_status wave_step(Ooc &o, const RunParams &rp, WaveState &w, bool &done)
             }
         }
         if (started) e.stats.explicit_iterations++;
+        if (!e.cfg.pipeline) {
+            // no pipelining (--no-pipeline): the loads finish before this
+            // iteration's kernel instead of overlapping it
+            for (auto &d : inflight) {
+                LT_CUDA_TRY(cudaStreamWaitEvent(e.s_compute, d.second, 0));
+                LT_TRY(set_entry(o, d.first, e.s_compute));
+                loading[d.first] = 0;
+            }
+            inflight.clear();
+        }
 
         // walkers to create: into a readable partition if one has them
         uint64_t chunks = 0, walkers = 0;
@@ -1054,7 +973,7 @@ lt_status wave_step(Ooc &o, const RunParams &rp, WaveState &w, bool &done)
             }
             if (lazy_p >= 0) G = wave_lazy_budget(o, chunks, walkers, o.lazy_left[lazy_p]);
         }
-        if (parts.empty() && G == 0 && inflight.empty()) {
+        if (parts.empty() && G == 0 && started == 0) {
             // Nothing readable holds walkers, none can be created and nothing
             // is loading: the pool is full of walkers queued outside the cache
             // while the cached partitions wait for spilled or uncreated ones.
@@ -1224,26 +1143,7 @@ lt_status ooc_run(lt_engine *e, int app, int start, uint32_t source, uint64_t W,
         reset_queues(o);
         refresh_all(o);
         o.prev_computed = -1;
-        bool fresh = true;
-        o.single = o.policy->single_pass() && o.zc_rp_base != 0;
-        if (o.single) {
-            LT_TRY(single_pass_run(o, rp, W));
-            refresh_all(o);
-            bool left = false;
-            for (uint32_t p = 0; p < o.P && !left; p++) left = o.waiting[p] > 0;
-            if (!left) continue;
-            // a walker left the readable set (cannot happen while every
-            // partition is mapped); drain it with the regular loop
-            o.single = false;
-            for (uint32_t p = 0; p < o.P; p++)
-                if (o.slot_of[p] < 0) {
-                    uncached_entry(o, p);
-                    LT_TRY(set_entry(o, p, e->s_compute));
-                }
-            fresh = false;
-        }
-        if (!fresh) {
-        } else if (start == kStartSource) {
+        if (start == kStartSource) {
             o.q[g.find_partition(source)].lazy_total = W;
         } else if (start == kStartPerVertex) {
             const uint64_t wraps = W / g.V, rem = W % g.V;
@@ -1619,13 +1519,6 @@ lt_status serve_open(lt_engine *e, uint32_t max_active, uint64_t table_slots, fl
     e->stats = lt_stats{};
     o.serve = s;
     if (o.policy->wave()) s->wave = new WaveState(o.P);
-    o.single = !s->wave && o.policy->serve_single_pass() && o.zc_rp_base != 0;
-    if (o.single)
-        for (uint32_t p = 0; p < o.P; p++)
-            if (o.slot_of[p] < 0) {
-                uncached_entry(o, p);
-                LT_TRY(set_entry(o, p, e->s_compute));
-            }
     *out = s;
     return LT_OK;
 }
@@ -1654,8 +1547,6 @@ lt_status serve_step(lt_server *s, uint32_t *completed, uint32_t *active, uint32
     LT_TRY(serve_admit(*s));
     uint32_t p = 0;
     SchedView v = view(o);
-    bool spilled = false;
-    for (uint32_t i = 0; i < o.P && !spilled; i++) spilled = !o.q[i].host_chunks.empty();
     if (s->wave) {
         // light load: every step is a final sweep that finishes the admitted
         // walkers in one kernel; heavy load: waves with overlapped loads
@@ -1665,30 +1556,6 @@ lt_status serve_step(lt_server *s, uint32_t *completed, uint32_t *active, uint32
         rp.thr = s->thr;
         bool idle = false;
         LT_TRY(wave_step(o, rp, *s->wave, idle));
-    } else if (o.single && !spilled) {
-        // every partition readable: drain all in-flight walkers in one launch
-        std::vector<uint32_t> parts;
-        for (uint32_t i = 0; i < o.P; i++)
-            if (!o.q[i].dev_chunks.empty()) parts.push_back(i);
-        std::vector<std::pair<uint32_t, cudaEvent_t>> deferred;
-        o.iteration++;
-        e.stats.iterations++;
-        LT_TRY(update_cache(o, deferred));
-        RunParams rp{};
-        rp.app = kPPR;
-        rp.start = kStartSource;
-        rp.thr = s->thr;
-        if (!parts.empty()) {
-            Lazy none{};
-            none.mode = kStartSource;
-            LT_TRY(step_and_bucket_parts(o, rp, parts, -1, none, false, &deferred));
-        }
-        for (auto &d : deferred) {
-            LT_CUDA_TRY(cudaStreamWaitEvent(e.s_compute, d.second, 0));
-            LT_TRY(set_entry(o, d.first, e.s_compute));
-        }
-        drain_timers(o, false);
-        o.policy->observe(view(o));
     } else if (o.policy->next(v, o.prev_computed, false, p) || o.policy->next(v, o.prev_computed, true, p)) {
         RunParams rp{};
         rp.app = kPPR;
@@ -1756,15 +1623,6 @@ void serve_close(lt_server *s)
         }
         drain_timers(*s->o, true);
         s->o->serve = nullptr;
-        if (s->o->single) {
-            s->o->single = false;
-            for (uint32_t p = 0; p < s->o->P; p++)
-                if (s->o->slot_of[p] < 0) {
-                    uncached_entry(*s->o, p);
-                    set_entry(*s->o, p, s->e->s_compute);
-                }
-            cudaStreamSynchronize(s->e->s_compute);
-        }
         reset_queues(*s->o);
         refresh_all(*s->o);
     }

@@ -15,8 +15,8 @@
 //   no look-ahead loads (the reference loads the partition it is about to
 //                     compute, :173-213).
 // The FIFO policy restates the FIFO_SCHE variant (:113-127, :391-418).
-// The learned policy (mlp.h) keeps these rules but scores partitions by the
-// walker arrivals a small MLP predicts, and loads predicted partitions ahead.
+// The learned, frequency and batched policies run the engine in waves (see
+// Policy::wave) and differ only in which cached partitions they give up.
 #pragma once
 
 #include <cstdint>
@@ -49,25 +49,10 @@ public:
     virtual int32_t victim(const SchedView &v, int32_t except, uint32_t incoming);
     // shouldZerocopy for a partition that is not cached.
     virtual bool zero_copy(const SchedView &v, uint32_t p, uint64_t threshold) { return v.waiting[p] < threshold; }
-    // Look-ahead loads: candidates (best first), how many per iteration, and
-    // the cached partition to give up for candidate c (-1: do not load c).
-    virtual void prefetch_order(const SchedView &v, uint32_t exclude, std::vector<uint32_t> &out) { out.clear(); }
-    virtual size_t prefetch_depth(const SchedView &v) { return 0; }
-    virtual int32_t victim_for_prefetch(const SchedView &v, int32_t computing, uint32_t c) { return -1; }
     // Called after every iteration; v.arrivals holds that iteration's arrivals.
     virtual void observe(const SchedView &v) {}
-    // Single-pass mode: every partition stays readable -- cached, or read
-    // zero-copy from pinned host memory -- so walkers never queue and every
-    // batch of walkers finishes in one step kernel; the policy only chooses
-    // which partitions hold cache slots, by cache_score (higher = keep), and
-    // swaps at most swap_budget partitions per batch.
-    virtual bool single_pass() const { return false; }
-    // The same while serving queries (light, latency-bound load).
-    virtual bool serve_single_pass() const { return false; }
+    // Wave runs: higher = better kept in the cache (victims have the lowest).
     virtual double cache_score(const SchedView &v, uint32_t p) { return 0.0; }
-    virtual size_t swap_budget() const { return 0; }
-    // a cached partition is given up only for one scoring swap_ratio() times higher
-    virtual double swap_ratio() const { return 1.25; }
     // Wave runs: each step kernel drains every readable queue (all cached
     // partitions with walkers, plus a zero-copy set in the final phase) while
     // the loads for the next kernel run on the copy stream.  At most

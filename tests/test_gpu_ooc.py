@@ -130,3 +130,16 @@ def test_wave_runs_take_fewer_iterations(lt, require_gpu, g16):
         res[sched] = (e.ppr(0, 300000, 0.15), e.stats())
     assert (res[0][0] == res[4][0]).all()
     assert res[4][1]["iterations"] < res[0][1]["iterations"]
+
+
+def test_wave_runs_without_pipelining(lt, require_gpu, g16):
+    """--no-pipeline: loads finish before the kernel of their iteration;
+    results identical, same loads."""
+    rp, col = g16
+    out = {}
+    for pipe in (True, False):
+        g, e = _eng(lt, rp, col, 256 << 10, partitions=4, sched=4, seed=9, pipeline=pipe, zerocopy_threshold=0)
+        out[pipe] = (e.ppr(0, 300000, 0.15), e.stats())
+    assert (out[True][0] == out[False][0]).all()
+    want, _, _ = oracle.ppr(rp, col, 0, 300000, prob=0.15, seed=9)
+    assert (out[False][0] == want).all()
