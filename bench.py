@@ -299,7 +299,7 @@ def gb300_ooc(args, cfg):
     V, E = g.num_nodes, g.num_edges
     W = 2 * V
     link_peak = lt.host_link_gbs(local)
-    counts = np.zeros(V, dtype=np.uint64)
+    counts = lt.pinned_empty(V, np.uint64)   # host count buffer in page-locked memory
     clocks = ClockSampler(local)
     clocks.start()
     time.sleep(0.3)
@@ -613,10 +613,12 @@ def gb300_batch(args, cfg):
     elapsed_ms = max_over_ranks(dist, local, a.elapsed_time(b))
     # one more batch through the public host API: stats (hops) and e2e time
     e2e = []
-    for _ in range(2):
+    pinned_out = (lt.pinned_empty(n + 1, np.uint64), lt.pinned_empty(Wt, np.uint32), lt.pinned_empty(Wt, np.uint32))
+    for _ in range(3):
         t0 = time.perf_counter()
-        off, v, c = e.ppr_batch(sources, walkers, seeds, cfg["prob"])
+        off, v, c = e.ppr_batch(sources, walkers, seeds, cfg["prob"], out=pinned_out)
         e2e.append(time.perf_counter() - t0)
+    e2e = e2e[1:]
     st = e.stats()
     assert int(c.astype(np.uint64).sum()) == Wt, "PPR invariant (one count per walk) violated"
     moves = st["moves"]

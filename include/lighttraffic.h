@@ -342,6 +342,13 @@ lt_status lt_mlp_check(int device, uint32_t n, const float *x, const float *y, c
  * in the reference. */
 lt_status lt_host_link_gbs(int device, double *gbs);
 
+/* Page-locked host memory (portable, mapped) for the host buffers of the
+ * lt_run_* / lt_ppr_batch calls: results then come back at the link's speed
+ * instead of through the driver's staging copies into pageable memory.  No
+ * counterpart in the reference. */
+lt_status lt_host_alloc(uint64_t bytes, void **out);
+void lt_host_free(void *p);
+
 /* The remainder x[i] % d[i] as the walk kernels compute it (host build of the
  * same code), for checking it against native division.  No counterpart in
  * the reference. */

@@ -132,6 +132,8 @@ def _load():
         "lt_walk_device_compact": ([C.c_int, C.c_int, vp, vp, C.c_uint32, C.c_uint32, C.c_uint64, C.c_uint32,
                                     C.c_float, C.c_uint32, C.c_uint64, vp, vp, vp, vp, vp, vp], C.c_int),
         "lt_rowptr_narrow": ([vp, vp, C.c_uint32, vp], C.c_int),
+        "lt_host_alloc": ([C.c_uint64, C.POINTER(vp)], C.c_int),
+        "lt_host_free": ([vp], None),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)
@@ -279,6 +281,29 @@ class Graph:
             pass
 
 
+class _Pinned:
+    def __init__(self, nbytes):
+        self.ptr = C.c_void_p()
+        check(lib.lt_host_alloc(nbytes, C.byref(self.ptr)))
+        self.nbytes = nbytes
+
+    def __del__(self):
+        if self.ptr:
+            lib.lt_host_free(self.ptr)
+            self.ptr = C.c_void_p()
+
+
+def pinned_empty(n: int, dtype=np.uint64) -> np.ndarray:
+    """Uninitialised numpy array in page-locked host memory (lt_host_alloc),
+    freed with the array: host buffers for results that come back from the
+    device at the link's speed."""
+    dt = np.dtype(dtype)
+    owner = _Pinned(max(1, n * dt.itemsize))
+    raw = (C.c_uint8 * owner.nbytes).from_address(owner.ptr.value)
+    raw._lt_owner = owner
+    return np.frombuffer(raw, dtype=dt, count=n)
+
+
 class Server:
     """Continuous-batching PPR server on an out-of-core engine."""
 
@@ -380,17 +405,25 @@ class Engine:
                               _ptr(pa, C.c_uint32)))
         return ep, pa
 
-    def ppr_batch(self, sources, walkers, seeds=None, prob: float = 0.15):
+    def ppr_batch(self, sources, walkers, seeds=None, prob: float = 0.15, out=None):
         """Batched multi-source PPR: returns (offsets[n+1], vertices, counts);
-        query q's pairs are [offsets[q], offsets[q+1])."""
+        query q's pairs are [offsets[q], offsets[q+1]).  `out` = (offsets,
+        vertices, counts) arrays to fill (u64[n+1], u32[>= sum(walkers)] x 2),
+        e.g. from pinned_empty, instead of fresh ones."""
         src = np.ascontiguousarray(sources, dtype=np.uint32)
         w = np.ascontiguousarray(walkers, dtype=np.uint64)
         sd = None if seeds is None else np.ascontiguousarray(seeds, dtype=np.uint64)
         n = len(src)
         cap = int(w.sum())
-        off = np.zeros(n + 1, np.uint64)
-        v = np.zeros(max(1, cap), np.uint32)
-        c = np.zeros(max(1, cap), np.uint32)
+        if out is None:
+            off = np.zeros(n + 1, np.uint64)
+            v = np.zeros(max(1, cap), np.uint32)
+            c = np.zeros(max(1, cap), np.uint32)
+        else:
+            off, v, c = out
+            if len(off) < n + 1 or len(v) < cap or len(c) < cap:
+                raise ValueError("output arrays too small for the batch")
+            cap = min(len(v), len(c))
         check(lib.lt_ppr_batch(self._h, n, _ptr(src, C.c_uint32), _ptr(w, C.c_uint64), _ptr(sd, C.c_uint64),
                                prob, _ptr(off, C.c_uint64), _ptr(v, C.c_uint32), _ptr(c, C.c_uint32), cap))
         tot = int(off[-1])

@@ -382,6 +382,26 @@ lt_status lt_walk_device_compact(int app, int start_mode, const uint32_t *d_rowp
                                seed, d_counts32, d_endpoints, d_paths, d_scratch, d_stats, (cudaStream_t)stream, 0);
 }
 
+lt_status lt_host_alloc(uint64_t bytes, void **out)
+{
+    if (!out) return fail(LT_ERR_INVALID, "null output");
+    *out = nullptr;
+    void *p = nullptr;
+    const cudaError_t ce = cudaHostAlloc(&p, bytes ? bytes : 1, cudaHostAllocPortable | cudaHostAllocMapped);
+    if (ce != cudaSuccess) {
+        cudaGetLastError();
+        return fail(ce == cudaErrorMemoryAllocation ? LT_ERR_NOMEM : LT_ERR_CUDA, "cudaHostAlloc of %llu bytes: %s",
+                    (unsigned long long)bytes, cudaGetErrorString(ce));
+    }
+    *out = p;
+    return LT_OK;
+}
+
+void lt_host_free(void *p)
+{
+    if (p) cudaFreeHost(p);
+}
+
 lt_status lt_rowptr_narrow(const uint64_t *d_rowptr, uint32_t *d_rowptr32, uint32_t num_nodes, void *stream)
 {
     return rowptr_narrow(d_rowptr, d_rowptr32, num_nodes, (cudaStream_t)stream);

@@ -89,3 +89,24 @@ def test_batch_needs_resident_graph(lt, require_gpu, graph16):
     e = lt.Engine(g, partitions=2)
     with pytest.raises(lt.LTError):
         e.ppr_batch([0], [10])
+
+
+def test_batch_into_pinned_outputs(lt, require_gpu):
+    """ppr_batch(out=...) with page-locked arrays from pinned_empty gives the
+    same pairs as fresh arrays, twice in a row (buffers reused)."""
+    g = lt.Graph.rmat(14, 1 << 18, seed=3, part_bytes=1 << 30)
+    e = lt.Engine(g, seed=5)
+    src = np.array([0, 3, 3, 17], np.uint32)
+    w = np.array([5000, 1200, 800, 3000], np.uint64)
+    seeds = np.array([1, 2, 3, 4], np.uint64)
+    ref = e.ppr_batch(src, w, seeds)
+    out = (lt.pinned_empty(len(src) + 1, np.uint64), lt.pinned_empty(int(w.sum()), np.uint32),
+           lt.pinned_empty(int(w.sum()), np.uint32))
+    for _ in range(2):
+        off, v, c = e.ppr_batch(src, w, seeds, out=out)
+        assert (off == ref[0]).all()
+        for q in range(len(src)):
+            a, b = int(off[q]), int(off[q + 1])
+            got = sorted(zip(v[a:b].tolist(), c[a:b].tolist()))
+            want = sorted(zip(ref[1][a:b].tolist(), ref[2][a:b].tolist()))
+            assert got == want
