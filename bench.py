@@ -37,7 +37,8 @@ vertices removed, stand in for the reference's datasets, which are absent):
       and 10 000 queries/s, uniform random sources, lognormal walk counts
       (median 1e4, sigma 1.0 -- left open by the workload) clipped to
       [1e3, 1e5]; continuous batching through lt_serve_*; p50 / p99 latency
-      and steps/s per rate for the learned and the plain scheduler.
+      and steps/s per rate for the learned and the plain scheduler, and for
+      wave steps with least-recently-used slots (batched, ablation).
 Steps per run: hops taken (PPR, the reference's 2|V|/0.15 estimate counted
 exactly) or updates (PageRank, W * l).
 --impl reference times the CPU restatement of the reference walk semantics
@@ -690,7 +691,7 @@ def gb300_serve(args, cfg):
     time.sleep(0.3)
     wall0 = time.time()
     out = {}
-    for name, sched in [("learned", lt.SCHED_LEARNED), ("plain", lt.SCHED_PLAIN)]:
+    for name, sched in [("learned", lt.SCHED_LEARNED), ("plain", lt.SCHED_PLAIN), ("batched", lt.SCHED_BATCHED)]:
         e = lt.Engine(g, partitions=cfg["partitions"], batch=cfg["batch"], seed=SEED_WALK, sched=sched, device=local)
         per_rate = {}
         for rate, seconds in zip(cfg["rates"], cfg["seconds"]):
