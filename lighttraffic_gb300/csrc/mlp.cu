@@ -461,7 +461,7 @@ public:
             if (cudaEventRecord(stage_ev_[slot], st) != cudaSuccess) fail_net();
             return;
         }
-        // pick up the previous round if it has finished; never wait for it
+        // pick up the previous prediction pass if it has finished; never wait for it
         if (inflight_) {
             if (cudaEventQuery(ev_) != cudaSuccess) {
                 cudaGetLastError();
