@@ -75,7 +75,7 @@ def test_pagerank_ooc(lt, require_gpu, g16, case, start):
     assert (s["updates"], s["moves"], s["teleports"]) == tuple(int(x) for x in st)
 
 
-@pytest.mark.parametrize("case", CASES[:3] + CASES[4:5])
+@pytest.mark.parametrize("case", CASES[:3] + CASES[4:5] + [(4, 0, None, 4), (3, 20000, 0, 2), (4, 0, 1 << 40, 4)])
 def test_walk_ooc(lt, require_gpu, g16, case):
     K, B, zc, sched = case
     rp, col = g16
