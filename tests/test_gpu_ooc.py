@@ -97,9 +97,10 @@ def test_resident_and_ooc_agree(lt, require_gpu, g16):
     assert (full.pagerank(3 * V, 10, start=2) == part.pagerank(3 * V, 10, start=2)).all()
 
 
-def test_repeated_runs_and_drop_cache(lt, require_gpu, g16):
+@pytest.mark.parametrize("sched", [0, 2, 4])
+def test_repeated_runs_and_drop_cache(lt, require_gpu, g16, sched):
     rp, col = g16
-    g, e = _eng(lt, rp, col, 256 << 10, partitions=3, seed=12)
+    g, e = _eng(lt, rp, col, 256 << 10, partitions=3, seed=12, sched=sched)
     a = e.ppr(0, 100000, 0.15)
     b = e.ppr(0, 100000, 0.15)                 # warm cache
     e.drop_cache()
