@@ -310,6 +310,7 @@ def gb300_ooc(args, cfg):
               "frequency": lt.SCHED_FREQUENCY}
 
     engines = {}
+    zc_model_all = [0]   # modelled zero-copy bytes over every run, warm-up included
 
     def one_run(name):
         # one engine per scheduler for the whole benchmark (its pinned host
@@ -324,7 +325,9 @@ def gb300_ooc(args, cfg):
         e.ppr(0, W, cfg["prob"], out=counts)
         t1 = time.perf_counter()
         assert int(counts.sum()) == W, "PPR invariant (one count per walk) violated"
-        return (t1 - t0, e.stats(), e.policy_stats())
+        st = e.stats()
+        zc_model_all[0] += st["zerocopy_bytes"]
+        return (t1 - t0, st, e.policy_stats())
 
     # W warm-up runs of the headline (learned) and of the reference policy;
     # one of each ablation (its code paths warm) keeps the link traffic
@@ -393,6 +396,11 @@ def gb300_ooc(args, cfg):
                       "achieved_gbs": link_bytes(s) / (L["elapsed"] / args.steps) / 1e9,
                       "peak_gbs": link_peak, "frac": link_bytes(s) / (L["elapsed"] / args.steps) / 1e9 / link_peak,
                       "peak_gbs_after_timed_runs": link_after,
+                      "bytes_by_kind": {name: {"graph_loads": results[name]["stats"]["h2d_graph_bytes"],
+                                               "zero_copy_model": results[name]["stats"]["zerocopy_bytes"],
+                                               "walker_spill": results[name]["stats"]["h2d_walker_bytes"]
+                                               + results[name]["stats"]["d2h_walker_bytes"]} for name in scheds},
+                      "zero_copy_model_bytes_all_runs": zc_model_all[0],
                       "peak_source": "measured pinned H2D copy in this run, before the warm-up",
                       "zerocopy_bytes_model": "256 B per zero-copy hop (two 128 B host lines)"},
         "plain": {"value": plain_value, "bytes_per_step": link_bytes(Pn["stats"]) / Pn["steps"],
