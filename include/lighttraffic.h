@@ -43,7 +43,8 @@ typedef enum lt_status {
     LT_ERR_PARTITION = 6,   /* one vertex does not fit the partition size */
     LT_ERR_TIMEOUT = 7,     /* a bounded device-side wait gave up */
     LT_ERR_CAPACITY = 8,    /* a device queue or buffer limit was exceeded */
-    LT_ERR_UNSUPPORTED = 9  /* configuration not supported by this build */
+    LT_ERR_UNSUPPORTED = 9, /* configuration not supported by this build */
+    LT_INTERRUPTED = 10     /* the run stopped at a checkpoint, as lt_engine_checkpoint asked */
 } lt_status;
 
 typedef enum lt_app { LT_APP_PPR = 0, LT_APP_PAGERANK = 1, LT_APP_WALK = 2 } lt_app;
@@ -201,6 +202,39 @@ lt_status lt_run_walk(lt_engine *e, uint64_t num_walkers, uint32_t length, uint3
 /* Statistics and phase timers of the last run (Scheduler::timing,
  * src/Scheduler.h:440-453). */
 lt_status lt_engine_stats(const lt_engine *e, lt_stats *out);
+
+/* ------------------------------------------------- checkpoint / resume */
+
+/* Checkpoints of out-of-core runs (no counterpart in the reference, whose
+ * runs cannot be resumed).  Once armed, every lt_run_* call on this engine
+ * writes the run's state to `path` every `every` scheduler iterations
+ * (replacing the previous file atomically); with stop != 0 the call returns
+ * LT_INTERRUPTED right after the first checkpoint, as a preempted job would.
+ * path = NULL disarms.  LT_ERR_UNSUPPORTED on an engine that holds the whole
+ * graph (its runs are one kernel). */
+lt_status lt_engine_checkpoint(lt_engine *e, const char *path, uint64_t every, int stop);
+
+typedef struct lt_checkpoint_info {
+    int app;                 /* lt_app */
+    int start_mode;          /* lt_start */
+    uint32_t source, length, runs, run_index;
+    uint64_t num_walkers;
+    uint32_t num_nodes;
+    int has_endpoints, has_paths;
+    uint64_t iteration;      /* scheduler iterations done when it was written */
+} lt_checkpoint_info;
+
+/* What a checkpoint file holds, for sizing the outputs of lt_resume. */
+lt_status lt_checkpoint_read_info(const char *path, lt_checkpoint_info *out);
+
+/* Finish the run saved in `path` on an out-of-core engine over the same
+ * graph (any cache size, walker pool or scheduler) and write the outputs the
+ * interrupted call would have written: counts u64[V] (PPR / PageRank),
+ * endpoints u32[W] and paths u32[W*(length+1)] (generic walk, when the
+ * original call asked for them).  The walks keep the checkpoint's seed, and
+ * the results are those of a run that was never interrupted. */
+lt_status lt_resume(lt_engine *e, const char *path, uint64_t *counts_out, uint32_t *endpoints_out,
+                    uint32_t *paths_out);
 
 /* ------------------------------------------------- device-resident kernels */
 

@@ -24,6 +24,7 @@ LIB_PATH = os.path.join(PKG, "liblighttraffic.so")
 BIN_DIR = os.path.join(PKG, "bin")
 
 APP_PPR, APP_PAGERANK, APP_WALK = 0, 1, 2
+INTERRUPTED = 10  # lt_status: the run stopped at a checkpoint
 START_SOURCE, START_UNIFORM, START_PER_VERTEX = 0, 1, 2
 SCHED_PLAIN, SCHED_FIFO, SCHED_LEARNED, SCHED_FREQUENCY, SCHED_BATCHED = 0, 1, 2, 3, 4
 INVALID_NODE = 0xFFFFFFFF
@@ -59,6 +60,13 @@ class BatchTune(C.Structure):
 class PolicyStats(C.Structure):
     _fields_ = [("name", C.c_char * 16), ("train_steps", C.c_uint64), ("net_loss", C.c_double),
                 ("baseline_loss", C.c_double), ("predictions", C.c_uint64)]
+
+
+class CheckpointInfo(C.Structure):
+    _fields_ = [("app", C.c_int), ("start_mode", C.c_int), ("source", C.c_uint32), ("length", C.c_uint32),
+                ("runs", C.c_uint32), ("run_index", C.c_uint32), ("num_walkers", C.c_uint64),
+                ("num_nodes", C.c_uint32), ("has_endpoints", C.c_int), ("has_paths", C.c_int),
+                ("iteration", C.c_uint64)]
 
 
 class Stats(C.Structure):
@@ -133,6 +141,9 @@ def _load():
                                     C.c_float, C.c_uint32, C.c_uint64, vp, vp, vp, vp, vp, vp], C.c_int),
         "lt_rowptr_narrow": ([vp, vp, C.c_uint32, vp], C.c_int),
         "lt_host_alloc": ([C.c_uint64, C.POINTER(vp)], C.c_int),
+        "lt_engine_checkpoint": ([vp, C.c_char_p, C.c_uint64, C.c_int], C.c_int),
+        "lt_checkpoint_read_info": ([C.c_char_p, C.POINTER(CheckpointInfo)], C.c_int),
+        "lt_resume": ([vp, C.c_char_p, u64p, u32p, u32p], C.c_int),
         "lt_host_free": ([vp], None),
     }
     for name, (args, res) in sig.items():
@@ -293,6 +304,13 @@ class _Pinned:
             self.ptr = C.c_void_p()
 
 
+def checkpoint_info(path) -> dict:
+    """Header of a checkpoint file written by Engine.checkpoint."""
+    i = CheckpointInfo()
+    check(lib.lt_checkpoint_read_info(os.fsencode(path), C.byref(i)))
+    return {k: getattr(i, k) for k, _ in CheckpointInfo._fields_}
+
+
 def pinned_empty(n: int, dtype=np.uint64) -> np.ndarray:
     """Uninitialised numpy array in page-locked host memory (lt_host_alloc),
     freed with the array: host buffers for results that come back from the
@@ -437,6 +455,30 @@ class Engine:
         t = BatchTune()
         check(lib.lt_engine_batch_tune(self._h, C.byref(t)))
         return {"block": t.block, "ctas_per_sm": t.ctas_per_sm, "load_shift": t.load_shift, "tuned": bool(t.tuned)}
+
+    def checkpoint(self, path, every: int, stop: bool = False):
+        """Write the state of every following run to `path` every `every`
+        scheduler iterations; stop=True ends the run after the first one
+        (LTError with status INTERRUPTED).  path=None disarms."""
+        check(lib.lt_engine_checkpoint(self._h, None if path is None else os.fsencode(path), every, int(stop)))
+
+    def resume(self, path):
+        """Finish the run saved in `path`: counts (PPR / PageRank) or
+        (endpoints, paths or None) (generic walk)."""
+        info = checkpoint_info(path)
+        V, W = info["num_nodes"], info["num_walkers"]
+        counts = ep = pa = None
+        if info["app"] != APP_WALK:
+            counts = np.zeros(V, dtype=np.uint64)
+        if info["has_endpoints"]:
+            ep = np.zeros(W, dtype=np.uint32)
+        if info["has_paths"]:
+            pa = np.zeros(W * (info["length"] + 1), dtype=np.uint32)
+        check(lib.lt_resume(self._h, os.fsencode(path), _ptr(counts, C.c_uint64), _ptr(ep, C.c_uint32),
+                            _ptr(pa, C.c_uint32)))
+        if info["app"] != APP_WALK:
+            return counts
+        return ep, pa
 
     def policy_stats(self) -> dict:
         s = PolicyStats()

@@ -23,6 +23,7 @@ const char *lt_strerror(lt_status s)
     case LT_ERR_TIMEOUT: return "bounded device wait expired";
     case LT_ERR_CAPACITY: return "capacity exceeded";
     case LT_ERR_UNSUPPORTED: return "unsupported configuration";
+    case LT_INTERRUPTED: return "run stopped at a checkpoint";
     }
     return "unknown status";
 }
@@ -380,6 +381,28 @@ lt_status lt_walk_device_compact(int app, int start_mode, const uint32_t *d_rowp
 {
     return walk_device_compact(app, start_mode, d_rowptr32, d_col, num_nodes, source, num_walkers, length, prob, run,
                                seed, d_counts32, d_endpoints, d_paths, d_scratch, d_stats, (cudaStream_t)stream, 0);
+}
+
+lt_status lt_engine_checkpoint(lt_engine *e, const char *path, uint64_t every, int stop)
+{
+    if (!e) return fail(LT_ERR_INVALID, "null engine");
+    if (!e->ooc) return fail(LT_ERR_UNSUPPORTED, "checkpoints apply to out-of-core engines (-p below the partition count)");
+    if (path && every == 0) return fail(LT_ERR_INVALID, "checkpoint interval must be positive");
+    return ooc_checkpoint(e->ooc, path, every, stop);
+}
+
+lt_status lt_checkpoint_read_info(const char *path, lt_checkpoint_info *out)
+{
+    if (!path || !out) return fail(LT_ERR_INVALID, "null argument");
+    return checkpoint_info(path, out);
+}
+
+lt_status lt_resume(lt_engine *e, const char *path, uint64_t *counts_out, uint32_t *endpoints_out, uint32_t *paths_out)
+{
+    if (!e || !path) return fail(LT_ERR_INVALID, "null argument");
+    if (!e->ooc) return fail(LT_ERR_UNSUPPORTED, "checkpoints apply to out-of-core engines (-p below the partition count)");
+    LT_CUDA_TRY(cudaSetDevice(e->device));
+    return ooc_resume(e, path, counts_out, endpoints_out, paths_out);
 }
 
 lt_status lt_host_alloc(uint64_t bytes, void **out)

@@ -27,6 +27,8 @@
 #include <map>
 #include <chrono>
 #include <cstring>
+#include <cstdio>
+#include <string>
 
 #include "engine.h"
 #include "lt_core.cuh"
@@ -116,6 +118,13 @@ struct Ooc {
     // zero-copy set of the next step kernel (wave runs)
     uint32_t zc_mask[kZcMaskWords] = {};
     bool zc_mask_any = false;
+    // checkpoints of runs (lt_engine_checkpoint): every ckpt_every
+    // iterations, the run stopping after the first one when ckpt_stop
+    std::string ckpt_path;
+    uint64_t ckpt_every = 0;
+    bool ckpt_stop = false;
+    uint32_t run_runs = 1, run_base = 0, run_index = 0;  // multi-run position of the run in progress
+    float run_prob = 0.f;
     int grid[3] = {0, 0, 0};
 
     std::vector<cudaEvent_t> ev_free;
@@ -994,11 +1003,28 @@ lt_status wave_step(Ooc &o, const RunParams &rp, WaveState &w, bool &done)
     return LT_OK;
 }
 
-lt_status wave_run(Ooc &o, const RunParams &rp)
+lt_status ckpt_point(Ooc &o, const RunParams &rp, bool &stop);
+
+lt_status wave_run(Ooc &o, const RunParams &rp, bool &stop)
 {
     WaveState w(o.P);
     bool done = false;
-    while (!done) LT_TRY(wave_step(o, rp, w, done));
+    stop = false;
+    while (!done) {
+        LT_TRY(wave_step(o, rp, w, done));
+        if (done) break;
+        LT_TRY(ckpt_point(o, rp, stop));
+        if (stop) {
+            // leave the cache consistent: loads in flight land and are published
+            lt_engine &e = *o.e;
+            for (auto &d : w.inflight) {
+                LT_CUDA_TRY(cudaStreamWaitEvent(e.s_compute, d.second, 0));
+                LT_TRY(set_entry(o, d.first, e.s_compute));
+            }
+            LT_CUDA_TRY(cudaStreamSynchronize(e.s_compute));
+            return LT_OK;
+        }
+    }
     return LT_OK;
 }
 
@@ -1105,30 +1131,328 @@ lt_status ooc_drop_cache(Ooc *o)
     return LT_OK;
 }
 
-lt_status ooc_run(lt_engine *e, int app, int start, uint32_t source, uint64_t W, uint32_t length, uint32_t runs,
-                  uint32_t run_base, float prob, uint64_t *counts_out, uint32_t *endpoints_out, uint32_t *paths_out)
+// ------------------------------------------------------------- checkpoints
+//
+// A checkpoint is the state of a run between two scheduler iterations: every
+// walker is then in a partition queue (device or host chunks) or not yet
+// created, so the file holds (little-endian)
+//   "LTCKPT01" | u32 version | u32 app, start, source, length, runs, run_base,
+//   run_index, flags (1 counts, 2 endpoints, 4 paths) | u64 W | f32 prob |
+//   u64 seed | u32 V | u64 E | u32 P | u64 iteration | u64 device stats[8] |
+//   counts u64[V] | endpoints u32[W] | paths u32[W (length+1)] |
+//   per partition: u64 lazy_total, lazy_next, n | u32 cur[n], step[n],
+//   idx[n], query[n].
+// The cache is not saved: a resumed run starts from a cold cache, and since
+// every draw is keyed by walker and step its results equal those of the run
+// that was never interrupted.
+namespace {
+
+constexpr char kCkptMagic[8] = {'L', 'T', 'C', 'K', 'P', 'T', '0', '1'};
+constexpr uint32_t kCkptVersion = 1;
+
+struct CkptHeader {
+    uint32_t app = 0, start = 0, source = 0, length = 0, runs = 1, run_base = 0, run_index = 0, flags = 0;
+    uint64_t W = 0;
+    float prob = 0.f;
+    uint64_t seed = 0;
+    uint32_t V = 0;
+    uint64_t E = 0;
+    uint32_t P = 0;
+    uint64_t iteration = 0;
+};
+
+struct Writer {
+    FILE *f;
+    bool ok = true;
+    void put(const void *p, size_t n) { ok = ok && (n == 0 || fwrite(p, 1, n, f) == n); }
+    void u32(uint32_t v) { put(&v, 4); }
+    void u64(uint64_t v) { put(&v, 8); }
+};
+
+struct Reader {
+    FILE *f;
+    bool ok = true;
+    void get(void *p, size_t n) { ok = ok && (n == 0 || fread(p, 1, n, f) == n); }
+    uint32_t u32()
+    {
+        uint32_t v = 0;
+        get(&v, 4);
+        return v;
+    }
+    uint64_t u64()
+    {
+        uint64_t v = 0;
+        get(&v, 8);
+        return v;
+    }
+};
+
+void put_header(Writer &w, const CkptHeader &h)
+{
+    w.put(kCkptMagic, 8);
+    w.u32(kCkptVersion);
+    for (uint32_t v : {h.app, h.start, h.source, h.length, h.runs, h.run_base, h.run_index, h.flags}) w.u32(v);
+    w.u64(h.W);
+    w.put(&h.prob, 4);
+    w.u64(h.seed);
+    w.u32(h.V);
+    w.u64(h.E);
+    w.u32(h.P);
+    w.u64(h.iteration);
+}
+
+lt_status get_header(Reader &r, const char *path, CkptHeader &h)
+{
+    char magic[8];
+    r.get(magic, 8);
+    const uint32_t version = r.u32();
+    if (!r.ok || std::memcmp(magic, kCkptMagic, 8) != 0) return fail(LT_ERR_FORMAT, "%s: not a checkpoint", path);
+    if (version != kCkptVersion) return fail(LT_ERR_FORMAT, "%s: checkpoint version %u", path, version);
+    uint32_t *f32[] = {&h.app, &h.start, &h.source, &h.length, &h.runs, &h.run_base, &h.run_index, &h.flags};
+    for (uint32_t *p : f32) *p = r.u32();
+    h.W = r.u64();
+    r.get(&h.prob, 4);
+    h.seed = r.u64();
+    h.V = r.u32();
+    h.E = r.u64();
+    h.P = r.u32();
+    h.iteration = r.u64();
+    if (!r.ok) return fail(LT_ERR_FORMAT, "%s: truncated checkpoint header", path);
+    if (h.app > kWalk || h.start > kStartPerVertex || h.run_index >= h.runs || h.W >= (1ull << 32))
+        return fail(LT_ERR_FORMAT, "%s: inconsistent checkpoint header", path);
+    return LT_OK;
+}
+
+lt_status write_checkpoint(Ooc &o, const RunParams &rp)
+{
+    lt_engine &e = *o.e;
+    lt_graph &g = *o.g;
+    LT_CUDA_TRY(cudaStreamSynchronize(e.s_compute));
+    LT_CUDA_TRY(cudaStreamSynchronize(e.s_copyback));
+    CkptHeader h;
+    h.app = rp.app;
+    h.start = rp.start;
+    h.source = rp.source;
+    h.length = rp.length;
+    h.runs = o.run_runs;
+    h.run_base = o.run_base;
+    h.run_index = o.run_index;
+    h.flags = (rp.counts ? 1u : 0u) | (rp.endpoints ? 2u : 0u) | (rp.paths ? 4u : 0u);
+    h.W = rp.W;
+    h.prob = o.run_prob;
+    h.seed = e.cfg.seed;
+    h.V = g.V;
+    h.E = g.E;
+    h.P = o.P;
+    h.iteration = o.iteration;
+    const std::string tmp = o.ckpt_path + ".tmp";
+    FILE *f = std::fopen(tmp.c_str(), "wb");
+    if (!f) return fail(LT_ERR_IO, "cannot write checkpoint %s", tmp.c_str());
+    Writer w{f};
+    put_header(w, h);
+    unsigned long long hs[8];
+    cudaError_t ce = cudaMemcpy(hs, o.d_stats, sizeof hs, cudaMemcpyDeviceToHost);
+    w.put(hs, sizeof hs);
+    if (ce == cudaSuccess && rp.counts) {
+        std::vector<uint64_t> c(g.V);
+        ce = cudaMemcpy(c.data(), rp.counts, 8ull * g.V, cudaMemcpyDeviceToHost);
+        w.put(c.data(), 8ull * g.V);
+    }
+    if (ce == cudaSuccess && rp.endpoints) {
+        std::vector<uint32_t> v(rp.W);
+        ce = cudaMemcpy(v.data(), rp.endpoints, 4ull * rp.W, cudaMemcpyDeviceToHost);
+        w.put(v.data(), 4ull * rp.W);
+    }
+    if (ce == cudaSuccess && rp.paths) {
+        const uint64_t n = rp.W * ((uint64_t)rp.length + 1);
+        std::vector<uint32_t> v(n);
+        ce = cudaMemcpy(v.data(), rp.paths, 4ull * n, cudaMemcpyDeviceToHost);
+        w.put(v.data(), 4ull * n);
+    }
+    std::vector<uint32_t> chunk(4ull * kChunk), fld[4];
+    for (uint32_t p = 0; p < o.P && ce == cudaSuccess && w.ok; p++) {
+        const Queue &q = o.q[p];
+        for (auto &v : fld) v.clear();
+        auto take = [&](const uint32_t *c, uint32_t m) {
+            for (int k = 0; k < 4; k++) fld[k].insert(fld[k].end(), c + (uint64_t)k * kChunk, c + (uint64_t)k * kChunk + m);
+        };
+        for (size_t c = 0; c < q.dev_chunks.size() && ce == cudaSuccess; c++) {
+            ce = cudaMemcpy(chunk.data(), o.d_arena + (uint64_t)q.dev_chunks[c] * kChunkBytes, kChunkBytes,
+                            cudaMemcpyDeviceToHost);
+            take(chunk.data(), c + 1 == q.dev_chunks.size() ? q.tail_fill : kChunk);
+        }
+        for (uint32_t hc : q.host_chunks) take(reinterpret_cast<const uint32_t *>(o.host_chunk(hc)), kChunk);
+        w.u64(q.lazy_total);
+        w.u64(q.lazy_next);
+        w.u64(fld[0].size());
+        for (auto &v : fld) w.put(v.data(), 4ull * v.size());
+    }
+    const bool ok = w.ok && std::fclose(f) == 0 && ce == cudaSuccess;
+    if (!ok) {
+        std::remove(tmp.c_str());
+        if (ce != cudaSuccess) return fail(LT_ERR_CUDA, "checkpoint copy: %s", cudaGetErrorString(ce));
+        return fail(LT_ERR_IO, "short write of checkpoint %s", tmp.c_str());
+    }
+    if (std::rename(tmp.c_str(), o.ckpt_path.c_str()) != 0)
+        return fail(LT_ERR_IO, "cannot move checkpoint into %s", o.ckpt_path.c_str());
+    return LT_OK;
+}
+
+// Rebuild the queues of a checkpoint: full chunks on the device while room
+// is left (else spilled to host), each partition's partial chunk last on the
+// device.
+lt_status read_queues(Ooc &o, Reader &r, const char *path)
+{
+    const uint64_t reserve = (uint64_t)o.P + 2;
+    HostBuf stage;
+    LT_TRY(host_alloc(stage, kChunkBytes, true));
+    uint32_t *sc = static_cast<uint32_t *>(stage.ptr);
+    std::vector<uint32_t> fld[4];
+    lt_status st = LT_OK;
+    for (uint32_t p = 0; p < o.P && st == LT_OK; p++) {
+        Queue &q = o.q[p];
+        q.lazy_total = r.u64();
+        q.lazy_next = r.u64();
+        const uint64_t n = r.u64();
+        if (!r.ok || q.lazy_next > q.lazy_total || n > (1ull << 32)) {
+            st = fail(LT_ERR_FORMAT, "%s: truncated or inconsistent queue of partition %u", path, p);
+            break;
+        }
+        for (auto &v : fld) {
+            v.resize(n);
+            r.get(v.data(), 4ull * n);
+        }
+        if (!r.ok) {
+            st = fail(LT_ERR_FORMAT, "%s: truncated queue of partition %u", path, p);
+            break;
+        }
+        for (uint64_t b = 0; b < n && st == LT_OK; b += kChunk) {
+            const uint32_t m = (uint32_t)std::min<uint64_t>(kChunk, n - b);
+            const bool last = b + m == n;
+            if (m == kChunk && !last && o.free_chunks.size() <= reserve + 1) {
+                uint32_t hid;
+                st = host_chunk_alloc(o, hid);
+                if (st != LT_OK) break;
+                uint32_t *hc = reinterpret_cast<uint32_t *>(o.host_chunk(hid));
+                for (int k = 0; k < 4; k++) std::memcpy(hc + (uint64_t)k * kChunk, fld[k].data() + b, 4ull * kChunk);
+                q.host_chunks.push_back(hid);
+                continue;
+            }
+            if (o.free_chunks.empty()) {
+                st = fail(LT_ERR_CAPACITY, "walker pool too small for the checkpoint's queues");
+                break;
+            }
+            for (int k = 0; k < 4; k++) std::memcpy(sc + (uint64_t)k * kChunk, fld[k].data() + b, 4ull * m);
+            const uint32_t c = o.free_chunks.back();
+            o.free_chunks.pop_back();
+            if (cudaMemcpy(o.d_arena + (uint64_t)c * kChunkBytes, sc, kChunkBytes, cudaMemcpyHostToDevice) != cudaSuccess) {
+                cudaGetLastError();
+                st = fail(LT_ERR_CUDA, "checkpoint upload failed");
+                break;
+            }
+            q.dev_chunks.push_back(c);
+            q.tail_fill = m;
+        }
+        refresh(o, p);
+    }
+    host_free(stage);
+    return st;
+}
+
+}  // namespace
+
+namespace {
+
+lt_status ckpt_point(Ooc &o, const RunParams &rp, bool &stop)
+{
+    stop = false;
+    if (o.ckpt_every == 0 || o.ckpt_path.empty() || o.iteration % o.ckpt_every != 0) return LT_OK;
+    LT_TRY(write_checkpoint(o, rp));
+    stop = o.ckpt_stop;
+    return LT_OK;
+}
+
+// Queues of a fresh run: the start mode's walkers, not yet created (source,
+// per-vertex) or created and bucketed right away (uniform starts,
+// createWalkers).
+lt_status run_prepare(Ooc &o, const RunParams &rp)
+{
+    lt_graph &g = *o.g;
+    reset_queues(o);
+    refresh_all(o);
+    o.prev_computed = -1;
+    if (rp.start == kStartSource) {
+        o.q[g.find_partition(rp.source)].lazy_total = rp.W;
+    } else if (rp.start == kStartPerVertex) {
+        const uint64_t wraps = rp.W / g.V, rem = rp.W % g.V;
+        for (uint32_t p = 0; p < o.P; p++) {
+            const uint64_t nb = g.node_off[p], n = g.node_off[p + 1] - nb;
+            const uint64_t tail = rem > nb ? std::min<uint64_t>(rem - nb, n) : 0;
+            o.q[p].lazy_total = wraps * n + tail;
+        }
+    } else {
+        uint64_t made = 0;
+        while (made < rp.W) {
+            uint64_t G = lazy_budget(o, -1, rp.W - made);
+            if (G == 0) {
+                LT_TRY(spill_until(o, (uint64_t)o.P + 2 + 1, -1));
+                G = lazy_budget(o, -1, rp.W - made);
+                if (G == 0) return fail(LT_ERR_CAPACITY, "walker pool too small to create walkers");
+            }
+            LT_TRY(step_and_bucket(o, rp, -1, lazy_of(o, rp, -1, made, G), false, nullptr));
+            made += G;
+        }
+    }
+    refresh_all(o);
+    return LT_OK;
+}
+
+// The scheduler loop of one run; stop = the run ended at a checkpoint.
+lt_status run_loop(Ooc &o, const RunParams &rp, bool &stop)
+{
+    stop = false;
+    if (o.policy->wave()) return wave_run(o, rp, stop);
+    // Scheduler::start (src/Scheduler.h:425-438)
+    bool sync = false;
+    uint32_t p = 0;
+    SchedView v = view(o);
+    while (o.policy->next(v, o.prev_computed, sync, p)) {
+        sync = false;
+        do {
+            LT_TRY(process(o, rp, p));
+            LT_TRY(ckpt_point(o, rp, stop));
+            if (stop) return LT_OK;
+            v = view(o);
+        } while (o.policy->next(v, o.prev_computed, false, p));
+        sync = true;
+        v = view(o);
+    }
+    return LT_OK;
+}
+
+// Device buffers and parameters of a call.
+lt_status run_setup(lt_engine *e, RunParams &rp, int app, int start, uint32_t source, uint64_t W, uint32_t length,
+                    float prob, bool endpoints, bool paths)
 {
     Ooc &o = *e->ooc;
     lt_graph &g = *e->g;
     if (W >= (1ull << 32)) return fail(LT_ERR_INVALID, "out-of-core runs take fewer than 2^32 walkers per run");
-    if (runs == 0) runs = 1;
     LT_TRY(ensure_pool(o, W));
     e->stats = lt_stats{};
-    const double t0 = now_ms();
     cudaStream_t st = e->s_compute;
     if (app != kWalk) LT_CUDA_TRY(cudaMemsetAsync(e->d_counts, 0, 8ull * g.V, st));
     LT_CUDA_TRY(cudaMemsetAsync(o.d_stats, 0, 64, st));
-    if (endpoints_out) {
+    if (endpoints) {
         LT_CUDA_TRY(cudaFree(e->d_endpoints));
         e->d_endpoints = nullptr;
         LT_TRY(dalloc(&e->d_endpoints, W));
     }
-    if (paths_out) {
+    if (paths) {
         LT_CUDA_TRY(cudaFree(e->d_paths));
         e->d_paths = nullptr;
         LT_TRY(dalloc(&e->d_paths, W * ((uint64_t)length + 1)));
     }
-    RunParams rp{};
+    rp = RunParams{};
     rp.app = app;
     rp.start = start;
     rp.source = source;
@@ -1136,61 +1460,40 @@ lt_status ooc_run(lt_engine *e, int app, int start, uint32_t source, uint64_t W,
     rp.W = W;
     rp.thr = app == kWalk ? 0 : threshold53(prob);
     rp.counts = app == kWalk ? nullptr : e->d_counts;
-    rp.endpoints = endpoints_out ? e->d_endpoints : nullptr;
-    rp.paths = paths_out ? e->d_paths : nullptr;
-    for (uint32_t r = 0; r < runs; r++) {
+    rp.endpoints = endpoints ? e->d_endpoints : nullptr;
+    rp.paths = paths ? e->d_paths : nullptr;
+    return LT_OK;
+}
+
+// Runs run_index .. runs-1 (the first continuing from its queues when
+// `resumed`), then the outputs.
+lt_status run_all(lt_engine *e, RunParams &rp, uint32_t runs, uint32_t run_base, uint32_t first, bool resumed,
+                  double t0, uint64_t *counts_out, uint32_t *endpoints_out, uint32_t *paths_out)
+{
+    Ooc &o = *e->ooc;
+    lt_graph &g = *e->g;
+    cudaStream_t st = e->s_compute;
+    for (uint32_t r = first; r < runs; r++) {
         rp.run = run_base + r;
-        reset_queues(o);
-        refresh_all(o);
-        o.prev_computed = -1;
-        if (start == kStartSource) {
-            o.q[g.find_partition(source)].lazy_total = W;
-        } else if (start == kStartPerVertex) {
-            const uint64_t wraps = W / g.V, rem = W % g.V;
-            for (uint32_t p = 0; p < o.P; p++) {
-                const uint64_t nb = g.node_off[p], n = g.node_off[p + 1] - nb;
-                const uint64_t tail = rem > nb ? std::min<uint64_t>(rem - nb, n) : 0;
-                o.q[p].lazy_total = wraps * n + tail;
-            }
-        } else {
-            // uniform starts: create and bucket them first (createWalkers)
-            uint64_t made = 0;
-            while (made < W) {
-                uint64_t G = lazy_budget(o, -1, W - made);
-                if (G == 0) {
-                    LT_TRY(spill_until(o, (uint64_t)o.P + 2 + 1, -1));
-                    G = lazy_budget(o, -1, W - made);
-                    if (G == 0) return fail(LT_ERR_CAPACITY, "walker pool too small to create walkers");
-                }
-                LT_TRY(step_and_bucket(o, rp, -1, lazy_of(o, rp, -1, made, G), false, nullptr));
-                made += G;
-            }
-        }
-        refresh_all(o);
-        if (o.policy->wave()) {
-            LT_TRY(wave_run(o, rp));
-            continue;
-        }
-        // Scheduler::start (src/Scheduler.h:425-438)
-        bool sync = false;
-        uint32_t p = 0;
-        SchedView v = view(o);
-        while (o.policy->next(v, o.prev_computed, sync, p)) {
-            sync = false;
-            do {
-                LT_TRY(process(o, rp, p));
-                v = view(o);
-            } while (o.policy->next(v, o.prev_computed, false, p));
-            sync = true;
-            v = view(o);
+        o.run_index = r;
+        if (!(resumed && r == first)) LT_TRY(run_prepare(o, rp));
+        bool stop = false;
+        LT_TRY(run_loop(o, rp, stop));
+        if (stop) {
+            LT_CUDA_TRY(cudaStreamSynchronize(st));
+            LT_CUDA_TRY(cudaStreamSynchronize(e->s_copy));
+            drain_timers(o, true);
+            return fail(LT_INTERRUPTED, "run stopped at the checkpoint %s (iteration %llu)", o.ckpt_path.c_str(),
+                        (unsigned long long)o.iteration);
         }
     }
     unsigned long long hs[8];
     LT_CUDA_TRY(cudaMemcpyAsync(hs, o.d_stats, sizeof hs, cudaMemcpyDeviceToHost, st));
-    if (counts_out) LT_CUDA_TRY(cudaMemcpyAsync(counts_out, e->d_counts, 8ull * g.V, cudaMemcpyDeviceToHost, st));
-    if (endpoints_out) LT_CUDA_TRY(cudaMemcpyAsync(endpoints_out, e->d_endpoints, 4 * W, cudaMemcpyDeviceToHost, st));
-    if (paths_out)
-        LT_CUDA_TRY(cudaMemcpyAsync(paths_out, e->d_paths, 4 * W * ((uint64_t)length + 1), cudaMemcpyDeviceToHost, st));
+    if (counts_out && rp.counts) LT_CUDA_TRY(cudaMemcpyAsync(counts_out, rp.counts, 8ull * g.V, cudaMemcpyDeviceToHost, st));
+    if (endpoints_out && rp.endpoints)
+        LT_CUDA_TRY(cudaMemcpyAsync(endpoints_out, rp.endpoints, 4 * rp.W, cudaMemcpyDeviceToHost, st));
+    if (paths_out && rp.paths)
+        LT_CUDA_TRY(cudaMemcpyAsync(paths_out, rp.paths, 4 * rp.W * ((uint64_t)rp.length + 1), cudaMemcpyDeviceToHost, st));
     LT_CUDA_TRY(cudaStreamSynchronize(st));
     LT_CUDA_TRY(cudaStreamSynchronize(e->s_copy));
     drain_timers(o, true);
@@ -1201,6 +1504,122 @@ lt_status ooc_run(lt_engine *e, int app, int start, uint32_t source, uint64_t W,
     e->stats.handoffs = hs[4];
     e->stats.running_ms = now_ms() - t0;
     return LT_OK;
+}
+
+}  // namespace
+
+lt_status ooc_run(lt_engine *e, int app, int start, uint32_t source, uint64_t W, uint32_t length, uint32_t runs,
+                  uint32_t run_base, float prob, uint64_t *counts_out, uint32_t *endpoints_out, uint32_t *paths_out)
+{
+    Ooc &o = *e->ooc;
+    if (runs == 0) runs = 1;
+    const double t0 = now_ms();
+    RunParams rp;
+    LT_TRY(run_setup(e, rp, app, start, source, W, length, prob, endpoints_out != nullptr, paths_out != nullptr));
+    o.run_runs = runs;
+    o.run_base = run_base;
+    o.run_prob = prob;
+    return run_all(e, rp, runs, run_base, 0, false, t0, counts_out, endpoints_out, paths_out);
+}
+
+lt_status ooc_checkpoint(Ooc *o, const char *path, uint64_t every, int stop)
+{
+    o->ckpt_path = path ? path : "";
+    o->ckpt_every = path ? every : 0;
+    o->ckpt_stop = stop != 0;
+    return LT_OK;
+}
+
+lt_status checkpoint_info(const char *path, lt_checkpoint_info *out)
+{
+    FILE *f = std::fopen(path, "rb");
+    if (!f) return fail(LT_ERR_IO, "cannot open checkpoint %s", path);
+    Reader r{f};
+    CkptHeader h;
+    const lt_status s = get_header(r, path, h);
+    std::fclose(f);
+    if (s != LT_OK) return s;
+    out->app = (int)h.app;
+    out->start_mode = (int)h.start;
+    out->source = h.source;
+    out->length = h.length;
+    out->runs = h.runs;
+    out->run_index = h.run_index;
+    out->num_walkers = h.W;
+    out->num_nodes = h.V;
+    out->has_endpoints = (h.flags & 2u) ? 1 : 0;
+    out->has_paths = (h.flags & 4u) ? 1 : 0;
+    out->iteration = h.iteration;
+    return LT_OK;
+}
+
+lt_status ooc_resume(lt_engine *e, const char *path, uint64_t *counts_out, uint32_t *endpoints_out, uint32_t *paths_out)
+{
+    Ooc &o = *e->ooc;
+    lt_graph &g = *e->g;
+    FILE *f = std::fopen(path, "rb");
+    if (!f) return fail(LT_ERR_IO, "cannot open checkpoint %s", path);
+    Reader r{f};
+    CkptHeader h;
+    lt_status s = get_header(r, path, h);
+    if (s == LT_OK && (h.V != g.V || h.E != g.E || h.P != o.P))
+        s = fail(LT_ERR_INVALID, "%s: checkpoint of another graph (V %u, E %llu, %u partitions)", path, h.V,
+                 (unsigned long long)h.E, h.P);
+    const double t0 = now_ms();
+    RunParams rp;
+    if (s == LT_OK)
+        s = run_setup(e, rp, (int)h.app, (int)h.start, h.source, h.W, h.length, h.prob, (h.flags & 2u) != 0,
+                      (h.flags & 4u) != 0);
+    unsigned long long hs[8];
+    if (s == LT_OK) {
+        r.get(hs, sizeof hs);
+        std::vector<uint64_t> c;
+        std::vector<uint32_t> v;
+        if (rp.counts) {
+            c.resize(g.V);
+            r.get(c.data(), 8ull * g.V);
+        }
+        if (r.ok && rp.counts && cudaMemcpy(rp.counts, c.data(), 8ull * g.V, cudaMemcpyHostToDevice) != cudaSuccess)
+            s = fail(LT_ERR_CUDA, "checkpoint upload failed");
+        if (s == LT_OK && rp.endpoints) {
+            v.resize(h.W);
+            r.get(v.data(), 4ull * h.W);
+            if (r.ok && cudaMemcpy(rp.endpoints, v.data(), 4ull * h.W, cudaMemcpyHostToDevice) != cudaSuccess)
+                s = fail(LT_ERR_CUDA, "checkpoint upload failed");
+        }
+        if (s == LT_OK && rp.paths) {
+            const uint64_t n = h.W * ((uint64_t)h.length + 1);
+            v.resize(n);
+            r.get(v.data(), 4ull * n);
+            if (r.ok && cudaMemcpy(rp.paths, v.data(), 4ull * n, cudaMemcpyHostToDevice) != cudaSuccess)
+                s = fail(LT_ERR_CUDA, "checkpoint upload failed");
+        }
+        if (s == LT_OK && !r.ok) s = fail(LT_ERR_FORMAT, "%s: truncated checkpoint", path);
+        if (s == LT_OK && cudaMemcpy(o.d_stats, hs, sizeof hs, cudaMemcpyHostToDevice) != cudaSuccess)
+            s = fail(LT_ERR_CUDA, "checkpoint upload failed");
+    }
+    if (s == LT_OK) {
+        reset_queues(o);
+        s = read_queues(o, r, path);
+    }
+    std::fclose(f);
+    if (s != LT_OK) {
+        reset_queues(o);
+        refresh_all(o);
+        return s;
+    }
+    refresh_all(o);
+    o.prev_computed = -1;
+    o.run_runs = h.runs;
+    o.run_base = h.run_base;
+    o.run_prob = h.prob;
+    o.iteration = h.iteration;
+    // the walks continue with the checkpoint's random stream
+    const uint64_t seed = e->cfg.seed;
+    e->cfg.seed = h.seed;
+    s = run_all(e, rp, h.runs, h.run_base, h.run_index, true, t0, counts_out, endpoints_out, paths_out);
+    e->cfg.seed = seed;
+    return s;
 }
 
 }  // namespace lt

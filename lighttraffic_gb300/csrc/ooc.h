@@ -39,6 +39,11 @@ void ooc_policy_stats(const Ooc *o, lt_policy_stats &s);
 lt_status ooc_run(lt_engine *e, int app, int start, uint32_t source, uint64_t W, uint32_t length, uint32_t runs,
                   uint32_t run_base, float prob, uint64_t *counts_out, uint32_t *endpoints_out, uint32_t *paths_out);
 
+lt_status ooc_checkpoint(Ooc *o, const char *path, uint64_t every, int stop);
+lt_status ooc_resume(lt_engine *e, const char *path, uint64_t *counts_out, uint32_t *endpoints_out,
+                     uint32_t *paths_out);
+lt_status checkpoint_info(const char *path, lt_checkpoint_info *out);
+
 // Serving: PPR queries admitted, stepped and completed continuously.
 lt_status serve_open(lt_engine *e, uint32_t max_active, uint64_t table_slots, float prob, lt_server **out);
 lt_status serve_submit(lt_server *s, uint32_t source, uint64_t walkers, uint64_t seed, double arrival_ms,

@@ -67,3 +67,11 @@ def test_compact_rejects_counter_overflow(lt):
     rc = lt.lib.lt_walk_device_compact(0, 0, fake, fake, 10, 0, 1 << 32, 0, ctypes.c_float(0.15), 0, 1, fake,
                                        None, None, fake, None, None)
     assert rc == 1 and b"overflow u32" in lt.lib.lt_last_error()
+
+
+def test_checkpoint_info_rejects_bad_files(lt, tmp_path):
+    info = lt.CheckpointInfo()
+    assert lt.lib.lt_checkpoint_read_info(str(tmp_path / "missing").encode(), ctypes.byref(info)) == 2   # LT_ERR_IO
+    bad = tmp_path / "bad.ckpt"
+    bad.write_bytes(b"not a checkpoint at all")
+    assert lt.lib.lt_checkpoint_read_info(str(bad).encode(), ctypes.byref(info)) == 3     # LT_ERR_FORMAT
