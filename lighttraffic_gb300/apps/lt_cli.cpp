@@ -39,6 +39,9 @@ struct Opts {
     int pipeline = 1;
     unsigned long long zc = UINT64_MAX;
     std::string counts_out, endpoints_out, paths_out;
+    std::string checkpoint, resume;
+    unsigned long long checkpoint_every = 100;
+    bool checkpoint_stop = false;
 };
 
 [[noreturn]] void usage(const char *argv0, const char *msg)
@@ -47,7 +50,8 @@ struct Opts {
     fprintf(stderr,
             "usage: %s -f G.bcsr [-m] [-s MB] [-p P] [-b B] [-w W] [-l L] [--runs R] [--source v] [--prob p]\n"
             "          [--seed S] [--start uniform|pervertex] [--alpha a] [--sched plain|fifo|learned|frequency|batched]\n"
-            "          [--no-pipeline] [--zerocopy-threshold N] [--counts-out F] [--endpoints-out F] [--paths-out F]\n",
+            "          [--no-pipeline] [--zerocopy-threshold N] [--counts-out F] [--endpoints-out F] [--paths-out F]\n"
+            "          [--checkpoint F [--checkpoint-every N] [--stop-at-checkpoint]] [--resume F]\n",
             argv0);
     exit(2);
 }
@@ -114,6 +118,10 @@ Opts parse(int argc, char **argv)
         else if (a == "--counts-out") o.counts_out = next();
         else if (a == "--endpoints-out") o.endpoints_out = next();
         else if (a == "--paths-out") o.paths_out = next();
+        else if (a == "--checkpoint") o.checkpoint = next();
+        else if (a == "--checkpoint-every") o.checkpoint_every = strtoull(next().c_str(), nullptr, 0);
+        else if (a == "--stop-at-checkpoint") o.checkpoint_stop = true;
+        else if (a == "--resume") o.resume = next();
         else if (a == "-h" || a == "--help") usage(argv[0], nullptr);
         else usage(argv[0], ("unknown option " + a).c_str());
     }
@@ -145,7 +153,16 @@ int main(int argc, char **argv)
     if (s != LT_OK) return die(s);
     lt_graph_info gi;
     lt_graph_info_get(g, &gi);
-    const uint64_t W = o.walkers > 0 ? (uint64_t)o.walkers : 2ull * gi.num_nodes;
+    lt_checkpoint_info ci{};
+    if (!o.resume.empty()) {
+        s = lt_checkpoint_read_info(o.resume.c_str(), &ci);
+        if (s != LT_OK) return die(s);
+        if (ci.app != LT_CLI_APP) {
+            fprintf(stderr, "error: %s was written by another app\n", o.resume.c_str());
+            return 1;
+        }
+    }
+    const uint64_t W = !o.resume.empty() ? ci.num_walkers : o.walkers > 0 ? (uint64_t)o.walkers : 2ull * gi.num_nodes;
     printf("num nodes: %u, num edges: %lu, num walkers: %lu\n", gi.num_nodes, (unsigned long)gi.num_edges,
            (unsigned long)W);
 
@@ -167,9 +184,40 @@ int main(int argc, char **argv)
            (unsigned long)(gi.partition_bytes * (cached < gi.num_partitions ? cached : gi.num_partitions) / 1024 / 1024),
            (unsigned long)(dev_walkers * walker_bytes / 1024 / 1024));
 
+    if (!o.checkpoint.empty()) {
+        s = lt_engine_checkpoint(e, o.checkpoint.c_str(), o.checkpoint_every, o.checkpoint_stop ? 1 : 0);
+        if (s != LT_OK) return die(s);
+    }
     std::vector<uint64_t> counts;
     const uint64_t *rowptr = nullptr;
     lt_graph_csr(g, &rowptr, nullptr);
+#if LT_CLI_APP == 2
+    std::vector<uint32_t> endpoints, paths;
+    lt_stats acc{};
+#endif
+    if (!o.resume.empty()) {
+        // finish the run saved in the checkpoint (one run for genericwalk)
+#if LT_CLI_APP != 2
+        counts.resize(gi.num_nodes);
+        s = lt_resume(e, o.resume.c_str(), counts.data(), nullptr, nullptr);
+#else
+        endpoints.resize(ci.has_endpoints ? W : 0);
+        paths.resize(ci.has_paths ? W * (uint64_t)(ci.length + 1) : 0);
+        s = lt_resume(e, o.resume.c_str(), nullptr, endpoints.empty() ? nullptr : endpoints.data(),
+                      paths.empty() ? nullptr : paths.data());
+        if (s == LT_OK && !o.endpoints_out.empty() && !endpoints.empty() &&
+            !dump(o.endpoints_out, endpoints.data(), 4 * endpoints.size()))
+            fprintf(stderr, "cannot write %s\n", o.endpoints_out.c_str());
+        if (s == LT_OK && !o.paths_out.empty() && !paths.empty() && !dump(o.paths_out, paths.data(), 4 * paths.size()))
+            fprintf(stderr, "cannot write %s\n", o.paths_out.c_str());
+        if (s == LT_OK) {
+            printf("resumed run finished\n");
+            lt_engine_destroy(e);
+            lt_graph_close(g);
+            return 0;
+        }
+#endif
+    } else {
 #if LT_CLI_APP == 0
     counts.resize(gi.num_nodes);
     s = lt_run_ppr(e, (uint32_t)o.source, W, (float)o.prob, counts.data());
@@ -177,9 +225,8 @@ int main(int argc, char **argv)
     counts.resize(gi.num_nodes);
     s = lt_run_pagerank(e, W, (uint32_t)o.length, (uint32_t)o.runs, (float)o.alpha, o.start, counts.data());
 #else
-    std::vector<uint32_t> endpoints(o.endpoints_out.empty() ? 0 : W);
-    std::vector<uint32_t> paths(o.paths_out.empty() ? 0 : W * (uint64_t)(o.length + 1));
-    lt_stats acc{};
+    endpoints.resize(o.endpoints_out.empty() ? 0 : W);
+    paths.resize(o.paths_out.empty() ? 0 : W * (uint64_t)(o.length + 1));
     for (long long r = 0; r < o.runs && s == LT_OK; r++) {
         s = lt_run_walk(e, W, (uint32_t)o.length, (uint32_t)r, o.start, endpoints.empty() ? nullptr : endpoints.data(),
                         paths.empty() ? nullptr : paths.data());
@@ -194,6 +241,11 @@ int main(int argc, char **argv)
         acc.computing_calls += st.computing_calls;
     }
 #endif
+    }
+    if (s == LT_INTERRUPTED) {
+        printf("interrupted at checkpoint %s\n", o.checkpoint.c_str());
+        return 4;
+    }
     if (s != LT_OK) return die(s);
     lt_stats st;
     lt_engine_stats(e, &st);

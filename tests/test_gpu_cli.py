@@ -64,3 +64,20 @@ def test_pagerank_and_walk_binaries(lt, require_gpu, bcsr, tmp_path):
     paths = np.fromfile(str(tmp_path / "p"), dtype=np.uint32)
     _, want, _ = oracle.generic_walk(rp, col, 1000, length=5, start_mode=oracle.START_PER_VERTEX, seed=4, paths=True)
     assert (paths == want).all()
+
+
+def test_ppr_binary_checkpoint_and_resume(lt, require_gpu, bcsr, tmp_path):
+    """--checkpoint ... --stop-at-checkpoint ends the run (exit 4); --resume on
+    another cache size finishes it with the counts of an uninterrupted run."""
+    path, rp, col = bcsr
+    ck = str(tmp_path / "run.ckpt")
+    out = str(tmp_path / "counts.u64")
+    r = _run(lt, "ppr", "-f", path, "-m", "-s", "1", "-p", "3", "-w", "200000", "--seed", "9",
+             "--checkpoint", ck, "--checkpoint-every", "4", "--stop-at-checkpoint")
+    assert r.returncode == 4, r.stdout + r.stderr
+    assert "interrupted at checkpoint" in r.stdout and os.path.exists(ck)
+    r = _run(lt, "ppr", "-f", path, "-p", "2", "--resume", ck, "--counts-out", out)
+    assert r.returncode == 0, r.stderr
+    assert "result correct" in r.stdout
+    want, _, _ = oracle.ppr(rp, col, 0, 200000, prob=0.15, seed=9)
+    assert (np.fromfile(out, dtype=np.uint64) == want).all()
