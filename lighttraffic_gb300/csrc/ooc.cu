@@ -1,6 +1,7 @@
 // ooc.cu -- out-of-core run loop.
 //
-// One iteration (GPUScheduler::run, src/Scheduler.h:311-330):
+// Reference loop (plain, FIFO), one iteration per partition
+// (GPUScheduler::run, src/Scheduler.h:311-330):
 //   1. the policy picks partition p;
 //   2. p is made readable: loaded into a cache slot (evicting the policy's
 //      victim) or, below the zero-copy threshold, read from pinned host memory
@@ -8,18 +9,17 @@
 //   3. p's spilled walkers come back from the host (walkerLoadingPhase,
 //      :215-233), evicting other partitions' walkers to the host if the
 //      device pool is short (handleWalkerPoolOverflow, :59-82);
-//   4. the policy may start loading partitions it expects to need next into
-//      free or evictable slots; the copies overlap the step kernel
-//      (the reference overlaps loads with computing other cached partitions,
-//      :194-208);
-//   5. one step-kernel launch drains p's queue (and creates the walkers that
+//   4. one step-kernel launch drains p's queue (and creates the walkers that
 //      start in p), walking every walker through all readable partitions;
-//   6. walkers that leave for an unreadable partition are bucketed into their
+//   5. walkers that leave for an unreadable partition are bucketed into their
 //      destination queues by the scatter kernel, into chunks allocated here.
+// Wave runs (learned, frequency, batched; wave_step) drain every cached queue
+// per launch while the next loads stream in -- see the comment at wave_step.
 // Queue bookkeeping lives on the host (exact counts, no per-decision D2H of
 // queue metadata as in src/buffer/Pool.h:604-606); per iteration one small
-// D2H (the destination histogram) and one small H2D (the chunk plan) cross
-// the link.
+// D2H (the destination histogram) crosses the link, and the work list and
+// chunk plan go up by a kernel reading mapped pinned memory.  Checkpoints and
+// resume of runs, and the serving loop, are at the end of the file.
 #include "ooc.h"
 
 #include <algorithm>
@@ -289,7 +289,7 @@ int32_t free_slot(Ooc &o)
 // after every compute operation enqueued so far (the slot's previous occupant
 // may still be read by them).  The table entry is published on the compute
 // stream once the copy is done: right away (the next kernel waits for the
-// copy), or, for prefetches, after the kernel about to be launched.
+// copy), or, for the loads of a wave, before the next wave's kernel.
 lt_status start_load(Ooc &o, uint32_t p, int32_t slot, std::vector<std::pair<uint32_t, cudaEvent_t>> *deferred)
 {
     lt_engine &e = *o.e;
