@@ -777,7 +777,10 @@ uint64_t wave_lazy_budget(Ooc &o, uint64_t chunks, uint64_t walkers, uint64_t le
 }
 
 constexpr uint64_t kSweepWalkers = 1ull << 18;    // about one walker per resident lane
-constexpr uint64_t kZcGroupBytes = 128ull << 20;  // zero-copy group: host bytes touched, about the L2
+// zero-copy group: estimated host bytes its walkers touch.  Measured on the
+// 2^33-edge graph: 128 MB 1.73 s, 256 MB 1.67 s, 512 MB 1.65 s per run (one
+// kernel over every partition with tens of millions of walkers: 6.9 s)
+constexpr uint64_t kZcGroupBytes = 512ull << 20;
 
 // Wave run.  Iteration i: publish the loads started in iteration i-1; drain,
 // in one step kernel, the queues of every cached partition (the ones just
@@ -932,10 +935,10 @@ lt_status wave_step(Ooc &o, const RunParams &rp, WaveState &w, bool &done)
 
         // Nothing worth a load and no room for new walkers: read partitions
         // outside the cache zero-copy.  Zero-copy hops are fast only while
-        // the host lines they touch stay in L2, so the partitions go in groups
-        // whose estimated footprint is about the L2, most waiting walkers
-        // first; once few walkers are left, one sweep makes every partition
-        // readable and finishes them in a single, latency-bound kernel.
+        // the host lines they touch stay cached, so the partitions go in
+        // groups of bounded estimated footprint, most waiting walkers first;
+        // once few walkers are left, one sweep makes every partition readable
+        // and finishes them in a single, latency-bound kernel.
         std::memset(o.zc_mask, 0, sizeof o.zc_mask);
         o.zc_mask_any = false;
         bool lazy_left = false;
