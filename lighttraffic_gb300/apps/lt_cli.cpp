@@ -7,7 +7,8 @@
 //   --prob p  -m/--materialized-partition
 // plus: --seed S, --start uniform|pervertex, --alpha a (PageRank teleport
 // test, default 0.85 as app/pagerank.cu:6), --sched plain|fifo|learned|frequency|batched,
-// --no-pipeline, --zerocopy-threshold N, --counts-out FILE (u64[V] raw),
+// --no-pipeline, --host-index (rowptr slices travel with the partitions,
+// as in the reference), --zerocopy-threshold N, --counts-out FILE (u64[V] raw),
 // --endpoints-out FILE / --paths-out FILE (genericwalk, u32 raw).
 // Prints the reference's stdout lines (src/Config.h:92, src/LightTraffic.h:26,
 // src/Scheduler.h:441-452, app/ppr.cu:107-110, app/pagerank.cu:232-248),
@@ -37,6 +38,7 @@ struct Opts {
     int start = LT_START_UNIFORM;
     int sched = LT_SCHED_PLAIN;
     int pipeline = 1;
+    int resident_index = 1;
     unsigned long long zc = UINT64_MAX;
     std::string counts_out, endpoints_out, paths_out;
     std::string checkpoint, resume;
@@ -50,7 +52,7 @@ struct Opts {
     fprintf(stderr,
             "usage: %s -f G.bcsr [-m] [-s MB] [-p P] [-b B] [-w W] [-l L] [--runs R] [--source v] [--prob p]\n"
             "          [--seed S] [--start uniform|pervertex] [--alpha a] [--sched plain|fifo|learned|frequency|batched]\n"
-            "          [--no-pipeline] [--zerocopy-threshold N] [--counts-out F] [--endpoints-out F] [--paths-out F]\n"
+            "          [--no-pipeline] [--host-index] [--zerocopy-threshold N] [--counts-out F] [--endpoints-out F] [--paths-out F]\n"
             "          [--checkpoint F [--checkpoint-every N] [--stop-at-checkpoint]] [--resume F]\n",
             argv0);
     exit(2);
@@ -114,6 +116,7 @@ Opts parse(int argc, char **argv)
             else if (s == "batched") o.sched = LT_SCHED_BATCHED;
             else usage(argv[0], "--sched takes plain, fifo, learned, frequency or batched");
         } else if (a == "--no-pipeline") o.pipeline = 0;
+        else if (a == "--host-index") o.resident_index = 0;
         else if (a == "--zerocopy-threshold") o.zc = strtoull(next().c_str(), nullptr, 0);
         else if (a == "--counts-out") o.counts_out = next();
         else if (a == "--endpoints-out") o.endpoints_out = next();
@@ -172,6 +175,7 @@ int main(int argc, char **argv)
     cfg.num_device_walkers = o.batch > 0 ? (uint64_t)o.batch : 0;
     cfg.sched = o.sched;
     cfg.pipeline = o.pipeline;
+    cfg.resident_index = o.resident_index;
     cfg.zerocopy_threshold = o.zc;
     cfg.seed = o.seed;
     lt_engine *e = nullptr;

@@ -186,6 +186,7 @@ void lt_engine_cfg_default(lt_engine_cfg *cfg)
     cfg->seed = 0x5EED5EEDull;
     cfg->block_size = 0;
     cfg->ctas_per_sm = 0;
+    cfg->resident_index = 1;
 }
 
 lt_status lt_engine_create(lt_graph *g, const lt_engine_cfg *cfg, lt_engine **out)

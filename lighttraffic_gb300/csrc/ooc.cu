@@ -66,11 +66,13 @@ lt_status dalloc(T **p, uint64_t count)
 
 enum TimerKind { kTGraph = 0, kTCompute = 1, kTZero = 2 };
 
-// Host-link bytes per zero-copy hop, for the statistics: measured with ncu
-// (sectors the system-memory L2 filled from host memory) on the 2^33-edge
-// graph, 0.244 of the 256 bytes two 128-byte lines per hop would take --
-// hops grouped by partition share lines.
+// Host-link bytes per zero-copy hop: measured with ncu (sectors the
+// system-memory L2 filled from host memory) on the 2^33-edge graph, 0.244 of
+// the 256 bytes two 128-byte lines per hop would take -- hops grouped by
+// partition share lines.  With the vertex index on the device a hop reads
+// only its col entry from the host: one 32-byte sector (measured 31.9).
 constexpr uint64_t kZeroCopyBytesPerHop = 62;
+constexpr uint64_t kZeroCopyBytesPerHopIndexed = 32;
 
 }  // namespace
 
@@ -120,7 +122,11 @@ struct Ooc {
     int32_t prev_loaded = -1, prev_computed = -1;
     uint64_t iteration = 0;
     uint64_t zc_threshold = 0;
-    unsigned long long zc_rp_base = 0, zc_col_base = 0;  // device view of the pinned host CSR
+    unsigned long long zc_rp_base = 0, zc_col_base = 0;  // zero-copy rowptr and col bases
+    // vertex index (rowptr, V+1 u64) resident on the device: slots then hold
+    // only col slices and zero-copy hops read rowptr here; null: the
+    // reference's layout, rowptr slice then col slice in every slot
+    uint64_t *d_index = nullptr;
     // zero-copy set of the next step kernel (wave runs)
     uint32_t zc_mask[kZcMaskWords] = {};
     bool zc_mask_any = false;
@@ -192,6 +198,16 @@ void drain_timers(Ooc &o, bool all)
     }
     o.timed.resize(keep);
 }
+
+// Bytes a load of partition p copies (and its host footprint): the col
+// slice with the vertex index resident, else rowptr and col slices.
+uint64_t host_part_bytes(const Ooc &o, uint32_t p)
+{
+    const lt_graph &g = *o.g;
+    return o.d_index ? 4 * (g.edge_off[p + 1] - g.edge_off[p]) : g.slot_bytes(p);
+}
+
+uint64_t zc_bytes_per_hop(const Ooc &o) { return o.d_index ? kZeroCopyBytesPerHopIndexed : kZeroCopyBytesPerHop; }
 
 __global__ void set_entry_kernel(unsigned long long *rp, unsigned long long *col, uint32_t p, unsigned long long rv,
                                  unsigned long long cv)
@@ -291,7 +307,8 @@ int32_t free_slot(Ooc &o)
 }
 
 // GPUGraph::loadAsync (src/GraphLoader.h:193-214): the rowptr slice, then the
-// col slice at the next 16-byte boundary of slot `slot`, on the copy stream
+// col slice at the next 16-byte boundary of slot `slot` (only the col slice
+// when the vertex index is resident), on the copy stream
 // after every compute operation enqueued so far (the slot's previous occupant
 // may still be read by them).  The table entry is published on the compute
 // stream once the copy is done: right away (the next kernel waits for the
@@ -308,15 +325,15 @@ lt_status start_load(Ooc &o, uint32_t p, int32_t slot, std::vector<std::pair<uin
     const uint64_t n0 = g.node_off[p], n1 = g.node_off[p + 1];
     const uint64_t e0 = g.edge_off[p], e1 = g.edge_off[p + 1];
     uint8_t *base = o.d_slots + (uint64_t)slot * o.slot_stride;
-    const uint64_t rp_bytes = 8 * (n1 - n0 + 1);
+    const uint64_t rp_bytes = o.d_index ? 0 : 8 * (n1 - n0 + 1);
     const uint64_t col_off = (rp_bytes + 15) & ~15ull;
     Ooc::Timed t{ev_get(o), ev_get(o), kTGraph};
     LT_CUDA_TRY(cudaEventRecord(t.a, e.s_copy));
-    LT_CUDA_TRY(cudaMemcpyAsync(base, g.rowptr() + n0, rp_bytes, cudaMemcpyHostToDevice, e.s_copy));
+    if (rp_bytes) LT_CUDA_TRY(cudaMemcpyAsync(base, g.rowptr() + n0, rp_bytes, cudaMemcpyHostToDevice, e.s_copy));
     if (e1 > e0) LT_CUDA_TRY(cudaMemcpyAsync(base + col_off, g.col() + e0, 4 * (e1 - e0), cudaMemcpyHostToDevice, e.s_copy));
     LT_CUDA_TRY(cudaEventRecord(t.b, e.s_copy));
     o.timed.push_back(t);
-    o.h_rp[p] = (unsigned long long)(uintptr_t)base;
+    o.h_rp[p] = (unsigned long long)(uintptr_t)(o.d_index ? (uint8_t *)(o.d_index + n0) : base);
     o.h_col[p] = (unsigned long long)(uintptr_t)(base + col_off);
     o.slot_of[p] = slot;
     o.part_in_slot[slot] = (int32_t)p;
@@ -814,9 +831,20 @@ lt_status wave_step(Ooc &o, const RunParams &rp, WaveState &w, bool &done)
 {
     lt_engine &e = *o.e;
     const bool zc_ok = o.zc_rp_base != 0 && o.P <= kSmemPartMax && o.zc_threshold > 0;
-    // serving keeps the reference threshold and smaller zero-copy groups:
-    // shorter steps matter more there than fewer loads
-    const uint64_t load_min = zc_ok ? o.zc_threshold * (o.serve ? 1 : o.policy->wave_load_factor()) : 1;
+    // A wave loads a partition once its waiting walkers would read more host
+    // bytes zero-copy than the load copies.  The reference's threshold
+    // (partitionSize/128/2 walkers) is that break-even at 256 bytes per
+    // zero-copy hop; grouped hops cost 62 or 32 bytes, so the threshold
+    // scales by 256 / bytes per hop.  Measured per run on the 2^33-edge
+    // graph: host index 1x 1.63 s, 2x 1.49 s, 4x 1.47 s, 8x 1.64 s (6 300 /
+    // 4 900 / 3 100 / 256 loads); resident index 4x 1.30-1.41 s, 8x
+    // 1.20-1.25 s (3 100 / 256 loads).  Serving keeps the reference
+    // threshold and smaller zero-copy groups: shorter steps matter more
+    // there than fewer loads.
+    const uint64_t load_factor = o.serve ? 1 : 256 / zc_bytes_per_hop(o);
+    const uint64_t load_min = !zc_ok ? 1
+                              : o.zc_threshold > UINT64_MAX / load_factor ? UINT64_MAX
+                                                                          : o.zc_threshold * load_factor;
     const uint64_t zc_group_bytes = o.serve ? kZcGroupBytesServe : kZcGroupBytes;
     const uint64_t reserve = (uint64_t)o.P + 2;
     auto &inflight = w.inflight;
@@ -969,8 +997,11 @@ lt_status wave_step(Ooc &o, const RunParams &rp, WaveState &w, bool &done)
                     return o.waiting[a] != o.waiting[b] ? o.waiting[a] > o.waiting[b] : a < b;
                 });
                 // host bytes a partition's walkers touch: at most the partition,
-                // else about two 128-byte lines per hop, two hops per walker
-                auto footprint = [&](uint32_t p) { return std::min<uint64_t>(o.g->slot_bytes(p), 512 * o.waiting[p]); };
+                // else about two 128-byte lines per hop (one with the index
+                // resident), two hops per walker
+                auto footprint = [&](uint32_t p) {
+                    return std::min<uint64_t>(host_part_bytes(o, p), (o.d_index ? 256 : 512) * o.waiting[p]);
+                };
                 uint64_t bytes = 0;
                 size_t n = 0;
                 while (n < group.size() && (n == 0 || bytes + footprint(group[n]) <= zc_group_bytes))
@@ -1054,15 +1085,26 @@ lt_status ooc_create(lt_engine *e, Ooc **out)
     o->P = g.P();
     o->K = std::min<uint32_t>(e->cfg.num_device_partitions, o->P);
     if (o->K < 1) o->K = 1;
-    o->slot_stride = (g.part_bytes + 16 + 255) & ~255ull;
-    uint64_t max_slot = 0;
-    for (uint32_t p = 0; p < o->P; p++) max_slot = std::max<uint64_t>(max_slot, g.slot_bytes(p) + 16);
-    if (max_slot > o->slot_stride) o->slot_stride = (max_slot + 255) & ~255ull;
     o->ctl_words = o->hist_words() + 4;
     auto bail = [&](lt_status s) {
         ooc_destroy(o);
         return s;
     };
+    // The vertex index goes to the device first (8 (V+1) bytes, 2.9 GB at
+    // 2^30 vertices); where it does not fit, the slots carry rowptr slices.
+    if (e->cfg.resident_index) {
+        if (dalloc(&o->d_index, (uint64_t)g.V + 1) != LT_OK ||
+            cudaMemcpy(o->d_index, g.rowptr(), 8ull * ((uint64_t)g.V + 1), cudaMemcpyHostToDevice) != cudaSuccess) {
+            cudaGetLastError();
+            clear_error();
+            if (o->d_index) cudaFree(o->d_index);
+            o->d_index = nullptr;
+        }
+    }
+    uint64_t max_slot = 0;
+    for (uint32_t p = 0; p < o->P; p++) max_slot = std::max<uint64_t>(max_slot, host_part_bytes(*o, p) + 16);
+    o->slot_stride = (max_slot + 255) & ~255ull;
+    if (!o->d_index) o->slot_stride = std::max<uint64_t>(o->slot_stride, (g.part_bytes + 16 + 255) & ~255ull);
     lt_status s = dalloc(&o->d_slots, (uint64_t)o->K * o->slot_stride);
     if (s == LT_OK) s = dalloc(&o->d_node_off, o->P + 1);
     if (s == LT_OK) s = dalloc(&o->d_edge_off, o->P + 1);
@@ -1104,7 +1146,7 @@ lt_status ooc_create(lt_engine *e, Ooc **out)
         if (cudaHostGetDevicePointer(&rp_dev, (void *)g.rowptr(), 0) != cudaSuccess ||
             cudaHostGetDevicePointer(&col_dev, (void *)g.col(), 0) != cudaSuccess)
             return bail(fail(LT_ERR_CUDA, "pinned graph is not mapped for zero-copy reads"));
-        o->zc_rp_base = (unsigned long long)(uintptr_t)rp_dev;
+        o->zc_rp_base = (unsigned long long)(uintptr_t)(o->d_index ? (void *)o->d_index : rp_dev);
         o->zc_col_base = (unsigned long long)(uintptr_t)col_dev;
     } else {
         o->zc_threshold = 0;  // the graph is not in pinned memory: always load
@@ -1120,7 +1162,7 @@ void ooc_destroy(Ooc *o)
 {
     if (!o) return;
     drain_timers(*o, true);
-    for (void *p : {(void *)o->d_slots, (void *)o->d_node_off, (void *)o->d_edge_off, (void *)o->d_rp, (void *)o->d_col,
+    for (void *p : {(void *)o->d_index, (void *)o->d_slots, (void *)o->d_node_off, (void *)o->d_edge_off, (void *)o->d_rp, (void *)o->d_col,
                     (void *)o->d_arena, (void *)o->d_out, (void *)o->d_ctl, (void *)o->d_planbuf, (void *)o->d_work,
                     (void *)o->d_work_off, (void *)o->d_stats})
         if (p) cudaFree(p);
@@ -1515,7 +1557,7 @@ lt_status run_all(lt_engine *e, RunParams &rp, uint32_t runs, uint32_t run_base,
     e->stats.updates = hs[0];
     e->stats.moves = hs[1];
     e->stats.teleports = hs[2];
-    e->stats.zerocopy_bytes = hs[3] * kZeroCopyBytesPerHop;
+    e->stats.zerocopy_bytes = hs[3] * zc_bytes_per_hop(o);
     e->stats.handoffs = hs[4];
     e->stats.running_ms = now_ms() - t0;
     return LT_OK;
@@ -2046,7 +2088,7 @@ void serve_close(lt_server *s)
             s->e->stats.updates = hs[0];
             s->e->stats.moves = hs[1];
             s->e->stats.teleports = hs[2];
-            s->e->stats.zerocopy_bytes = hs[3] * kZeroCopyBytesPerHop;
+            s->e->stats.zerocopy_bytes = hs[3] * zc_bytes_per_hop(*s->o);
             s->e->stats.handoffs = hs[4];
         }
         if (s->wave) {

@@ -62,14 +62,6 @@ public:
     // recently used).
     virtual bool wave() const { return false; }
     virtual size_t wave_loads() const { return 8; }
-    // A wave loads a partition once its waiting walkers reach this multiple
-    // of the zero-copy threshold; below it they are read zero-copy.  The
-    // reference's threshold assumes 256 host bytes per zero-copy hop, but
-    // hops grouped by partition share host lines (measured: about a quarter
-    // of that), so fuller loads pay: on the 2^33-edge graph 1x 1.63 s, 2x
-    // 1.49 s, 4x 1.47 s, 8x 1.64 s per run, with 6 300 / 4 900 / 3 100 / 256
-    // loads.
-    virtual uint64_t wave_load_factor() const { return 4; }
     // Cache emptied (the learned state of a policy survives).
     virtual void reset() {}
     virtual void stats(lt_policy_stats &s) const

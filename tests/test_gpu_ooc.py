@@ -41,10 +41,14 @@ CASES = [
 
 
 @pytest.mark.parametrize("case", CASES)
-def test_ppr_ooc(lt, require_gpu, g16, case):
+@pytest.mark.parametrize("index", [True, False])
+def test_ppr_ooc(lt, require_gpu, g16, case, index):
+    """index: vertex index resident on the device (default) or rowptr slices
+    in the slots and read zero-copy from the host (the reference's layout)."""
     K, B, zc, sched = case
     rp, col = g16
-    g, e = _eng(lt, rp, col, 256 << 10, partitions=K, batch=B, zerocopy_threshold=zc, sched=sched, seed=9)
+    g, e = _eng(lt, rp, col, 256 << 10, partitions=K, batch=B, zerocopy_threshold=zc, sched=sched, seed=9,
+                resident_index=index)
     assert g.num_partitions > K
     W = 300000
     got = e.ppr(0, W, 0.15)
@@ -76,15 +80,36 @@ def test_pagerank_ooc(lt, require_gpu, g16, case, start):
 
 
 @pytest.mark.parametrize("case", CASES[:3] + CASES[4:5] + [(4, 0, None, 4), (3, 20000, 0, 2), (4, 0, 1 << 40, 4)])
-def test_walk_ooc(lt, require_gpu, g16, case):
+@pytest.mark.parametrize("index", [True, False])
+def test_walk_ooc(lt, require_gpu, g16, case, index):
     K, B, zc, sched = case
     rp, col = g16
     V = len(rp) - 1
-    g, e = _eng(lt, rp, col, 256 << 10, partitions=K, batch=B, zerocopy_threshold=zc, sched=sched, seed=6)
+    g, e = _eng(lt, rp, col, 256 << 10, partitions=K, batch=B, zerocopy_threshold=zc, sched=sched, seed=6,
+                resident_index=index)
     for start in (1, 2):
         ep, pa, _ = oracle.generic_walk(rp, col, V + 77, length=6, start_mode=start, run=1, seed=6, paths=True)
         gep, gpa = e.walk(V + 77, length=6, run=1, start=start, paths=True)
         assert (gep == ep).all() and (gpa == pa).all()
+
+
+@pytest.mark.parametrize("sched", [0, 4])
+def test_resident_index_loads_only_edges(lt, require_gpu, g16, sched):
+    """With the vertex index on the device a load copies only the col slice:
+    same loads and counts as the reference layout, fewer graph bytes, each
+    load at most the largest partition's col bytes."""
+    rp, col = g16
+    res = {}
+    for index in (True, False):
+        g, e = _eng(lt, rp, col, 256 << 10, partitions=3, zerocopy_threshold=0, sched=sched, seed=5,
+                    resident_index=index)
+        res[index] = (e.ppr(0, 200000, 0.15), e.stats(), g)
+    (c1, s1, g1), (c0, s0, _) = res[True], res[False]
+    assert (c1 == c0).all()
+    assert s1["partition_loads"] == s0["partition_loads"] > 0
+    assert 0 < s1["h2d_graph_bytes"] < s0["h2d_graph_bytes"]
+    eo = g1.partitions()[1].astype(np.int64)
+    assert s1["h2d_graph_bytes"] <= s1["partition_loads"] * 4 * int(np.diff(eo).max())
 
 
 def test_resident_and_ooc_agree(lt, require_gpu, g16):
