@@ -5,6 +5,11 @@ keyed by walker and step).  What the trained network gains over the method
 without it is measured on the engine's own traces: its mean squared error
 predicting per-partition visits over the next iterations, against the moving
 average of visits it replaces (the frequency policy's predictor).
+
+The network learns online, so the run must last long enough to train it:
+16 walkers per vertex give about 70 wave iterations (about 30 training
+steps).  With 8 per vertex (50 iterations, 21 steps) it had not yet caught
+up with the moving average (0.00196 vs 0.00158); at 16, 0.00141 vs 0.00200.
 """
 import pytest
 
@@ -18,7 +23,7 @@ def test_learned_matches_plain_and_beats_moving_average(lt, require_gpu):
     runs = {}
     for name, sched in [("plain", lt.SCHED_PLAIN), ("frequency", lt.SCHED_FREQUENCY), ("learned", lt.SCHED_LEARNED)]:
         e = lt.Engine(g, partitions=12, seed=1, sched=sched)
-        counts = e.ppr(0, 8 * V, 0.15)
+        counts = e.ppr(0, 16 * V, 0.15)
         s = e.stats()
         runs[name] = (counts, s, e.policy_stats())
         link = s["h2d_graph_bytes"] + s["h2d_walker_bytes"] + s["d2h_walker_bytes"] + s["zerocopy_bytes"]
@@ -27,6 +32,6 @@ def test_learned_matches_plain_and_beats_moving_average(lt, require_gpu):
     assert (runs["plain"][0] == runs["learned"][0]).all()
     assert (runs["plain"][0] == runs["frequency"][0]).all()
     ps = runs["learned"][2]
-    assert ps["name"] == "learned" and ps["train_steps"] >= 20 and ps["predictions"] >= 10
+    assert ps["name"] == "learned" and ps["train_steps"] >= 25 and ps["predictions"] >= 10
     print("network loss %.5f, moving-average loss %.5f" % (ps["net_loss"], ps["baseline_loss"]))
     assert ps["net_loss"] < ps["baseline_loss"]
