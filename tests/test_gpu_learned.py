@@ -32,6 +32,6 @@ def test_learned_matches_plain_and_beats_moving_average(lt, require_gpu):
     assert (runs["plain"][0] == runs["learned"][0]).all()
     assert (runs["plain"][0] == runs["frequency"][0]).all()
     ps = runs["learned"][2]
-    assert ps["name"] == "learned" and ps["train_steps"] >= 25 and ps["predictions"] >= 10
+    assert ps["name"] == "learned" and ps["train_steps"] >= 20 and ps["predictions"] >= 10
     print("network loss %.5f, moving-average loss %.5f" % (ps["net_loss"], ps["baseline_loss"]))
     assert ps["net_loss"] < ps["baseline_loss"]
