@@ -43,7 +43,7 @@ typedef enum lt_status {
     LT_ERR_PARTITION = 6,   /* one vertex does not fit the partition size */
     LT_ERR_TIMEOUT = 7,     /* a bounded device-side wait gave up */
     LT_ERR_CAPACITY = 8,    /* a device queue or buffer limit was exceeded */
-    LT_ERR_UNSUPPORTED = 9, /* configuration not supported by this build */
+    LT_ERR_UNSUPPORTED = 9, /* configuration this library does not support */
     LT_INTERRUPTED = 10     /* the run stopped at a checkpoint, as lt_engine_checkpoint asked */
 } lt_status;
 
