@@ -371,7 +371,7 @@ __global__ void pol_copy(float *dst, const float *src, uint32_t n)
 // Eviction scores are predicted visits (walkers entering the partition,
 // cached or not) over the next kLabelHorizon iterations plus the walkers
 // already waiting.  The network runs on its own stream; the host stages a few
-// kilobytes per iteration and picks up the forecasts of the previous round
+// kilobytes per iteration and picks up the forecasts of the previous pass
 // when they are ready, never waiting for them.
 class LearnedPolicy : public Policy {
 public:
