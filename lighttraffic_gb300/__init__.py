@@ -381,7 +381,12 @@ class Server:
 
 
 class Engine:
-    """One engine = the reference's LightTraffic<AppManager,App,Walker> object."""
+    """One engine = the reference's LightTraffic<AppManager,App,Walker> object.
+
+    partitions / batch are the reference's -p / -b.  resident_index=True
+    (default) keeps the vertex index on the device when the graph is out of
+    core, so loads and zero-copy reads move only edges; False uses the
+    reference's slot layout.  Results are identical either way."""
 
     def __init__(self, graph: Graph, partitions: int = 0, batch: int = 0, seed: int = 0x5EED5EED,
                  sched: int = SCHED_PLAIN, pipeline: bool = True, zerocopy_threshold=None,

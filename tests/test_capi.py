@@ -75,3 +75,18 @@ def test_checkpoint_info_rejects_bad_files(lt, tmp_path):
     bad = tmp_path / "bad.ckpt"
     bad.write_bytes(b"not a checkpoint at all")
     assert lt.lib.lt_checkpoint_read_info(str(bad).encode(), ctypes.byref(info)) == 3     # LT_ERR_FORMAT
+
+
+def test_engine_cfg_defaults(lt):
+    """lt_engine_cfg_default: reference threshold, pipelining on, the vertex
+    index resident on the device."""
+    cfg = lt.EngineCfg()
+    lt.lib.lt_engine_cfg_default(ctypes.byref(cfg))
+    assert cfg.pipeline == 1 and cfg.resident_index == 1
+    assert cfg.zerocopy_threshold == 2**64 - 1 and cfg.sched == 0
+
+
+def test_cli_accepts_host_index(lt):
+    exe = os.path.join(lt.BIN_DIR, "ppr")
+    r = subprocess.run([exe, "-f", "/nonexistent.bcsr", "--host-index"], capture_output=True, text=True)
+    assert r.returncode == 1 and "cannot open" in r.stderr
