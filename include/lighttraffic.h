@@ -282,14 +282,18 @@ lt_status lt_walk_device_compact(int app, int start_mode, const uint32_t *d_rowp
 lt_status lt_rowptr_narrow(const uint64_t *d_rowptr, uint32_t *d_rowptr32, uint32_t num_nodes, void *stream);
 
 /* lt_walk_device without the scratch argument, for callers that cannot
- * allocate device memory (inside a stream capture, or when a host framework
- * owns every device allocation and hands over only inputs and outputs).  No
- * counterpart in the reference.  It allocates nothing: its scratch is a
- * 256-byte static device array shared by every call in the process; the call
- * clears it on `stream` first, calls that overlap on the GPU race (order them
- * on one stream), and a scratch need above 256 bytes is rejected with
+ * allocate device memory: a plugin whose host framework owns every device
+ * allocation and hands over only inputs and outputs, or a process whose
+ * device memory another allocator has reserved in full.  No counterpart in
+ * the reference.  It allocates nothing: its scratch is a 256-byte static
+ * device array shared by every call in the process; the call clears it on
+ * `stream` first, calls that overlap on the GPU race (order them on one
+ * stream), and a scratch need above 256 bytes is rejected with
  * LT_ERR_CAPACITY.  The first call on each device looks up the array's device
- * address (cudaGetSymbolAddress); make it before any stream capture. */
+ * address (cudaGetSymbolAddress) and keeps it for the life of the process;
+ * make that first call before any stream capture begins, and do not call
+ * cudaDeviceReset on a device this entry point has used (the kept address
+ * would then be stale). */
 lt_status lt_walk_device_noalloc(int app, int start_mode, const uint64_t *d_rowptr, const uint32_t *d_col,
                                  uint32_t num_nodes, uint32_t source, uint64_t num_walkers,
                                  uint32_t length, float prob, uint32_t run, uint64_t seed,
@@ -394,6 +398,10 @@ void lt_host_free(void *p);
  * same code), for checking it against native division.  No counterpart in
  * the reference. */
 lt_status lt_mod_check(uint64_t n, const uint64_t *x, const uint64_t *d, uint64_t *out);
+/* The same remainder computed by the device build (device buffers, on
+ * `stream`; a zero divisor gives UINT64_MAX).  No counterpart in the
+ * reference. */
+lt_status lt_mod_check_device(uint64_t n, const uint64_t *d_x, const uint64_t *d_d, uint64_t *d_out, void *stream);
 
 #ifdef __cplusplus
 }

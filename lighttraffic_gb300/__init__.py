@@ -119,6 +119,7 @@ def _load():
         "lt_walk_scratch_bytes": ([], C.c_size_t),
         "lt_engine_policy_stats": ([vp, C.POINTER(PolicyStats)], C.c_int),
         "lt_mod_check": ([C.c_uint64, u64p, u64p, u64p], C.c_int),
+        "lt_mod_check_device": ([C.c_uint64, vp, vp, vp, vp], C.c_int),
         "lt_host_link_gbs": ([C.c_int, C.POINTER(C.c_double)], C.c_int),
         "lt_ppr_batch": ([vp, C.c_uint32, u32p, u64p, u64p, C.c_float, u64p, u32p, u32p, C.c_uint64], C.c_int),
         "lt_ppr_batch_device": ([vp, C.c_uint32, vp, vp, vp, C.c_float, vp, vp, vp, C.c_uint64, vp], C.c_int),

@@ -1195,17 +1195,25 @@ lt_status ooc_drop_cache(Ooc *o)
 // created, so the file holds (little-endian)
 //   "LTCKPT01" | u32 version | u32 app, start, source, length, runs, run_base,
 //   run_index, flags (1 counts, 2 endpoints, 4 paths) | u64 W | f32 prob |
-//   u64 seed | u32 V | u64 E | u32 P | u64 iteration | u64 device stats[8] |
+//   u64 seed | u32 V | u64 E | u32 P | u64 partition-table hash |
+//   u64 iteration | u64 device stats[8] |
 //   counts u64[V] | endpoints u32[W] | paths u32[W (length+1)] |
 //   per partition: u64 lazy_total, lazy_next, n | u32 cur[n], step[n],
 //   idx[n], query[n].
 // The cache is not saved: a resumed run starts from a cold cache, and since
 // every draw is keyed by walker and step its results equal those of the run
-// that was never interrupted.
+// that was never interrupted.  A file is trusted no further than it can be
+// checked: the header must describe a run the engine could have started
+// (source inside the graph, probability and length in range, the output
+// flags of the app), the partition table must hash to the engine's, each
+// partition's creation progress must be the one its start mode gives, and
+// every queued walker must lie in its partition, with an index below W and
+// a step the app can reach -- a corrupt record would otherwise become an
+// out-of-range device access in the step kernel.
 namespace {
 
 constexpr char kCkptMagic[8] = {'L', 'T', 'C', 'K', 'P', 'T', '0', '1'};
-constexpr uint32_t kCkptVersion = 1;
+constexpr uint32_t kCkptVersion = 2;
 
 struct CkptHeader {
     uint32_t app = 0, start = 0, source = 0, length = 0, runs = 1, run_base = 0, run_index = 0, flags = 0;
@@ -1215,8 +1223,25 @@ struct CkptHeader {
     uint32_t V = 0;
     uint64_t E = 0;
     uint32_t P = 0;
+    uint64_t part_hash = 0;
     uint64_t iteration = 0;
 };
+
+// FNV-1a over the partition table (partition size, node and edge offsets):
+// a checkpoint resumes only on an engine whose partitions have the same
+// boundaries, since its per-partition creation progress refers to them.
+uint64_t part_table_hash(const lt_graph &g)
+{
+    uint64_t h = 0xcbf29ce484222325ull;
+    auto mix = [&](const void *p, size_t n) {
+        const uint8_t *b = static_cast<const uint8_t *>(p);
+        for (size_t i = 0; i < n; i++) h = (h ^ b[i]) * 0x100000001b3ull;
+    };
+    mix(&g.part_bytes, sizeof g.part_bytes);
+    mix(g.node_off.data(), 4 * g.node_off.size());
+    mix(g.edge_off.data(), 8 * g.edge_off.size());
+    return h;
+}
 
 struct Writer {
     FILE *f;
@@ -1255,6 +1280,7 @@ void put_header(Writer &w, const CkptHeader &h)
     w.u32(h.V);
     w.u64(h.E);
     w.u32(h.P);
+    w.u64(h.part_hash);
     w.u64(h.iteration);
 }
 
@@ -1273,10 +1299,23 @@ lt_status get_header(Reader &r, const char *path, CkptHeader &h)
     h.V = r.u32();
     h.E = r.u64();
     h.P = r.u32();
+    h.part_hash = r.u64();
     h.iteration = r.u64();
     if (!r.ok) return fail(LT_ERR_FORMAT, "%s: truncated checkpoint header", path);
-    if (h.app > kWalk || h.start > kStartPerVertex || h.run_index >= h.runs || h.W >= (1ull << 32))
+    if (h.app > kWalk || h.start > kStartPerVertex || h.run_index >= h.runs || h.W >= (1ull << 32) || h.W == 0 ||
+        h.V == 0 || h.P == 0 || h.P > h.V)
         return fail(LT_ERR_FORMAT, "%s: inconsistent checkpoint header", path);
+    // the checks run_setup and the engine entry points make on a fresh run
+    if (h.start == kStartSource && h.source >= h.V)
+        return fail(LT_ERR_FORMAT, "%s: source %u outside the graph's %u vertices", path, h.source, h.V);
+    if (h.app == kPPR && !(h.prob > 0.0f && h.prob <= 1.0f))
+        return fail(LT_ERR_FORMAT, "%s: PPR stop probability outside (0, 1]", path);
+    if (h.app == kPageRank && !(h.prob >= 0.0f && h.prob <= 1.0f))
+        return fail(LT_ERR_FORMAT, "%s: PageRank probability outside [0, 1]", path);
+    if (h.app != kPPR && h.length == 0) return fail(LT_ERR_FORMAT, "%s: walk length 0", path);
+    const uint32_t want_flags = h.app == kWalk ? (h.flags & 6u) : 1u;  // counts, or endpoints / paths
+    if (h.flags != want_flags)
+        return fail(LT_ERR_FORMAT, "%s: output flags %u do not match the app", path, h.flags);
     return LT_OK;
 }
 
@@ -1301,6 +1340,7 @@ lt_status write_checkpoint(Ooc &o, const RunParams &rp)
     h.V = g.V;
     h.E = g.E;
     h.P = o.P;
+    h.part_hash = part_table_hash(g);
     h.iteration = o.iteration;
     const std::string tmp = o.ckpt_path + ".tmp";
     FILE *f = std::fopen(tmp.c_str(), "wb");
@@ -1355,10 +1395,26 @@ lt_status write_checkpoint(Ooc &o, const RunParams &rp)
     return LT_OK;
 }
 
+// Walkers partition p creates lazily in a fresh run of the checkpoint's
+// start mode (run_prepare): all W at the source's partition, per-vertex
+// starts spread by vertex range, none for uniform starts.
+uint64_t expected_lazy(const Ooc &o, const CkptHeader &h, uint32_t p)
+{
+    const lt_graph &g = *o.g;
+    if (h.start == kStartSource) return g.find_partition(h.source) == p ? h.W : 0;
+    if (h.start == kStartPerVertex) {
+        const uint64_t wraps = h.W / g.V, rem = h.W % g.V;
+        const uint64_t nb = g.node_off[p], n = g.node_off[p + 1] - nb;
+        const uint64_t tail = rem > nb ? std::min<uint64_t>(rem - nb, n) : 0;
+        return wraps * n + tail;
+    }
+    return 0;
+}
+
 // Rebuild the queues of a checkpoint: full chunks on the device while room
 // is left (else spilled to host), each partition's partial chunk last on the
-// device.
-lt_status read_queues(Ooc &o, Reader &r, const char *path)
+// device.  Every record is checked before anything is uploaded.
+lt_status read_queues(Ooc &o, Reader &r, const char *path, const CkptHeader &h)
 {
     const uint64_t reserve = (uint64_t)o.P + 2;
     HostBuf stage;
@@ -1371,7 +1427,7 @@ lt_status read_queues(Ooc &o, Reader &r, const char *path)
         q.lazy_total = r.u64();
         q.lazy_next = r.u64();
         const uint64_t n = r.u64();
-        if (!r.ok || q.lazy_next > q.lazy_total || n > (1ull << 32)) {
+        if (!r.ok || q.lazy_next > q.lazy_total || q.lazy_total != expected_lazy(o, h, p) || n > h.W) {
             st = fail(LT_ERR_FORMAT, "%s: truncated or inconsistent queue of partition %u", path, p);
             break;
         }
@@ -1383,6 +1439,19 @@ lt_status read_queues(Ooc &o, Reader &r, const char *path)
             st = fail(LT_ERR_FORMAT, "%s: truncated queue of partition %u", path, p);
             break;
         }
+        const uint32_t nb = o.g->node_off[p], ne = o.g->node_off[p + 1];
+        for (uint64_t i = 0; i < n; i++) {
+            const uint32_t cur = fld[0][i], step = fld[1][i], idx = fld[2][i], qs = fld[3][i];
+            // a queued walker still needs the graph: PPR step >= 2, PageRank /
+            // generic walk 1 <= step <= length
+            const bool step_ok = h.app == kPPR ? step >= 2 : step >= 1 && step <= h.length;
+            if (cur < nb || cur >= ne || idx >= h.W || qs != 0 || !step_ok) {
+                st = fail(LT_ERR_FORMAT, "%s: walker %llu of partition %u is invalid (vertex %u, step %u, index %u)",
+                          path, (unsigned long long)i, p, cur, step, idx);
+                break;
+            }
+        }
+        if (st != LT_OK) break;
         for (uint64_t b = 0; b < n && st == LT_OK; b += kChunk) {
             const uint32_t m = (uint32_t)std::min<uint64_t>(kChunk, n - b);
             const bool last = b + m == n;
@@ -1622,6 +1691,9 @@ lt_status ooc_resume(lt_engine *e, const char *path, uint64_t *counts_out, uint3
     if (s == LT_OK && (h.V != g.V || h.E != g.E || h.P != o.P))
         s = fail(LT_ERR_INVALID, "%s: checkpoint of another graph (V %u, E %llu, %u partitions)", path, h.V,
                  (unsigned long long)h.E, h.P);
+    if (s == LT_OK && h.part_hash != part_table_hash(g))
+        s = fail(LT_ERR_INVALID, "%s: checkpoint of other partition boundaries (partition size %llu here)", path,
+                 (unsigned long long)g.part_bytes);
     const double t0 = now_ms();
     RunParams rp;
     if (s == LT_OK)
@@ -1657,7 +1729,7 @@ lt_status ooc_resume(lt_engine *e, const char *path, uint64_t *counts_out, uint3
     }
     if (s == LT_OK) {
         reset_queues(o);
-        s = read_queues(o, r, path);
+        s = read_queues(o, r, path, h);
     }
     std::fclose(f);
     if (s != LT_OK) {

@@ -16,6 +16,9 @@
 //  * Graph reads: rowptr[cur], rowptr[cur+1] (16 B) and col[e] (4 B) through
 //    the read-only path; counters are u64 reductions resolved in L2.  Column
 //    loads are evict-first, row offsets and counters evict-last (mem.cuh).
+#include <algorithm>
+
+#include "common.h"
 #include "lt_core.cuh"
 #include "mem.cuh"
 #include "walk_whole.h"
@@ -254,16 +257,39 @@ cudaError_t launch_walk_whole(const WholeArgs &a, int app, int start, int grid, 
     }
 }
 
+namespace {
+
+__global__ void mod_check_kernel(uint64_t n, const uint64_t *x, const uint64_t *d, uint64_t *out)
+{
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride)
+        out[i] = d[i] ? mod_u64(x[i], d[i]) : ~0ull;
+}
+
+}  // namespace
+
 }  // namespace lt
+
+// The device build of the walk kernels' remainder, for checking it against
+// native division (a zero divisor gives all ones).
+extern "C" lt_status lt_mod_check_device(uint64_t n, const uint64_t *d_x, const uint64_t *d_d, uint64_t *d_out,
+                                         void *stream)
+{
+    if (n == 0) return LT_OK;
+    if (!d_x || !d_d || !d_out) return lt::fail(LT_ERR_INVALID, "null argument");
+    const uint64_t blocks = std::min<uint64_t>((n + 255) / 256, 152ull * 8);
+    lt::mod_check_kernel<<<(unsigned)blocks, 256, 0, (cudaStream_t)stream>>>(n, d_x, d_d, d_out);
+    LT_CUDA_TRY(cudaGetLastError());
+    return LT_OK;
+}
 
 // ---------------------------------------------------------------------------
 // Allocation-free variant of lt_walk_device.
 //
-// Some callers cannot allocate device memory: code running inside a stream
-// capture that must not call cudaMalloc, plugins handed fixed input and output
-// buffers by a host framework that owns every allocation, and processes whose
-// device memory is fully reserved by another allocator.  lt_walk_device asks
-// them for a scratch buffer; this entry point needs none.  Its scratch (the
+// Some callers cannot allocate device memory: plugins handed fixed input and
+// output buffers by a host framework that owns every allocation, and
+// processes whose device memory another allocator has reserved in full.
+// lt_walk_device asks them for a scratch buffer; this entry point needs none.  Its scratch (the
 // next-walker counter of the step kernel) lives in the file-scope array below,
 // which every GPU that loads this library holds until the process exits.
 //
@@ -279,8 +305,10 @@ cudaError_t launch_walk_whole(const WholeArgs &a, int app, int start, int grid, 
 // stream.
 //
 // The device address of the array is looked up once per device, on the first
-// call made with that device current (cudaGetSymbolAddress); make that first
-// call before any stream capture begins.
+// call made with that device current (cudaGetSymbolAddress), and kept for the
+// life of the process; make that first call before any stream capture begins.
+// The kept address assumes the device's primary context is never reset: after
+// a cudaDeviceReset the module is loaded again and the address may be stale.
 // ---------------------------------------------------------------------------
 
 #include <mutex>

@@ -77,6 +77,50 @@ def test_checkpoint_info_rejects_bad_files(lt, tmp_path):
     assert lt.lib.lt_checkpoint_read_info(str(bad).encode(), ctypes.byref(info)) == 3     # LT_ERR_FORMAT
 
 
+def _ckpt_header(app=0, start=0, source=0, length=0, runs=1, run_base=0, run_index=0, flags=1, W=64,
+                 prob=0.15, seed=1, V=100, E=400, P=2, part_hash=0, iteration=3):
+    import struct
+    return (b"LTCKPT01" + struct.pack("<I", 2)
+            + struct.pack("<8I", app, start, source, length, runs, run_base, run_index, flags)
+            + struct.pack("<Qf", W, prob) + struct.pack("<QIQI", seed, V, E, P)
+            + struct.pack("<QQ", part_hash, iteration))
+
+
+@pytest.mark.parametrize("bad", [
+    dict(source=100),                      # source outside the graph
+    dict(prob=0.0),                        # PPR stop probability outside (0, 1]
+    dict(prob=float("nan")),
+    dict(app=1, prob=1.5, length=10),      # PageRank probability outside [0, 1]
+    dict(app=1, length=0, prob=0.85),      # no steps
+    dict(app=2, length=0, flags=2),
+    dict(app=2, length=5, flags=1),        # generic walks write no counts
+    dict(flags=3),                         # PPR writes counts only
+    dict(W=0), dict(V=0), dict(P=0), dict(P=101),
+    dict(run_index=1, runs=1), dict(app=3), dict(start=3),
+])
+def test_checkpoint_header_rejects_corrupt_fields(lt, tmp_path, bad):
+    """A checkpoint whose header describes a run the engine could not have
+    started is refused with LT_ERR_FORMAT before anything reaches the device."""
+    info = lt.CheckpointInfo()
+    good = tmp_path / "good.ckpt"
+    good.write_bytes(_ckpt_header())
+    assert lt.lib.lt_checkpoint_read_info(str(good).encode(), ctypes.byref(info)) == 0
+    assert info.num_walkers == 64 and info.num_nodes == 100 and info.iteration == 3
+    path = tmp_path / "bad.ckpt"
+    path.write_bytes(_ckpt_header(**bad))
+    assert lt.lib.lt_checkpoint_read_info(str(path).encode(), ctypes.byref(info)) == 3   # LT_ERR_FORMAT
+
+
+def test_checkpoint_header_rejects_old_version(lt, tmp_path):
+    import struct
+    path = tmp_path / "v1.ckpt"
+    hdr = bytearray(_ckpt_header())
+    hdr[8:12] = struct.pack("<I", 1)
+    path.write_bytes(bytes(hdr))
+    info = lt.CheckpointInfo()
+    assert lt.lib.lt_checkpoint_read_info(str(path).encode(), ctypes.byref(info)) == 3
+
+
 def test_engine_cfg_defaults(lt):
     """lt_engine_cfg_default: reference threshold, pipelining on, the vertex
     index resident on the device."""

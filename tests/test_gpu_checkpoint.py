@@ -86,3 +86,49 @@ def test_resume_rejects_other_graph(lt, require_gpu, g16, tmp_path):
     with pytest.raises(lt.LTError) as ei:
         e2.resume(path)
     assert ei.value.status == 1
+
+
+def _first_queue(raw, V, P):
+    """Offset of the first non-empty queue record block of a PPR checkpoint
+    (header 96 B, device statistics 64 B, counts u64[V], then per partition
+    u64 lazy_total, lazy_next, n and u32 cur[n], step[n], idx[n], query[n])."""
+    off = 96 + 64 + 8 * V
+    for _ in range(P):
+        n = int(np.frombuffer(raw, np.uint64, 3, off)[2])
+        if n:
+            return off + 24, n
+        off += 24
+    raise AssertionError("no queued walkers in the checkpoint")
+
+
+@pytest.mark.parametrize("field,value,status", [
+    (0, "V", 3),       # vertex outside the graph
+    (2, "W", 3),       # walker index beyond the run
+    (1, 1, 3),         # a PPR walker in a queue has at least 2 steps left
+    (3, 7, 3),         # query slot of a run that serves no queries
+    (None, None, 1),   # partition table of another partition size
+])
+def test_resume_rejects_corrupt_checkpoint(lt, require_gpu, g16, tmp_path, field, value, status):
+    """A corrupt checkpoint is refused before any walker reaches the device."""
+    rp, col = g16
+    V, W = len(rp) - 1, 300000
+    g, e = _engine(lt, rp, col, partitions=4, sched=0, seed=9)
+    path = tmp_path / "c.ckpt"
+    e.checkpoint(path, every=3, stop=True)
+    with pytest.raises(lt.LTError):
+        e.ppr(0, W, 0.15)
+    raw = bytearray(path.read_bytes())
+    if field is None:
+        raw[80:88] = bytes(a ^ 0xFF for a in raw[80:88])   # the partition-table hash
+    else:
+        off, n = _first_queue(bytes(raw), V, g.num_partitions)
+        v = {"V": V + 5, "W": W + 1}.get(value, value)
+        np.frombuffer(raw, np.uint32, 1, off + 4 * n * field)[:] = v
+    path.write_bytes(bytes(raw))
+    _, e2 = _engine(lt, rp, col, partitions=2, sched=0, seed=1)
+    with pytest.raises(lt.LTError) as ei:
+        e2.resume(path)
+    assert ei.value.status == status
+    # the engine stays usable
+    want, _, _ = oracle.ppr(rp, col, 0, 5000, prob=0.15, seed=1)
+    assert (e2.ppr(0, 5000, 0.15) == want).all()

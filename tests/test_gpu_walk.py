@@ -203,3 +203,62 @@ def test_compact_entry_point(lt, require_gpu, rmat16, app, start, length):
                                               paths=True)
             assert (ep == wep).all()
             assert (d_pa.cpu().numpy().view(np.uint32) == wpa.ravel()).all()
+
+
+def test_device_remainder_matches_native(lt, require_gpu):
+    """The device build of the integer remainder (no 64-bit division): the
+    three-remainder path below 2^16 and the single-precision estimate with
+    integer correction from 2^16 to 2^32, against native %."""
+    import torch
+    rng = np.random.default_rng(3)
+    n = 4_000_000
+    x = rng.integers(0, np.iinfo(np.uint64).max, n, dtype=np.uint64, endpoint=True)
+    d = np.concatenate([
+        rng.integers(1, 1 << 16, n // 4, dtype=np.uint64),
+        rng.integers(1 << 16, 1 << 32, n // 4, dtype=np.uint64),
+        (np.uint64(1) << rng.integers(16, 32, n // 4, dtype=np.uint64)) - rng.integers(0, 3, n // 4, dtype=np.uint64),
+        (np.uint64(1) << rng.integers(16, 32, n // 4, dtype=np.uint64)) + rng.integers(0, 3, n // 4, dtype=np.uint64)])
+    d = np.minimum(d, np.uint64(0xFFFFFFFF))
+    edge_x = np.array([0, 1, 2**32 - 1, 2**32, 2**63, 2**64 - 1, 2**64 - 2] * 9, dtype=np.uint64)
+    edge_d = np.array([1, 2, 3, 65535, 65536, 65537, 2**31, 2**32 - 1, 2**32 - 2] * 7, dtype=np.uint64)
+    x = np.concatenate([x, edge_x])
+    d = np.concatenate([d, edge_d])
+    dev = torch.device("cuda:0")
+    tx = torch.from_numpy(x.view(np.int64)).to(dev)
+    td = torch.from_numpy(d.view(np.int64)).to(dev)
+    to = torch.empty_like(tx)
+    lt.check(lt.lib.lt_mod_check_device(len(x), tx.data_ptr(), td.data_ptr(), to.data_ptr(),
+                                        torch.cuda.current_stream().cuda_stream))
+    torch.cuda.synchronize()
+    got = to.cpu().numpy().view(np.uint64)
+    assert (got == x % d).all()
+
+
+def test_hub_degrees_above_2_16(lt, require_gpu):
+    """Walks through hubs whose degrees need the large-divisor remainder
+    (65 536 .. 1 048 583 out-edges): counts, endpoints and paths bit-exact."""
+    degs = [1 << 16, (1 << 16) + 1, 100003, (1 << 20) + 7]
+    leaves = 1 << 12
+    H = len(degs)
+    V = H + leaves
+    rows, cols = [], []
+    rng = np.random.default_rng(5)
+    for h, dg in enumerate(degs):
+        rows.append(np.full(dg, h, np.uint32))
+        cols.append((H + rng.integers(0, leaves, dg)).astype(np.uint32))
+    for v in range(H, V):   # every leaf links back to two hubs
+        rows.append(np.full(2, v, np.uint32))
+        cols.append(rng.integers(0, H, 2).astype(np.uint32))
+    r = np.concatenate(rows)
+    c = np.concatenate(cols)
+    order = np.argsort(r, kind="stable")
+    r, c = r[order], c[order]
+    rp = np.zeros(V + 1, np.uint64)
+    np.add.at(rp, r.astype(np.int64) + 1, 1)
+    rp = np.cumsum(rp).astype(np.uint64)
+    g, e = _engine(lt, rp, c, seed=17)
+    want, _, _ = oracle.ppr(rp, c, 3, 200000, prob=0.15, seed=17)
+    assert (e.ppr(3, 200000, 0.15) == want).all()
+    ep, pa, _ = oracle.generic_walk(rp, c, 50000, length=12, start_mode=1, seed=17, paths=True)
+    gep, gpa = e.walk(50000, length=12, start=1, paths=True)
+    assert (gep == ep).all() and (gpa == pa).all()

@@ -1,12 +1,13 @@
 """lt_walk_device_noalloc -- the allocation-free step-kernel entry point.
 
-Callers that cannot allocate device memory (code inside a stream capture, or a
-host framework that owns every device allocation and hands over only inputs
-and outputs) use this entry point instead of lt_walk_device, which needs a
-caller-provided scratch buffer.  Its scratch is a static device array shared
-by all calls, so this test checks, through the C ABI, that back-to-back calls
-give exactly the outputs of lt_walk_device (integer counts: the tolerance is
-zero) -- the shared array must be cleared by each call.
+Callers that cannot allocate device memory (a plugin whose host framework
+owns every device allocation and hands over only inputs and outputs, or a
+process whose device memory another allocator has reserved) use this entry
+point instead of lt_walk_device, which needs a caller-provided scratch
+buffer.  Its scratch is a static device array shared by all calls, so this
+test checks, through the C ABI, that back-to-back calls give exactly the
+outputs of lt_walk_device and of the CPU oracle (integer counts: the
+tolerance is zero) -- the shared array must be cleared by each call.
 
 The file name makes pytest collect it last.
 """
@@ -14,6 +15,8 @@ import ctypes
 
 import numpy as np
 import pytest
+
+import oracle
 
 pytestmark = pytest.mark.gpu
 
@@ -57,3 +60,8 @@ def test_noalloc_matches_walk_device(lt, require_gpu):
         assert torch.equal(got_st, want_st)
         expect_sum = W if app == 0 else W * length
         assert int(got.sum().item()) == expect_sum
+        if app == 0:
+            ref, _, _ = oracle.ppr(rp, col, src, W, prob=prob, seed=77)
+        else:
+            ref, _ = oracle.pagerank(rp, col, W, length=length, alpha=prob, seed=77, start_mode=start)
+        assert (got.cpu().numpy().view(np.uint64) == ref).all(), (app, start)
