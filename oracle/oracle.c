@@ -42,14 +42,20 @@
  *   PPR length trials: init draw t gives two trials, m53 of (x0,x1) first,
  *   then m53 of (x2,x3).
  *
- * Pinning.  Walk semantics: parity unpinned against reference outputs (the
- * reference cannot produce reproducible ones, see above).  The walk functions
- * are pinned to the reference's own invariants instead: PPR counts sum to the
- * number of walkers (app/ppr.cu:77-85), PageRank counts to walkers x length x
- * runs (app/pagerank.cu:202-210), and hand-checkable graphs where every
- * endpoint is known.  Philox is pinned to the Random123 known-answer
- * vectors.  The partitioner (orc_partition) is pinned byte for byte to the
- * reference's EqualSizeStrategy compiled from its own sources.
+ * Pinning.  Walk semantics: the reference's own update code is the pin.
+ * oracle/ref_apps_main.cpp compiles app/ppr.cu, app/pagerank.cu and
+ * app/genericwalk.cu in place with g++ (host stand-ins for their GPU
+ * plumbing in oracle/ref_shim/) and drives their App::update partition by
+ * partition, as src/WalkManager.h:229-246 does, with the keyed stream above
+ * in place of cuRAND; its outputs (tests/golden/ref_walks.json) must equal
+ * this file's bit for bit (tests/test_ref_pin.py).  The reference's cuRAND
+ * streams themselves are not reproducible (uninitialised seed), so they are
+ * not the target.  Also pinned: the sum invariants (PPR counts sum to the
+ * number of walkers, app/ppr.cu:77-85; PageRank to walkers x length x runs,
+ * app/pagerank.cu:89-97), hand-checkable graphs, Philox against the
+ * Random123 known-answer vectors, and the partitioner (orc_partition) byte
+ * for byte against the reference's EqualSizeStrategy compiled from its own
+ * sources.
  *
  * The RMAT generator (a seeded stand-in for the reference's datasets, which
  * are absent) is restated here as well so the GPU generator can be checked

@@ -262,3 +262,37 @@ def test_hub_degrees_above_2_16(lt, require_gpu):
     ep, pa, _ = oracle.generic_walk(rp, c, 50000, length=12, start_mode=1, seed=17, paths=True)
     gep, gpa = e.walk(50000, length=12, start=1, paths=True)
     assert (gep == ep).all() and (gpa == pa).all()
+
+
+def _ref_cases():
+    import json
+    with open(os.path.join(GOLDEN, "ref_walks.json")) as f:
+        return [c for c in json.load(f)["cases"] if not (c["app"] == "ppr" and c["runs"] > 1)]
+
+
+@pytest.mark.parametrize("case", _ref_cases(), ids=lambda c: f"{c['app']}-{c['graph']}-s{c['start']}-{c['seed']:x}")
+def test_engine_matches_reference_update_vectors(lt, require_gpu, case):
+    """The CUDA engine against the outputs of the reference's own App::update
+    code (tests/golden/ref_walks.json), resident and out of core."""
+    import hashlib
+    rp, col = _golden(case["graph"])
+    W, L = case["walkers"], case["length"]
+
+    def digest(arrays):
+        return [{"sha256": hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest(),
+                 "sum": int(a.astype(np.uint64).sum())} for a in arrays]
+
+    V = len(rp) - 1
+    fit = 24 + 4 * int(np.diff(rp.astype(np.int64)).max())   # the largest vertex's rowptr pair and edges
+    for part_bytes, kw in ((1 << 30, {}), (max(fit, (8 * (V + 1) + 4 * len(col)) // 3), dict(partitions=1))):
+        g = lt.Graph.from_csr(rp, col, part_bytes)
+        if kw and g.num_partitions < 2:
+            continue
+        e = lt.Engine(g, seed=case["seed"], **kw)
+        if case["app"] == "ppr":
+            got = [e.ppr(case["source"], W, case["prob"])]
+        elif case["app"] == "pagerank":
+            got = [e.pagerank(W, length=L, runs=case["runs"], start=case["start"], alpha=case["prob"])]
+        else:
+            got = list(e.walk(W, length=L, run=case["run0"], start=case["start"], paths=True))
+        assert digest(got) == case["outputs"], kw
