@@ -87,8 +87,12 @@ typedef struct lt_engine_cfg {
     uint32_t num_device_partitions;  /* -p: partitions cached on the device (0 = all) */
     uint64_t num_device_walkers;     /* -b: walkers held on the device (0 = all) */
     int sched;                       /* lt_sched */
-    int pipeline;                    /* wave-run policies: overlap the next partition loads with the
-                                        current step kernel (1 = on; 0 = loads finish first) */
+    int pipeline;                    /* overlap partition loads with stepping (1 = on; 0 = loads
+                                        finish first, the reference's NO_PIPELINE build,
+                                        benchmark/figure13/Makefile): plain / FIFO compute other
+                                        cached partitions while a load is in flight
+                                        (src/Scheduler.h:194-208); wave runs overlap the next
+                                        loads with the current step kernel */
     uint64_t zerocopy_threshold;     /* walkers below which a cold partition is read zero-copy;
                                         UINT64_MAX = default partitionSize/128/2 (src/Scheduler.h:295) */
     uint64_t seed;                   /* Philox key */
@@ -128,6 +132,12 @@ typedef struct lt_stats {
     uint64_t walker_evicting_calls;
     double step_kernel_ms;    /* CUDA-event time of the step kernels of the last run */
     uint64_t handoffs;        /* walkers staged and bucketed into another partition's queue */
+    uint64_t overlap_computes; /* plain / FIFO loop: cached partitions computed while a load was in
+                                  flight (getComputedPartition, src/Scheduler.h:194-208) */
+    uint64_t zerocopy_groups;  /* wave runs: step kernels that read a bounded group of uncached
+                                  partitions zero-copy */
+    uint64_t zerocopy_sweeps;  /* wave runs: step kernels that read every uncached partition
+                                  zero-copy to finish the last walkers */
 } lt_stats;
 
 const char *lt_strerror(lt_status s);

@@ -81,7 +81,8 @@ class Stats(C.Structure):
                 ("graph_loading_calls", C.c_uint64), ("computing_calls", C.c_uint64),
                 ("zerocopy_calls", C.c_uint64), ("walker_loading_calls", C.c_uint64),
                 ("walker_evicting_calls", C.c_uint64), ("step_kernel_ms", C.c_double),
-                ("handoffs", C.c_uint64)]
+                ("handoffs", C.c_uint64), ("overlap_computes", C.c_uint64),
+                ("zerocopy_groups", C.c_uint64), ("zerocopy_sweeps", C.c_uint64)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}

@@ -115,7 +115,7 @@ struct Ooc {
     // device views of h_plan / h_work (null: not mapped, upload by copy)
     uint8_t *h_plan_dev = nullptr, *h_work_dev = nullptr;
     std::vector<uint32_t> arrivals, visits;
-    std::vector<uint64_t> waiting, lazy_left;
+    std::vector<uint64_t> waiting, lazy_left, dev_waiting;
 
     std::vector<Queue> q;
     std::unique_ptr<Policy> policy;
@@ -257,6 +257,7 @@ void refresh(Ooc &o, uint32_t p)
 {
     o.waiting[p] = o.q[p].total();
     o.lazy_left[p] = o.q[p].lazy_left();
+    o.dev_waiting[p] = o.q[p].dev_count();
 }
 void refresh_all(Ooc &o)
 {
@@ -270,6 +271,7 @@ SchedView view(Ooc &o)
     v.K = o.K;
     v.waiting = o.waiting.data();
     v.lazy = o.lazy_left.data();
+    v.dev = o.dev_waiting.data();
     v.slot_of = o.slot_of.data();
     v.last_used = o.last_used.data();
     v.arrivals = o.arrivals.data();
@@ -349,7 +351,7 @@ lt_status start_load(Ooc &o, uint32_t p, int32_t slot, std::vector<std::pair<uin
     return LT_OK;
 }
 
-lt_status load_partition(Ooc &o, uint32_t p)
+lt_status load_partition(Ooc &o, uint32_t p, std::vector<std::pair<uint32_t, cudaEvent_t>> *deferred)
 {
     if (o.slot_of[p] >= 0) return LT_OK;
     int32_t slot = free_slot(o);
@@ -363,7 +365,7 @@ lt_status load_partition(Ooc &o, uint32_t p)
         slot = o.slot_of[victim];
         LT_TRY(evict_partition(o, (uint32_t)victim));
     }
-    return start_load(o, p, slot, nullptr);
+    return start_load(o, p, slot, deferred);
 }
 
 lt_status host_chunk_alloc(Ooc &o, uint32_t &id)
@@ -746,6 +748,28 @@ void reset_queues(Ooc &o)
     }
 }
 
+// graphLoadingPhase's pipeline (src/Scheduler.h:194-208): while the load of
+// p is on the copy engine, drain the device queue of the cached partition the
+// policy picks (getComputedPartition), one synchronous step kernel at a time,
+// until the copy has finished or nothing is worth computing.  The walkers
+// these kernels send to p queue there: p is published only afterwards.
+lt_status overlap_load(Ooc &o, const RunParams &rp, uint32_t p, cudaEvent_t copy_done)
+{
+    lt_engine &e = *o.e;
+    for (uint32_t k = 0; k < o.P; k++) {
+        const cudaError_t q = cudaEventQuery(copy_done);
+        if (q == cudaSuccess) break;
+        if (q != cudaErrorNotReady) LT_CUDA_TRY(q);
+        const int32_t c = o.policy->overlap(view(o), (int32_t)p);
+        if (c < 0) break;
+        LT_TRY(step_and_bucket(o, rp, c, Lazy{}, false, nullptr));
+        e.stats.overlap_computes++;
+        drain_timers(o, false);
+    }
+    cudaGetLastError();
+    return LT_OK;
+}
+
 // One iteration for partition p (GPUScheduler::run).
 lt_status process(Ooc &o, const RunParams &rp, uint32_t p)
 {
@@ -759,7 +783,15 @@ lt_status process(Ooc &o, const RunParams &rp, uint32_t p)
     const bool zero_copy = o.slot_of[p] < 0 && o.policy->zero_copy(v0, p, o.zc_threshold);
     if (!zero_copy) {
         e.stats.explicit_iterations++;
-        LT_TRY(load_partition(o, p));
+        std::vector<std::pair<uint32_t, cudaEvent_t>> pending;
+        LT_TRY(load_partition(o, p, &pending));
+        if (!pending.empty()) {
+            if (e.cfg.pipeline) LT_TRY(overlap_load(o, rp, p, pending.front().second));
+            for (auto &d : pending) {
+                LT_CUDA_TRY(cudaStreamWaitEvent(e.s_compute, d.second, 0));
+                LT_TRY(set_entry(o, d.first, e.s_compute));
+            }
+        }
         o.prev_loaded = (int32_t)p;
     }
     // walkerLoadingPhase: bring spilled walkers back, keeping room to make progress
@@ -1012,6 +1044,12 @@ lt_status wave_step(Ooc &o, const RunParams &rp, WaveState &w, bool &done)
                 for (uint32_t p = 0; p < o.P; p++)
                     if (o.slot_of[p] < 0) group.push_back(p);
             }
+            if (!group.empty()) {
+                if (sweep)
+                    e.stats.zerocopy_sweeps++;
+                else
+                    e.stats.zerocopy_groups++;
+            }
             for (uint32_t p : group) {
                 o.zc_mask[p >> 5] |= 1u << (p & 31);
                 o.zc_mask_any = true;
@@ -1127,6 +1165,7 @@ lt_status ooc_create(lt_engine *e, Ooc **out)
     o->visits.assign(o->P, 0);
     o->waiting.assign(o->P, 0);
     o->lazy_left.assign(o->P, 0);
+    o->dev_waiting.assign(o->P, 0);
     o->q.assign(o->P, Queue{});
     if (e->cfg.sched == LT_SCHED_FIFO) {
         o->policy.reset(new FifoPolicy());

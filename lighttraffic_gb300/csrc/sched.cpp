@@ -32,6 +32,39 @@ int32_t Policy::victim(const SchedView &v, int32_t except, uint32_t /*incoming*/
     return best;
 }
 
+// getComputedPartition (src/Scheduler.h:84-111): among cached partitions
+// other than `except`, those with a full reference page on the device
+// compete on the fewest walkers in total (device + host + not yet created);
+// when none has one, the partition with the most device walkers.
+int32_t Policy::overlap(const SchedView &v, int32_t except)
+{
+    int32_t full = -1, notfull = -1;
+    for (uint32_t i = 0; i < v.P; i++) {
+        if ((int32_t)i == except || v.slot_of[i] < 0) continue;
+        const uint64_t on_gpu = v.dev[i];
+        if (on_gpu >= kRefPageWalkers) {
+            if (full < 0 || v.waiting[i] < v.waiting[full]) full = (int32_t)i;
+        } else if (full < 0 && on_gpu > 0) {
+            if (notfull < 0 || on_gpu > v.dev[notfull]) notfull = (int32_t)i;
+        }
+    }
+    return full >= 0 ? full : notfull;
+}
+
+// FIFO variant (src/Scheduler.h:113-127): the first cached partition after
+// `except` in cyclic order.  The reference would compute it even with an
+// empty device queue (nothing to do until the copy ends); here such a pick
+// ends the overlap.
+int32_t FifoPolicy::overlap(const SchedView &v, int32_t except)
+{
+    const uint32_t start = except < 0 ? 0 : (uint32_t)except;
+    for (uint32_t k = 1; k < v.P; k++) {
+        const uint32_t i = (start + k) % v.P;
+        if (v.slot_of[i] >= 0) return v.dev[i] > 0 ? (int32_t)i : -1;
+    }
+    return -1;
+}
+
 // FIFO_SCHE nextPartition (src/Scheduler.h:393-416): sweep partitions in id
 // order, returning each one that has walkers; a finished sweep returns false
 // once, after which the caller's outer loop starts the next sweep.

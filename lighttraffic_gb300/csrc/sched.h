@@ -13,7 +13,13 @@
 //                     walkers than the threshold is read over the host link
 //                     (shouldZerocopy, :243-252);
 //   no look-ahead loads (the reference loads the partition it is about to
-//                     compute, :173-213).
+//                     compute, :173-213);
+//   overlap           = while that load is on the copy engine, compute a
+//                     cached partition: among those holding at least a
+//                     reference page (167 936 walkers, src/Type.h:15) on the
+//                     device the one with the fewest walkers in total, else
+//                     the one with the most device walkers
+//                     (getComputedPartition, :84-111, used at :194-208).
 // The FIFO policy restates the FIFO_SCHE variant (:113-127, :391-418).
 // The learned, frequency and batched policies run the engine in waves (see
 // Policy::wave) and differ only in which cached partitions they give up.
@@ -32,6 +38,7 @@ struct SchedView {
     uint32_t K = 0;                      // cache slots
     const uint64_t *waiting = nullptr;   // P: walkers waiting per partition (device + host + not yet created)
     const uint64_t *lazy = nullptr;      // P: of those, walkers not yet created
+    const uint64_t *dev = nullptr;       // P: of those, walkers in device chunks
     const int32_t *slot_of = nullptr;    // P: cache slot or -1
     const uint64_t *last_used = nullptr; // P: iteration the partition was last loaded or computed
     const uint32_t *arrivals = nullptr;  // P: walkers queued at each partition in the last iteration
@@ -40,6 +47,11 @@ struct SchedView {
     uint64_t zc_threshold = 0;           // walkers below which a cold partition is read zero-copy
 };
 
+// Walkers in one page of the reference's device queues (numBlock x
+// threadPerBlock x walkerPerThread, src/Type.h:10-15): the "full page" test
+// of getComputedPartition.
+constexpr uint64_t kRefPageWalkers = 82ull * 512 * 4;
+
 class Policy {
 public:
     virtual ~Policy() = default;
@@ -47,6 +59,10 @@ public:
     virtual bool next(const SchedView &v, int32_t prev_computed, bool sync, uint32_t &choice);
     // findPartitionwithleastWalker over cached partitions other than `except`; -1 if none.
     virtual int32_t victim(const SchedView &v, int32_t except, uint32_t incoming);
+    // getComputedPartition: a cached partition other than `except` whose
+    // device walkers to step while the load of `except` is in flight; -1 if
+    // none.
+    virtual int32_t overlap(const SchedView &v, int32_t except);
     // shouldZerocopy for a partition that is not cached.
     virtual bool zero_copy(const SchedView &v, uint32_t p, uint64_t threshold) { return v.waiting[p] < threshold; }
     // Called after every iteration; v.arrivals holds that iteration's arrivals.
@@ -86,6 +102,7 @@ class FifoPolicy : public Policy {
 public:
     bool next(const SchedView &v, int32_t prev_computed, bool sync, uint32_t &choice) override;
     int32_t victim(const SchedView &v, int32_t except, uint32_t incoming) override;
+    int32_t overlap(const SchedView &v, int32_t except) override;
     void reset() override { cursor_ = 0; }
     const char *name() const override { return "fifo"; }
 };

@@ -110,3 +110,22 @@ def test_batch_into_pinned_outputs(lt, require_gpu):
             got = sorted(zip(v[a:b].tolist(), c[a:b].tolist()))
             want = sorted(zip(ref[1][a:b].tolist(), ref[2][a:b].tolist()))
             assert got == want
+
+
+def test_c3s_zipf_batch_matches_oracle(lt, require_gpu):
+    """The c3 batch workload scaled down (RMAT 2^22 / 2^26, 256 sources drawn
+    Zipf(1.1) by out-degree rank, lognormal walks clipped to [1e3, 1e6]):
+    every query's sparse counts equal the oracle's PPR with its seed."""
+    import bench
+    g = lt.Graph.rmat(22, 1 << 26, seed=1, part_bytes=32 << 20)
+    rp, col = g.csr_views()
+    sources, walkers, seeds = bench.c3_queries(bench.CONFIGS["c3s"], rp)
+    e = lt.Engine(g, seed=1)
+    off, v, c = e.ppr_batch(sources, walkers, seeds, 0.15)
+    for q in range(len(sources)):
+        got = _as_dict(off, v, c, q)
+        assert got == _oracle_dict(rp, col, int(sources[q]), int(walkers[q]), int(seeds[q])), q
+    e.autotune()
+    off2, v2, c2 = e.ppr_batch(sources, walkers, seeds, 0.15)
+    for q in (0, 1, len(sources) // 2, len(sources) - 1):
+        assert _as_dict(off2, v2, c2, q) == _as_dict(off, v, c, q)

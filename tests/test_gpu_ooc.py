@@ -169,3 +169,36 @@ def test_wave_runs_without_pipelining(lt, require_gpu, g16):
     assert (out[True][0] == out[False][0]).all()
     want, _, _ = oracle.ppr(rp, col, 0, 300000, prob=0.15, seed=9)
     assert (out[False][0] == want).all()
+
+
+@pytest.fixture(scope="module")
+def c2s(lt):
+    """The c2 out-of-core workload scaled down: RMAT 2^24 / 2^28 (1.1 GiB in
+    pinned host memory, 32 MiB partitions), W = 2|V| PPR walks from vertex 0,
+    against the oracle on the same arrays."""
+    g = lt.Graph.rmat(24, 1 << 28, seed=1, part_bytes=32 << 20)
+    rp, col = g.csr_views()
+    W = 2 * g.num_nodes
+    want, _, st = oracle.ppr(rp, col, 0, W, prob=0.15, seed=1)
+    return g, W, want, st
+
+
+@pytest.mark.parametrize("sched,pipeline", [(2, True), (4, True), (3, True), (0, True), (0, False), (1, True)])
+def test_c2s_scale_ooc(lt, require_gpu, c2s, sched, pipeline):
+    """16 of the graph's partitions cached, walker pool 2^22: every scheduler,
+    with and without the load/compute overlap, gives the oracle's counts bit
+    for bit; wave runs read bounded zero-copy groups (the path that takes
+    most of a c2 run) and the plain loop computes cached partitions while
+    loads are in flight."""
+    g, W, want, st = c2s
+    assert g.num_partitions > 16
+    e = lt.Engine(g, partitions=16, batch=1 << 22, seed=1, sched=sched, pipeline=pipeline)
+    got = e.ppr(0, W, 0.15)
+    assert (got == want).all()
+    s = e.stats()
+    assert s["moves"] == st[1]
+    if sched in (2, 3, 4):
+        assert s["zerocopy_groups"] > 0
+    if sched == 0:
+        assert (s["overlap_computes"] > 0) == pipeline
+    e.close()
