@@ -6,15 +6,20 @@
 Workloads (synthetic RMAT graphs, a=.57 b=.19 c=.19 d=.05, seed 1, isolated
 vertices removed, stand in for the reference's datasets, which are absent):
   c2 (default): out-of-core PPR -- RMAT(2^30 vertices, 2^33 edges), 32 MiB
-      partitions in pinned host memory, 256 cached on the device (-p 256,
-      8 GiB), walker pool 2^28 (-b), W = 2|V| walks from source 0, stop
-      probability 0.15.  One step = one full run from a cold device cache,
-      through the public API (lt_run_ppr with a host count buffer): every
-      partition load, zero-copy read and walker spill is inside the timed
-      region.  `value` is the learned scheduler (wave runs, cache slots by
-      predicted visits); the plain (reference) scheduler is timed beside it
-      under "plain", and wave runs with least-recently-used slots (batched)
-      or moving-average scores (frequency) under "ablations".
+      partitions in pinned host memory, -p 256 (the graph gets 256 x 32 MiB =
+      8 GiB of device memory, the vertex index included), walker pool 2^28
+      (-b), W = 2|V| walks from source 0, stop probability 0.15.  One step =
+      one full run from a cold device cache, through the public API
+      (lt_run_ppr with a host count buffer): every partition load, zero-copy
+      read and walker spill is inside the timed region.  `value` is the
+      learned scheduler (wave runs, cache slots by predicted visits); beside
+      it under "variants": the plain (reference) scheduler, the plain
+      scheduler at the wave runs' calibrated zero-copy threshold (plain_x8),
+      the batched / frequency ablations, and learned / plain with the
+      reference's slot layout (host index).  Every run of every variant must
+      give the first run's counts bit for bit, and the cpu_baseline sample
+      must equal the same walkers run through the product.  The line also
+      carries serving latency at 1 000 queries/s (learned and plain).
   c2s: the c2 setup scaled down for profiler captures -- RMAT(2^24, 2^28),
       16 of its 32 MiB partitions cached, walker pool 2^22.
   c1: walk-based PageRank on RMAT(2^23, 2^27) resident in HBM (32 MiB
@@ -42,8 +47,10 @@ vertices removed, stand in for the reference's datasets, which are absent):
 Steps per run: hops taken (PPR, the reference's 2|V|/0.15 estimate counted
 exactly) or updates (PageRank, W * l).
 --impl reference times the CPU restatement of the reference walk semantics
-(oracle/, OpenMP over all host cores) on a bounded sample of the same
-workload; the c2 input graph for it is made by the GPU generator.
+(oracle/, OpenMP over all host cores; its update rules pinned to the
+reference's own App::update code) on a bounded sample of the same workload
+per step (SAMPLES); its input graph comes from the oracle's CPU generator,
+so that arm uses neither the GPU nor this repository's library.
 """
 from __future__ import annotations
 
@@ -177,84 +184,119 @@ def profiled_traffic(workload):
 
 # ---------------------------------------------------------- CPU oracle
 
-def cpu_rate(cfg, rp, col, seconds, threads):
-    """Oracle (CPU restatement of the reference semantics) on a bounded
-    sample: the first n walkers of the run.  Returns (steps/s, description)."""
+# Oracle sample of each workload: the same bounded piece of the workload for
+# the reference arm (one sample per step) and the cpu_baseline leg (repeated
+# samples, median), so the two CPU figures measure identical work.
+#   walkers: the first n walkers of the run; queries: the first n queries.
+SAMPLES = {"c2": dict(walkers=1 << 22), "c2s": dict(walkers=1 << 20), "c4": dict(walkers=1 << 22),
+           "c1": dict(walkers=None), "c0": dict(walkers=None), "c3": dict(queries=64), "c3s": dict(queries=64)}
+
+
+def cpu_sample(name, cfg, rp, col, threads):
+    """One oracle run over the workload's sample.  Returns (steps, seconds,
+    outputs, description): PPR / PageRank counts of the first n walkers, or
+    the per-query counts of the first n queries."""
     import oracle
     V = len(rp) - 1
     W = 2 * V
+    smp = SAMPLES[name]
+    t = time.perf_counter()
+    if cfg.get("batch_queries"):
+        sources, walkers, seeds = c3_queries(cfg, rp)
+        q = min(smp["queries"], len(sources))
+        outs, hops = [], 0
+        for i in range(q):
+            c, _, st = oracle.ppr(rp, col, int(sources[i]), int(walkers[i]), prob=cfg["prob"], seed=int(seeds[i]),
+                                  threads=threads)
+            nz = np.nonzero(c)[0]
+            outs.append((nz, c[nz]))
+            hops += int(st[1])
+        dt = time.perf_counter() - t
+        return hops, dt, outs, f"first {q} of {len(sources)} queries ({hops} hops)"
+    n = min(W, smp["walkers"] or W)
+    if cfg["app"] == 1:
+        c, st = oracle.pagerank(rp, col, n, length=cfg["length"], alpha=cfg["prob"], seed=SEED_WALK,
+                                start_mode=cfg["start"], threads=threads)
+        steps = int(st[0])
+    else:
+        c, _, st = oracle.ppr(rp, col, 0, n, prob=cfg["prob"], seed=SEED_WALK, threads=threads)
+        steps = int(st[1])
+    dt = time.perf_counter() - t
+    return steps, dt, c, f"first {n} of {W} walkers ({steps} steps)"
 
-    def run(n):
-        t = time.perf_counter()
-        if cfg["app"] == 1:
-            _, st = oracle.pagerank(rp, col, n, length=cfg["length"], seed=SEED_WALK,
-                                    start_mode=cfg["start"], threads=threads)
-            steps = int(st[0])
-        else:
-            _, _, st = oracle.ppr(rp, col, 0, n, prob=cfg["prob"], seed=SEED_WALK, threads=threads)
-            steps = int(st[1])
-        return steps, time.perf_counter() - t
 
-    n = min(W, 1 << 17)
-    steps, dt = run(n)
-    n2 = int(min(W, max(n, n * seconds / max(dt, 1e-3))))
-    if n2 > n:
-        steps, dt = run(n2)
-        n = n2
-    return steps / dt, f"first {n} of {W} walkers ({steps} steps, {dt:.1f} s)"
+def cpu_baseline_leg(name, cfg, rp, col, seconds):
+    """cpu_baseline: the oracle sample repeated until about `seconds` of CPU
+    work (at least 3 samples), median rate; also returns the sample's
+    outputs for the parity check against the product."""
+    threads = os.cpu_count() or 1
+    rates, out, desc, total = [], None, "", 0.0
+    while len(rates) < 3 or (total < seconds and len(rates) < 20):
+        steps, dt, out, desc = cpu_sample(name, cfg, rp, col, threads)
+        rates.append(steps / dt)
+        total += dt
+    value = statistics.median(rates)
+    return ({"value": value, "unit": "steps/s", "cores": threads, "kind": "port",
+             "sample": f"{desc}; median of {len(rates)} samples, {total:.1f} s of CPU work"}, out)
 
 
-def cpu_batch_rate(cfg, rp, col, seconds):
-    """Oracle over the first queries of the batch workload (one query at a
-    time, OpenMP over its walkers) for about `seconds`."""
-    import oracle
-    sources, walkers, seeds = c3_queries(cfg, rp)
-    t0 = time.perf_counter()
-    done, hops, q = 0.0, 0, 0
-    while done < seconds and q < len(sources):
-        _, _, st = oracle.ppr(rp, col, int(sources[q]), int(walkers[q]), prob=cfg["prob"], seed=int(seeds[q]))
-        hops += int(st[1])
-        q += 1
-        done = time.perf_counter() - t0
-    return hops / done, f"first {q} of {len(sources)} queries ({hops} hops, {done:.1f} s)"
+def workload_config(name, cfg, V, E, P):
+    """The workload the line is measured on (identical in both arms)."""
+    c = {"workload": cfg["workload"], "V": V, "E": E, "partitions": P, "partition_mb": cfg["part_mb"]}
+    if "partitions" in cfg:
+        c.update({"cached_partitions": cfg["partitions"],
+                  "device_graph_bytes": cfg["partitions"] * (cfg["part_mb"] << 20),
+                  "walker_pool": cfg["batch"], "walkers": 2 * V, "source": 0, "prob": cfg["prob"],
+                  "l2": "graph (%d GiB) in host memory, far larger than L2; device cache dropped before every step"
+                        % ((8 * (V + 1) + 4 * E) >> 30)})
+    elif cfg.get("batch_queries"):
+        c.update({"queries": cfg["queries"], "zipf": cfg["zipf"],
+                  "walks": "lognormal median %g sigma %g in [%g, %g]" % (cfg["walk_median"], cfg["walk_sigma"],
+                                                                         cfg["walk_min"], cfg["walk_max"]),
+                  "prob": cfg["prob"], "l2": "graph (%d MiB) larger than L2, no flush" % ((8 * (V + 1) + 4 * E) >> 20)})
+    else:
+        gb = 8 * (V + 1) + 4 * E
+        c.update({"walkers": 2 * V, "length": cfg["length"], "prob": cfg["prob"], "start": cfg["start"],
+                  "l2": ("inputs larger than L2 (graph %d MiB > 129 MB L2), no flush" % (gb >> 20)) if gb > 129e6
+                  else "graph (%d MiB) fits in L2 and is not flushed: a parity case, not a bench line" % (gb >> 20)})
+    return c
 
 
 def reference_arm(args, cfg):
+    """The CPU restatement of the reference's walk semantics (oracle/, its
+    App::update pinned to the reference's own code) on the host cores, over
+    a bounded sample of the same workload per step.  The input graph is made
+    by the oracle's CPU generator (bit-identical to the GPU generator): no
+    GPU and no library of this repository is used in this arm."""
     ws, rank, local = dist_env()
     if rank != 0:
         return 0
+    import oracle
     threads = os.cpu_count() or 1
-    if cfg["scale"] >= 26:
-        # input graph only: the oracle's CPU generator would take tens of minutes
-        import lighttraffic_gb300 as lt
-        g = lt.Graph.rmat(cfg["scale"], cfg["edges"], seed=SEED_GRAPH, part_bytes=cfg["part_mb"] << 20,
-                          device=local)
-        rp, col = g.csr_views()
-    else:
-        import oracle
-        g = None
-        rp, col = oracle.rmat(cfg["scale"], cfg["edges"], seed=SEED_GRAPH)
-    per_step = max(1.0, min(6.0, 150.0 / max(1, args.steps + args.warmup)))
-    rates, desc = [], ""
+    t0 = time.perf_counter()
+    rp, col = oracle.rmat(cfg["scale"], cfg["edges"], seed=SEED_GRAPH)
+    node_off, _ = oracle.partition(rp, cfg["part_mb"] << 20)
+    setup_s = time.perf_counter() - t0
+    V, E, P = len(rp) - 1, len(col), len(node_off) - 1
+    rates, desc, total = [], "", 0.0
     for i in range(args.warmup + args.steps):
-        if cfg.get("batch_queries"):
-            r, desc = cpu_batch_rate(cfg, rp, col, per_step)
-        else:
-            r, desc = cpu_rate(cfg, rp, col, per_step, threads)
+        steps, dt, _, desc = cpu_sample(args.config, cfg, rp, col, threads)
         if i >= args.warmup:
-            rates.append(r)
+            rates.append(steps / dt)
+            total += dt
     value = statistics.median(rates)
     line = {
         "impl": "reference", "metric": "walk steps/s", "value": value, "unit": "steps/s",
-        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": None,
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": total / len(rates) * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64",
         "data": "synthetic RMAT (seeded), stand-in for the reference datasets",
-        "config": {"workload": cfg["workload"], "V": len(rp) - 1, "E": len(col), "walkers": 2 * (len(rp) - 1)},
-        "cpu_baseline": {"value": value, "unit": "steps/s", "cores": threads, "kind": "port", "sample": desc},
+        "config": workload_config(args.config, cfg, V, E, P),
+        "cpu_baseline": {"value": value, "unit": "steps/s", "cores": threads, "kind": "port",
+                         "sample": f"{desc} per step; median of {len(rates)} steps"},
         "e2e": {"value": value, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "setup": {"graph_generation_s": setup_s, "generator": "oracle (CPU, OpenMP)"},
     }
     print(json.dumps(line), flush=True)
-    del g
     return 0
 
 
@@ -288,6 +330,42 @@ def link_bytes(s):
     return s["h2d_graph_bytes"] + s["h2d_walker_bytes"] + s["d2h_walker_bytes"] + s["zerocopy_bytes"]
 
 
+def serve_rate(lt, e, cfg, V, rate, seconds, seed):
+    """Serve a Poisson trace at `rate` queries/s on engine e (continuous
+    batching through lt_serve_*); p50 / p99 latency from arrival to result."""
+    srv = lt.Server(e, max_active=4096, table_slots=1 << 27, prob=cfg["prob"])
+    t, src, w, seeds = serve_trace(cfg, V, rate, seconds, seed)
+    n = len(t)
+    lat = []
+    nxt = 0
+    t0 = lt.Server.now_ms()
+    while len(lat) < n:
+        now = lt.Server.now_ms() - t0
+        while nxt < n and t[nxt] <= now:
+            srv.submit(int(src[nxt]), int(w[nxt]), int(seeds[nxt]), arrival_ms=t0 + float(t[nxt]))
+            nxt += 1
+        c, a, p = srv.step()
+        if c:
+            for tk in srv.finished():
+                lat.append(srv.latency_ms(tk))
+                srv.result(tk)
+        if a == 0 and p == 0 and nxt < n:
+            time.sleep(max(0.0, (t[nxt] - (lt.Server.now_ms() - t0)) / 1e3))
+    span_s = (lt.Server.now_ms() - t0) / 1e3
+    srv.close()
+    st = e.stats()
+    lat = np.array(lat)
+    return {"queries": n, "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+            "span_s": span_s, "walkers": int(w.sum()), "steps": st["moves"], "steps_per_s": st["moves"] / span_s,
+            "bytes_per_step": link_bytes(st) / max(1, st["moves"]), "iterations": st["iterations"],
+            "partition_loads": st["partition_loads"]}
+
+
+def spread(xs):
+    return {"min": min(xs), "median": statistics.median(xs), "max": max(xs),
+            "stdev": statistics.stdev(xs) if len(xs) > 1 else 0.0}
+
+
 def gb300_ooc(args, cfg):
     ws, rank, local = dist_env()
     dist = None
@@ -297,145 +375,188 @@ def gb300_ooc(args, cfg):
     import lighttraffic_gb300 as lt
 
     g = lt.Graph.rmat(cfg["scale"], cfg["edges"], seed=SEED_GRAPH, part_bytes=cfg["part_mb"] << 20, device=local)
-    V, E = g.num_nodes, g.num_edges
+    V, E, P = g.num_nodes, g.num_edges, g.num_partitions
     W = 2 * V
     link_peak = lt.host_link_gbs(local)
     counts = lt.pinned_empty(V, np.uint64)   # host count buffer in page-locked memory
     clocks = ClockSampler(local)
     clocks.start()
     time.sleep(0.3)
-    # learned = the headline; plain = the reference policy; batched and
-    # frequency = wave runs without predictions / with a moving average
-    scheds = {"learned": lt.SCHED_LEARNED, "plain": lt.SCHED_PLAIN, "batched": lt.SCHED_BATCHED,
-              "frequency": lt.SCHED_FREQUENCY}
-
+    thr_ref = (cfg["part_mb"] << 20) // 128 // 2   # src/Scheduler.h:295
+    # learned = the headline; plain = the reference policy (one partition per
+    # iteration, its zero-copy threshold, load / compute overlap on);
+    # plain_x8 = the same at the threshold the wave runs use (x8: 32 B per
+    # zero-copy hop measured, against the 256 B the reference's rule
+    # assumes); batched / frequency = wave runs without predictions / with a
+    # moving average; *_host_index = the reference's slot layout (rowptr
+    # slices travel with the partitions).  The default layout keeps the
+    # vertex index on the device inside the -p budget (fewer slots).
+    variants = {"learned": dict(sched=lt.SCHED_LEARNED), "plain": dict(sched=lt.SCHED_PLAIN),
+                "plain_x8": dict(sched=lt.SCHED_PLAIN, zerocopy_threshold=8 * thr_ref),
+                "batched": dict(sched=lt.SCHED_BATCHED), "frequency": dict(sched=lt.SCHED_FREQUENCY),
+                "learned_host_index": dict(sched=lt.SCHED_LEARNED, resident_index=False),
+                "plain_host_index": dict(sched=lt.SCHED_PLAIN, resident_index=False)}
+    K = args.steps
+    n_timed = {"learned": K, "batched": K, "frequency": K, "plain": min(K, 5), "plain_x8": min(K, 5),
+               "learned_host_index": min(K, 3), "plain_host_index": min(K, 3)}
     engines = {}
-    zc_all = [0]   # modelled zero-copy bytes over every run, warm-up included
+    ref_counts = [None]
+    checked = [0]
     first_run = {}       # the process's first run (for a profiler capture of exactly its step kernels)
 
     def one_run(name):
-        # one engine per scheduler for the whole benchmark (its pinned host
-        # spill slabs and the prefetcher's training persist); the device cache
-        # is emptied before every run, so each run starts cold
+        # one engine per variant for the whole benchmark (its pinned host
+        # spill slabs and the prefetcher's training persist); the device
+        # cache is emptied before every run, so each run starts cold
         if name not in engines:
             engines[name] = lt.Engine(g, partitions=cfg["partitions"], batch=cfg["batch"], seed=SEED_WALK,
-                                      sched=scheds[name], device=local)
+                                      device=local, **variants[name])
         e = engines[name]
         e.drop_cache()
         t0 = time.perf_counter()
         e.ppr(0, W, cfg["prob"], out=counts)
         t1 = time.perf_counter()
-        assert int(counts.sum()) == W, "PPR invariant (one count per walk) violated"
+        # every run of every variant must give the first run's counts, bit
+        # for bit (outside the timed interval)
+        if ref_counts[0] is None:
+            assert int(counts.sum()) == W, "PPR invariant (one count per walk) violated"
+            ref_counts[0] = counts.copy()
+        else:
+            assert np.array_equal(counts, ref_counts[0]), f"{name}: counts differ from the first run"
+        checked[0] += 1
         st = e.stats()
-        zc_all[0] += st["zerocopy_bytes"]
         if not first_run:
             first_run.update(sched=name, step_launches=st["computing_calls"] + st["zerocopy_calls"],
                              zero_copy_bytes=st["zerocopy_bytes"])
         return (t1 - t0, st, e.policy_stats())
 
-    # W warm-up runs of the headline (learned) and of the reference policy;
-    # one of each ablation (its code paths warm) keeps the link traffic
-    # before the timed runs down
     for i in range(args.warmup):
-        for name in scheds:
-            if i == 0 or name in ("learned", "plain"):
+        for name in variants:
+            if i == 0 or name == "learned":
                 one_run(name)
     if dist:
         dist.barrier()
     wall0 = time.time()
-    times = {name: [] for name in scheds}
+    times = {name: [] for name in variants}
     stats, pstats = {}, {}
-    order = list(scheds)
-    for k in range(args.steps):
+    order = list(variants)
+    for k in range(K):
         for name in (order if k % 2 == 0 else order[::-1]):
-            dt, st, ps = one_run(name)
-            times[name].append(dt)
-            stats[name], pstats[name] = st, ps
+            if k < n_timed[name]:
+                dt, st, ps = one_run(name)
+                times[name].append(dt)
+                stats[name], pstats[name] = st, ps
+    wall1 = time.time()
     # host-link bandwidth again after the timed runs: on these shared hosts it
     # can drop during a call (contention outside this process)
     link_after = lt.host_link_gbs(local)
-    results = {}
-    for name in scheds:
-        s = stats[name]
-        results[name] = {"elapsed": max_over_ranks(dist, local, sum(times[name])), "stats": s,
-                         "policy": pstats[name], "steps": s["moves"], "times": times[name]}
+    res = {}
+    for name in variants:
+        st = stats[name]
+        el = max_over_ranks(dist, local, sum(times[name]))
+        res[name] = {"value": st["moves"] * len(times[name]) * ws / el,
+                     "bytes_per_step": link_bytes(st) / st["moves"],
+                     "ms_per_step": el / len(times[name]) * 1e3, "runs": len(times[name]),
+                     "iterations": st["iterations"], "partition_loads": st["partition_loads"],
+                     "zerocopy_groups": st["zerocopy_groups"], "zerocopy_sweeps": st["zerocopy_sweeps"],
+                     "overlap_computes": st["overlap_computes"], "cache_slots": st["cache_slots"],
+                     "index_on_device": bool(st["index_on_device"]), "step_s": spread(times[name])}
+        if pstats[name]["name"] in ("learned", "frequency"):
+            res[name]["policy"] = pstats[name]
+
+    # serving latency on the same graph and cache (the c4 workload at 1 000
+    # queries/s), learned against the reference loop
+    serving = {}
+    c4 = CONFIGS["c4"]
+    for name in ("learned", "plain"):
+        serving[name] = serve_rate(lt, engines[name], c4, V, 1000, 2.0, SEED_WALK + 1000)
     clocks.stop()
-    clk = clocks.summary(wall0 - 0.5, time.time())
+    clk = clocks.summary(wall0 - 0.5, wall1)
+
+    # the oracle sample of the cpu_baseline leg, and the same walkers through
+    # the product: identical counts
+    parity = {"cross_variant_runs_identical": checked[0]}
+    cpu = None
+    if not args.no_cpu_baseline and ws == 1:
+        rp, col = g.csr_views()
+        cpu, sample_counts = cpu_baseline_leg(args.config, cfg, rp, col, args.cpu_seconds)
+        n = SAMPLES[args.config]["walkers"] or W
+        got = engines["learned"].ppr(0, min(n, W), cfg["prob"])
+        assert np.array_equal(got, sample_counts), "product and oracle differ on the sample"
+        parity["oracle_sample_identical"] = {"walkers": min(n, W), "identical": True}
     if rank != 0:
         if dist:
             dist.destroy_process_group()
         return 0
-    L, Pn = results["learned"], results["plain"]
-    value = L["steps"] * args.steps * ws / L["elapsed"]
-    plain_value = Pn["steps"] * args.steps * ws / Pn["elapsed"]
-    s = L["stats"]
+    L, Pn, P8 = res["learned"], res["plain"], res["plain_x8"]
+    s = stats["learned"]
+    value = L["value"]
+    el_learned = L["ms_per_step"] / 1e3
     launches = s["computing_calls"] + s["zerocopy_calls"]
-    # step kernel: 20 B per hop (rowptr pair + col), 16 B per count (one per
-    # walk), 48 B per hand-off (walker read + staged write + scatter read +
-    # queue write, 12 B each)
+    # step kernel, HBM side: 20 B per hop (rowptr pair + col), 16 B per count
+    # (one per walk), 48 B per hand-off (walker read + staged write + scatter
+    # read + queue write, 12 B each)
     alg = 20 * s["moves"] + 16 * W + 48 * s["handoffs"]
     kern_s = max(s["step_kernel_ms"], 1e-6) / 1e3
-    peak, peak_src = measured_peak("hbm_gbs", 6800.0)
-    achieved = alg / kern_s / 1e9
+    hbm_peak, peak_src = measured_peak("hbm_gbs", 6800.0)
+    run_link = link_bytes(s)
+    stronger = Pn if Pn["value"] >= P8["value"] else P8
     line = {
-        "metric": "walk steps/s", "value": value, "unit": "steps/s", "n_gpus": ws, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": L["elapsed"] / args.steps * 1e3, "higher_is_better": True,
+        "metric": "walk steps/s", "value": value, "unit": "steps/s", "n_gpus": ws, "steps": K,
+        "warmup": args.warmup, "ms_per_step": L["ms_per_step"], "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "u64",
         "data": "synthetic RMAT (seeded), stand-in for the reference datasets",
-        "config": {"workload": cfg["workload"], "V": V, "E": E, "partitions": g.num_partitions,
-                   "cached_partitions": cfg["partitions"], "walker_pool": cfg["batch"], "walkers": W,
-                   "prob": cfg["prob"], "scheduler": "learned",
-                   "vertex_index": "on the device (rowptr, %d MiB); partitions move only their edges"
-                                   % ((8 * (V + 1)) >> 20),
-                   "l2": "graph (%d GiB) in host memory, far larger than L2; cache dropped before every step"
-                         % ((8 * (V + 1) + 4 * E) >> 30),
-                   "parallelism": "replicas" if ws > 1 else "1 GPU"},
-        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": profiled_traffic(cfg["workload"]), "kernel": "walk_part_kernel",
-                     "alg_bytes_per_launch": alg / max(1, launches),
-                     "mean_launch_ms": s["step_kernel_ms"] / max(1, launches), "launches": launches,
-                     "peak_source": peak_src},
-        # the resource that bounds an out-of-core run: host-link bytes (graph
-        # loads, zero-copy reads at the measured bytes per hop, walker spills) over the run time,
-        # against the measured pinned H2D bandwidth
-        "host_link": {"bytes_per_step": link_bytes(s) / s["moves"],
-                      "achieved_gbs": link_bytes(s) / (L["elapsed"] / args.steps) / 1e9,
-                      "peak_gbs": link_peak, "frac": link_bytes(s) / (L["elapsed"] / args.steps) / 1e9 / link_peak,
-                      "peak_gbs_after_timed_runs": link_after,
-                      "bytes_by_kind": {name: {"graph_loads": results[name]["stats"]["h2d_graph_bytes"],
-                                               "zero_copy": results[name]["stats"]["zerocopy_bytes"],
-                                               "walker_spill": results[name]["stats"]["h2d_walker_bytes"]
-                                               + results[name]["stats"]["d2h_walker_bytes"]} for name in scheds},
-                      "zero_copy_bytes_all_runs": zc_all[0],
+        "config": workload_config(args.config, cfg, V, E, P),
+        "scheduler": "learned (wave runs, cache slots by the online-trained network's predicted visits)",
+        "layout": "vertex index on the device (%d MiB) inside the %d GiB graph budget: %d partition slots"
+                  % ((8 * (V + 1)) >> 20, (cfg["partitions"] * (cfg["part_mb"] << 20)) >> 30, s["cache_slots"]),
+        # the resource an out-of-core run spends: host-link bytes (graph
+        # loads and walker spills counted exactly, zero-copy reads at the
+        # bytes per hop measured with ncu) over the run time, against the
+        # pinned H2D bandwidth measured in this run
+        "roofline": {"bound": "host_link", "achieved": run_link / el_learned / 1e9, "peak": link_peak,
+                     "unit": "GB/s", "frac": run_link / el_learned / 1e9 / link_peak, "traffic": run_link,
+                     "traffic_is": "host-link bytes per step (run): graph H2D + zero-copy + walker spill",
+                     "kernel": "whole run (walk_part_kernel zero-copy reads, partition copies, spills)",
+                     "peak_source": "pinned H2D copy measured in this run, before the warm-up",
+                     "hbm": {"kernel": "walk_part_kernel", "achieved": alg / kern_s / 1e9, "peak": hbm_peak,
+                             "unit": "GB/s", "frac": alg / kern_s / 1e9 / hbm_peak,
+                             "alg_bytes_per_launch": alg / max(1, launches),
+                             "mean_launch_ms": s["step_kernel_ms"] / max(1, launches), "launches": launches,
+                             "traffic": profiled_traffic(cfg["workload"]), "peak_source": peak_src}},
+        "host_link": {"bytes_per_step": run_link / s["moves"], "achieved_gbs": run_link / el_learned / 1e9,
+                      "peak_gbs": link_peak, "peak_gbs_after_timed_runs": link_after,
+                      "bytes_by_kind": {"graph_loads": s["h2d_graph_bytes"], "zero_copy": s["zerocopy_bytes"],
+                                        "walker_spill": s["h2d_walker_bytes"] + s["d2h_walker_bytes"]},
                       "first_run": first_run,
-                      "peak_source": "measured pinned H2D copy in this run, before the warm-up",
-                      "zerocopy_bytes": "32 B per zero-copy hop (col only; the vertex index is on the device), "
-                                        "measured with ncu on this workload"},
-        "plain": {"value": plain_value, "bytes_per_step": link_bytes(Pn["stats"]) / Pn["steps"],
-                  "iterations": Pn["stats"]["iterations"], "partition_loads": Pn["stats"]["partition_loads"],
-                  "ms_per_step": Pn["elapsed"] / args.steps * 1e3, "step_s": Pn["times"]},
-        "learned": {"value": value, "bytes_per_step": link_bytes(s) / s["moves"], "iterations": s["iterations"],
-                    "partition_loads": s["partition_loads"], "policy": L["policy"], "step_s": L["times"]},
-        "learned_over_plain": {"steps_per_s": value / plain_value,
-                               "bytes_per_step": (link_bytes(s) / s["moves"]) / (link_bytes(Pn["stats"]) / Pn["steps"])},
-        "ablations": {name: {"value": results[name]["steps"] * args.steps * ws / results[name]["elapsed"],
-                             "bytes_per_step": link_bytes(results[name]["stats"]) / results[name]["steps"],
-                             "iterations": results[name]["stats"]["iterations"],
-                             "partition_loads": results[name]["stats"]["partition_loads"],
-                             "step_s": results[name]["times"]}
-                      for name in ("batched", "frequency")},
+                      "zerocopy_bytes": "32 B per zero-copy hop with the vertex index on the device (62 B "
+                                        "without), measured with ncu"},
+        "variants": res,
+        "learned_over_plain": {
+            "vs_plain": {"steps_per_s": value / Pn["value"], "bytes_per_step": L["bytes_per_step"] / Pn["bytes_per_step"]},
+            "vs_plain_x8": {"steps_per_s": value / P8["value"], "bytes_per_step": L["bytes_per_step"] / P8["bytes_per_step"]},
+            "vs_stronger_plain": {"which": "plain" if stronger is Pn else "plain_x8",
+                                  "steps_per_s": value / stronger["value"],
+                                  "bytes_per_step": L["bytes_per_step"] / stronger["bytes_per_step"]},
+            "host_index_layout": {
+                "steps_per_s": res["learned_host_index"]["value"] / res["plain_host_index"]["value"],
+                "bytes_per_step": res["learned_host_index"]["bytes_per_step"] / res["plain_host_index"]["bytes_per_step"]}},
+        "learned_over_ablations": {n: {"steps_per_s": value / res[n]["value"],
+                                       "bytes_per_step": L["bytes_per_step"] / res[n]["bytes_per_step"]}
+                                   for n in ("batched", "frequency")},
+        "serving_1000qps": serving,
+        "parity": parity,
         "e2e": {"value": value, "unit": "steps/s", "h2d_bytes_per_step": s["h2d_graph_bytes"] + s["h2d_walker_bytes"],
                 "d2h_bytes_per_step": 8 * V + s["d2h_walker_bytes"],
                 "note": "each step is a full run through lt_run_ppr from a cold cache with host output buffers"},
-        "gpu_launches": s["kernel_launches"] * args.steps,
+        "gpu_launches": s["kernel_launches"] * K,
         "clocks": clk,
     }
-    if not args.no_cpu_baseline and ws == 1:
-        rp, col = g.csr_views()
-        r, desc = cpu_rate(cfg, rp, col, args.cpu_seconds, os.cpu_count() or 1)
-        line["cpu_baseline"] = {"value": r, "unit": "steps/s", "cores": os.cpu_count() or 1, "kind": "port",
-                                "sample": desc}
+    if cpu:
+        line["cpu_baseline"] = cpu
     print(json.dumps(line), flush=True)
+    for e in engines.values():
+        e.close()
     if dist:
         dist.destroy_process_group()
     return 0
@@ -551,10 +672,8 @@ def gb300_resident(args, cfg):
         "warmup": args.warmup, "ms_per_step": elapsed_ms / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "u64",
         "data": "synthetic RMAT (seeded), stand-in for the reference datasets",
-        "config": {"workload": cfg["workload"], "V": V, "E": E, "partitions": g.num_partitions, "walkers": W,
-                   "length": length, "steps_per_pass": steps_per_pass,
-                   "l2": "inputs larger than L2 (graph %d MiB > 129 MB L2), no flush" % ((8 * (V + 1) + 4 * E) >> 20),
-                   "parallelism": "replicas" if ws > 1 else "1 GPU"},
+        "config": workload_config(args.config, cfg, V, E, g.num_partitions),
+        "steps_per_pass": steps_per_pass, "parallelism": "replicas" if ws > 1 else "1 GPU",
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": profiled_traffic(cfg["workload"] + ("-compact" if compact_ok else "")),
                      "kernel": "walk_whole_kernel" + (" (compact layout)" if compact_ok else ""),
@@ -570,9 +689,10 @@ def gb300_resident(args, cfg):
         "stats_per_pass": {"updates": updates, "moves": moves, "teleports": tele},
     }
     if not args.no_cpu_baseline and ws == 1:
-        r, desc = cpu_rate(cfg, rp, col, args.cpu_seconds, os.cpu_count() or 1)
-        line["cpu_baseline"] = {"value": r, "unit": "steps/s", "cores": os.cpu_count() or 1, "kind": "port",
-                                "sample": desc}
+        # the sample is the whole pass: the oracle's counts equal the product's
+        line["cpu_baseline"], want = cpu_baseline_leg(args.config, cfg, rp, col, args.cpu_seconds)
+        assert np.array_equal(host_counts, want), "product and oracle counts differ"
+        line["parity"] = {"oracle_identical": {"walkers": W, "identical": True}}
     print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()
@@ -670,10 +790,8 @@ def gb300_batch(args, cfg):
         "warmup": args.warmup, "ms_per_step": elapsed_ms / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "u32",
         "data": "synthetic RMAT (seeded) and synthetic Zipf / lognormal queries",
-        "config": {"workload": cfg["workload"], "V": V, "E": E, "queries": n, "walkers": Wt,
-                   "sparse_pairs": pairs, "autotune": tune,
-                   "l2": "graph (%d MiB) larger than L2, no flush" % ((8 * (V + 1) + 4 * E) >> 20),
-                   "parallelism": "replicas" if ws > 1 else "1 GPU"},
+        "config": workload_config(args.config, cfg, V, E, g.num_partitions),
+        "walkers": Wt, "sparse_pairs": pairs, "autotune": tune, "parallelism": "replicas" if ws > 1 else "1 GPU",
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": profiled_traffic(cfg["workload"]), "kernel": "batch pipeline (walk + tables)",
                      "alg_bytes_per_launch": alg, "mean_launch_ms": st["step_kernel_ms"], "peak_source": peak_src},
@@ -684,9 +802,12 @@ def gb300_batch(args, cfg):
         "clocks": clk,
     }
     if not args.no_cpu_baseline and ws == 1:
-        r, desc = cpu_batch_rate(cfg, rp, col, args.cpu_seconds)
-        line["cpu_baseline"] = {"value": r, "unit": "steps/s", "cores": os.cpu_count() or 1, "kind": "port",
-                                "sample": desc}
+        line["cpu_baseline"], want = cpu_baseline_leg(args.config, cfg, rp, col, args.cpu_seconds)
+        for q, (vs, cs) in enumerate(want):
+            a, b = int(off[q]), int(off[q + 1])
+            order = np.argsort(v[a:b], kind="stable")
+            assert np.array_equal(v[a:b][order], vs) and np.array_equal(c[a:b][order], cs), f"query {q} differs"
+        line["parity"] = {"oracle_identical": {"queries": len(want), "identical": True}}
     print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()
@@ -722,36 +843,7 @@ def gb300_serve(args, cfg):
         e = lt.Engine(g, partitions=cfg["partitions"], batch=cfg["batch"], seed=SEED_WALK, sched=sched, device=local)
         per_rate = {}
         for rate, seconds in zip(cfg["rates"], cfg["seconds"]):
-            srv = lt.Server(e, max_active=4096, table_slots=1 << 27, prob=cfg["prob"])
-            t, src, w, seeds = serve_trace(cfg, V, rate, seconds, SEED_WALK + rate)
-            n = len(t)
-            lat = []
-            nxt = 0
-            t0 = lt.Server.now_ms()
-            steps0 = e.stats()
-            while len(lat) < n:
-                now = lt.Server.now_ms() - t0
-                while nxt < n and t[nxt] <= now:
-                    srv.submit(int(src[nxt]), int(w[nxt]), int(seeds[nxt]), arrival_ms=t0 + float(t[nxt]))
-                    nxt += 1
-                c, a, p = srv.step()
-                if c:
-                    for tk in srv.finished():
-                        lat.append(srv.latency_ms(tk))
-                        srv.result(tk)
-                if a == 0 and p == 0 and nxt < n:
-                    time.sleep(max(0.0, (t[nxt] - (lt.Server.now_ms() - t0)) / 1e3))
-            span_s = (lt.Server.now_ms() - t0) / 1e3
-            srv.close()
-            st = e.stats()
-            lat = np.array(lat)
-            link = link_bytes(st)
-            per_rate[str(rate)] = {"queries": n, "p50_ms": float(np.percentile(lat, 50)),
-                                   "p99_ms": float(np.percentile(lat, 99)), "span_s": span_s,
-                                   "walkers": int(w.sum()), "steps": st["moves"],
-                                   "steps_per_s": st["moves"] / span_s,
-                                   "bytes_per_step": link / max(1, st["moves"]),
-                                   "iterations": st["iterations"], "partition_loads": st["partition_loads"]}
+            per_rate[str(rate)] = serve_rate(lt, e, cfg, V, rate, seconds, SEED_WALK + rate)
         out[name] = per_rate
         e.close()
     clocks.stop()

@@ -84,7 +84,10 @@ typedef struct lt_graph_info {
 
 typedef struct lt_engine_cfg {
     int device;                      /* CUDA device ordinal (the reference fixes 0, app/ppr.cu:101) */
-    uint32_t num_device_partitions;  /* -p: partitions cached on the device (0 = all) */
+    uint32_t num_device_partitions;  /* -p: the graph gets num_device_partitions x partition size bytes
+                                        of device memory, as in the reference (src/GraphLoader.h:
+                                        175-178); with resident_index the vertex index is paid from
+                                        that budget, leaving fewer partition slots (0 = all cached) */
     uint64_t num_device_walkers;     /* -b: walkers held on the device (0 = all) */
     int sched;                       /* lt_sched */
     int pipeline;                    /* overlap partition loads with stepping (1 = on; 0 = loads
@@ -101,7 +104,8 @@ typedef struct lt_engine_cfg {
     int resident_index;              /* out-of-core: keep the vertex index (rowptr, 8 (V+1) bytes) on
                                         the device, so partition loads copy only edges and zero-copy
                                         hops read only col over the host link (1 = on, the default,
-                                        falling back to 0 when the index does not fit; 0 = the
+                                        falling back to 0 when the index does not fit in the -p
+                                        budget with at least one slot beside it; 0 = the
                                         reference's layout, rowptr slices in the slots,
                                         src/GraphLoader.h:193-214) */
 } lt_engine_cfg;
@@ -138,6 +142,8 @@ typedef struct lt_stats {
                                   partitions zero-copy */
     uint64_t zerocopy_sweeps;  /* wave runs: step kernels that read every uncached partition
                                   zero-copy to finish the last walkers */
+    uint64_t cache_slots;      /* out of core: partition slots on the device */
+    uint64_t index_on_device;  /* out of core: 1 when the vertex index is resident on the device */
 } lt_stats;
 
 const char *lt_strerror(lt_status s);

@@ -82,7 +82,8 @@ class Stats(C.Structure):
                 ("zerocopy_calls", C.c_uint64), ("walker_loading_calls", C.c_uint64),
                 ("walker_evicting_calls", C.c_uint64), ("step_kernel_ms", C.c_double),
                 ("handoffs", C.c_uint64), ("overlap_computes", C.c_uint64),
-                ("zerocopy_groups", C.c_uint64), ("zerocopy_sweeps", C.c_uint64)]
+                ("zerocopy_groups", C.c_uint64), ("zerocopy_sweeps", C.c_uint64),
+                ("cache_slots", C.c_uint64), ("index_on_device", C.c_uint64)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}

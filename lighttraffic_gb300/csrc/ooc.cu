@@ -1142,7 +1142,23 @@ lt_status ooc_create(lt_engine *e, Ooc **out)
     uint64_t max_slot = 0;
     for (uint32_t p = 0; p < o->P; p++) max_slot = std::max<uint64_t>(max_slot, host_part_bytes(*o, p) + 16);
     o->slot_stride = (max_slot + 255) & ~255ull;
-    if (!o->d_index) o->slot_stride = std::max<uint64_t>(o->slot_stride, (g.part_bytes + 16 + 255) & ~255ull);
+    // -p P gives the graph P x partitionSize bytes of device memory, as the
+    // reference allocates (src/GraphLoader.h:176-190); a resident vertex
+    // index is paid from that budget, leaving fewer slots.  Where it leaves
+    // none, the slots carry rowptr slices instead.
+    if (o->d_index) {
+        const uint64_t budget = (uint64_t)o->K * g.part_bytes, index_bytes = 8ull * ((uint64_t)g.V + 1);
+        const uint64_t fit = budget > index_bytes ? (budget - index_bytes) / o->slot_stride : 0;
+        if (fit >= 1) {
+            o->K = (uint32_t)std::min<uint64_t>(o->K, fit);
+        } else {
+            cudaFree(o->d_index);
+            o->d_index = nullptr;
+            max_slot = 0;
+            for (uint32_t p = 0; p < o->P; p++) max_slot = std::max<uint64_t>(max_slot, host_part_bytes(*o, p) + 16);
+        }
+    }
+    if (!o->d_index) o->slot_stride = std::max<uint64_t>((max_slot + 255) & ~255ull, (g.part_bytes + 16 + 255) & ~255ull);
     lt_status s = dalloc(&o->d_slots, (uint64_t)o->K * o->slot_stride);
     if (s == LT_OK) s = dalloc(&o->d_node_off, o->P + 1);
     if (s == LT_OK) s = dalloc(&o->d_edge_off, o->P + 1);
@@ -1604,6 +1620,8 @@ lt_status run_setup(lt_engine *e, RunParams &rp, int app, int start, uint32_t so
     if (W >= (1ull << 32)) return fail(LT_ERR_INVALID, "out-of-core runs take fewer than 2^32 walkers per run");
     LT_TRY(ensure_pool(o, W));
     e->stats = lt_stats{};
+    e->stats.cache_slots = o.K;
+    e->stats.index_on_device = o.d_index != nullptr;
     cudaStream_t st = e->s_compute;
     if (app != kWalk) LT_CUDA_TRY(cudaMemsetAsync(e->d_counts, 0, 8ull * g.V, st));
     LT_CUDA_TRY(cudaMemsetAsync(o.d_stats, 0, 64, st));
@@ -2104,6 +2122,8 @@ lt_status serve_open(lt_engine *e, uint32_t max_active, uint64_t table_slots, fl
     refresh_all(o);
     cudaMemsetAsync(o.d_stats, 0, 64, e->s_compute);
     e->stats = lt_stats{};
+    e->stats.cache_slots = o.K;
+    e->stats.index_on_device = o.d_index != nullptr;
     o.serve = s;
     if (o.policy->wave()) s->wave = new WaveState(o.P);
     *out = s;

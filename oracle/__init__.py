@@ -64,6 +64,8 @@ def lib():
         L.orc_partition.argtypes = [u64p, C.c_uint32, C.c_uint64, u32p, u64p, C.c_uint32, u32p]
         L.orc_rmat_degrees.argtypes = [C.c_int, C.c_uint64, C.c_uint64, C.c_uint32, u64p, C.c_int]
         L.orc_rmat_fill.argtypes = [C.c_int, C.c_uint64, C.c_uint32, C.c_uint32, u64p, u32p, C.c_int]
+        L.orc_rmat_compact.argtypes = [C.c_uint64, C.c_uint64, u64p, u32p, u32p, C.POINTER(C.c_uint8), u64p,
+                                       C.POINTER(C.c_uint64), C.c_int]
         _lib = L
     return _lib
 
@@ -219,13 +221,17 @@ def rmat(scale, edges, seed=1, a=0.57, b=0.19, c=0.19, d=0.05, remove_isolated=T
     L.orc_rmat_fill(scale, seed, t_d0, t_d1, _p(rowptr, C.c_uint64), _p(col, C.c_uint32), threads)
     if not remove_isolated:
         return rowptr, col
-    # tools/rm_isolated_vertices.cc:70-87: keep vertices that appear in any edge, in order.
-    present = deg > 0
-    present[col] = True
-    newid = np.cumsum(present, dtype=np.uint64) - 1
-    rp = np.zeros(int(present.sum()) + 1, dtype=np.uint64)
-    np.cumsum(deg[present], out=rp[1:])
-    return rp, newid[col].astype(np.uint32)
+    # tools/rm_isolated_vertices.cc:70-87: keep vertices that appear in any
+    # edge, in order (orc_rmat_compact, OpenMP; col is rewritten in place)
+    del deg
+    newid = np.empty(V0, dtype=np.uint32)
+    present = np.empty(V0, dtype=np.uint8)
+    out = np.empty(V0 + 1, dtype=np.uint64)
+    V = C.c_uint64(0)
+    L.orc_rmat_compact(V0, edges, _p(rowptr, C.c_uint64), _p(col, C.c_uint32), _p(newid, C.c_uint32),
+                       _p(present, C.c_uint8), _p(out, C.c_uint64), C.byref(V), threads)
+    del newid, present, rowptr
+    return out[: V.value + 1].copy(), col
 
 
 # ------------------------------------------------- reference partitioner

@@ -372,3 +372,58 @@ int orc_rmat_fill(int scale, uint64_t seed, uint32_t t_d0, uint32_t t_d1,
     }
     return 0;
 }
+
+/*
+ * Phase 3: remove isolated raw vertices (no out-edges and never a
+ * destination), keeping order (tools/rm_isolated_vertices.cc:70-87).
+ *   rowptr : raw u64[V0 + 1] from the degrees
+ *   col    : raw u32[E], rewritten in place to the compacted ids
+ *   newid  : scratch u32[V0]; present : scratch u8[V0]
+ *   out_rp : u64[V0 + 1], not aliasing rowptr; its first *out_V + 1 entries
+ *            are the compacted rowptr (an isolated vertex has no edges, so a
+ *            kept vertex keeps its raw edge offset)
+ */
+int orc_rmat_compact(uint64_t V0, uint64_t E, const uint64_t *rowptr, uint32_t *col, uint32_t *newid,
+                     uint8_t *present, uint64_t *out_rp, uint64_t *out_V, int threads)
+{
+    if (threads <= 0) threads = omp_get_max_threads();
+#pragma omp parallel for schedule(static) num_threads(threads)
+    for (int64_t v = 0; v < (int64_t)V0; v++) present[v] = rowptr[v + 1] > rowptr[v];
+#pragma omp parallel for schedule(static) num_threads(threads)
+    for (int64_t i = 0; i < (int64_t)E; i++) __atomic_store_n(&present[col[i]], (uint8_t)1, __ATOMIC_RELAXED);
+    /* exclusive count of kept vertices: per-thread block sums, then a scan */
+    uint64_t sums[1024];
+    if (threads > 1023) threads = 1023;
+    const uint64_t blk = (V0 + threads - 1) / threads;
+#pragma omp parallel num_threads(threads)
+    {
+        const int t = omp_get_thread_num();
+        const uint64_t b = t * blk, e = b + blk < V0 ? b + blk : V0;
+        uint64_t s = 0;
+        for (uint64_t v = b; v < e; v++) s += present[v];
+        sums[t] = s;
+#pragma omp barrier
+#pragma omp single
+        {
+            uint64_t run = 0;
+            for (int k = 0; k < omp_get_num_threads(); k++) {
+                const uint64_t x = sums[k];
+                sums[k] = run;
+                run += x;
+            }
+            sums[omp_get_num_threads()] = run;
+        }
+        uint64_t id = sums[t];
+        for (uint64_t v = b; v < e; v++) {
+            newid[v] = (uint32_t)id;
+            if (present[v]) out_rp[id++] = rowptr[v];
+        }
+#pragma omp barrier
+#pragma omp single
+        *out_V = sums[omp_get_num_threads()];
+    }
+    out_rp[*out_V] = E;
+#pragma omp parallel for schedule(static) num_threads(threads)
+    for (int64_t i = 0; i < (int64_t)E; i++) col[i] = newid[col[i]];
+    return 0;
+}
