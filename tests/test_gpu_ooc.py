@@ -61,7 +61,12 @@ def test_ppr_ooc(lt, require_gpu, g16, case, index):
         assert s["h2d_graph_bytes"] > 0 and s["zerocopy_calls"] == 0
     if zc == 1 << 40:
         assert s["zerocopy_calls"] > 0
-    if B and sched < 2:
+    if index:
+        # the vertex index is paid from the K x partition-size budget
+        assert 1 <= s["cache_slots"] <= K
+    else:
+        assert s["cache_slots"] == K and s["index_on_device"] == 0
+    if B and sched < 2 and not index:
         assert s["d2h_walker_bytes"] > 0 and s["h2d_walker_bytes"] > 0
 
 
