@@ -85,8 +85,15 @@ __device__ __forceinline__ void ppr_count(const StepArgs &a, uint32_t qs, uint32
     atomicAdd(&a.q_done[qs], 1ull);
 }
 
+// Resident CTAs per SM the register budget is sized for: PPR fits 48
+// registers with no spills (5 x 256 threads), PageRank and generic walks 40
+// (6 x 256); unbounded, PPR took 55 (4 CTAs) and hops in flight were the limit
+// on zero-copy reads.
 template <int APP>
-__global__ void __launch_bounds__(kPartBlock) walk_part_kernel(StepArgs a)
+constexpr int part_min_blocks() { return APP == kPPR ? 5 : 6; }
+
+template <int APP>
+__global__ void __launch_bounds__(kPartBlock, part_min_blocks<APP>()) walk_part_kernel(StepArgs a)
 {
     extern __shared__ uint32_t smem[];
     const uint32_t P = a.t.P;
@@ -121,7 +128,9 @@ __global__ void __launch_bounds__(kPartBlock) walk_part_kernel(StepArgs a)
     unsigned long long cp_rp = 0, cp_col = 0;
     uint64_t cp_eb = 0;
     bool cp_zc = false;
-    uint64_t n_upd = 0, n_mov = 0, n_tel = 0, n_zc = 0, n_exit = 0, n_fin = 0;
+    // per-thread statistics of this launch (a launch makes far fewer than
+    // 2^32 updates per thread); widened in the warp reduction at the end
+    uint32_t n_upd = 0, n_mov = 0, n_tel = 0, n_zc = 0, n_exit = 0, n_fin = 0;
 
     while (true) {
         const unsigned idle = __ballot_sync(kFull, !active);
@@ -319,22 +328,23 @@ __global__ void __launch_bounds__(kPartBlock) walk_part_kernel(StepArgs a)
         }
     }
 
+    uint64_t w_upd = n_upd, w_mov = n_mov, w_tel = n_tel, w_zc = n_zc, w_exit = n_exit, w_fin = n_fin;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
-        n_upd += __shfl_down_sync(kFull, n_upd, o);
-        n_mov += __shfl_down_sync(kFull, n_mov, o);
-        n_tel += __shfl_down_sync(kFull, n_tel, o);
-        n_zc += __shfl_down_sync(kFull, n_zc, o);
-        n_exit += __shfl_down_sync(kFull, n_exit, o);
-        n_fin += __shfl_down_sync(kFull, n_fin, o);
+        w_upd += __shfl_down_sync(kFull, w_upd, o);
+        w_mov += __shfl_down_sync(kFull, w_mov, o);
+        w_tel += __shfl_down_sync(kFull, w_tel, o);
+        w_zc += __shfl_down_sync(kFull, w_zc, o);
+        w_exit += __shfl_down_sync(kFull, w_exit, o);
+        w_fin += __shfl_down_sync(kFull, w_fin, o);
     }
     if (lane == 0) {
-        atomicAdd(&a.stats[0], (unsigned long long)n_upd);
-        atomicAdd(&a.stats[1], (unsigned long long)n_mov);
-        atomicAdd(&a.stats[2], (unsigned long long)n_tel);
-        atomicAdd(&a.stats[3], (unsigned long long)n_zc);
-        atomicAdd(&a.stats[4], (unsigned long long)n_exit);
-        atomicAdd(&a.stats[5], (unsigned long long)n_fin);
+        atomicAdd(&a.stats[0], (unsigned long long)w_upd);
+        atomicAdd(&a.stats[1], (unsigned long long)w_mov);
+        atomicAdd(&a.stats[2], (unsigned long long)w_tel);
+        atomicAdd(&a.stats[3], (unsigned long long)w_zc);
+        atomicAdd(&a.stats[4], (unsigned long long)w_exit);
+        atomicAdd(&a.stats[5], (unsigned long long)w_fin);
     }
     if (in_smem) {
         __syncthreads();
