@@ -103,6 +103,9 @@ def parse():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--cpu-seconds", type=float, default=12.0,
                    help="target CPU time of the cpu_baseline sample")
+    p.add_argument("--variants", default="",
+                   help="out-of-core configs: comma-separated subset of the variants to run (profiler "
+                        "captures; the line then carries no comparisons and no serving)")
     return p.parse_args()
 
 
@@ -396,6 +399,10 @@ def gb300_ooc(args, cfg):
                 "batched": dict(sched=lt.SCHED_BATCHED), "frequency": dict(sched=lt.SCHED_FREQUENCY),
                 "learned_host_index": dict(sched=lt.SCHED_LEARNED, resident_index=False),
                 "plain_host_index": dict(sched=lt.SCHED_PLAIN, resident_index=False)}
+    if args.variants:
+        keep = args.variants.split(",")
+        variants = {k: v for k, v in variants.items() if k in keep}
+        assert variants, f"no variant among {keep}"
     K = args.steps
     n_timed = {"learned": K, "batched": K, "frequency": K, "plain": min(K, 5), "plain_x8": min(K, 5),
                "learned_host_index": min(K, 3), "plain_host_index": min(K, 3)}
@@ -469,9 +476,16 @@ def gb300_ooc(args, cfg):
     serving = {}
     c4 = CONFIGS["c4"]
     for name in ("learned", "plain"):
-        serving[name] = serve_rate(lt, engines[name], c4, V, 1000, 2.0, SEED_WALK + 1000)
+        if name in engines:
+            serving[name] = serve_rate(lt, engines[name], c4, V, 1000, 2.0, SEED_WALK + 1000)
     clocks.stop()
     clk = clocks.summary(wall0 - 0.5, wall1)
+    if args.variants:
+        print(json.dumps({"profile_run": True, "config": workload_config(args.config, cfg, V, E, P),
+                          "variants": res, "first_run": first_run}), flush=True)
+        for e in engines.values():
+            e.close()
+        return 0
 
     # the oracle sample of the cpu_baseline leg, and the same walkers through
     # the product: identical counts
@@ -508,8 +522,8 @@ def gb300_ooc(args, cfg):
         "data": "synthetic RMAT (seeded), stand-in for the reference datasets",
         "config": workload_config(args.config, cfg, V, E, P),
         "scheduler": "learned (wave runs, cache slots by the online-trained network's predicted visits)",
-        "layout": "vertex index on the device (%d MiB) inside the %d GiB graph budget: %d partition slots"
-                  % ((8 * (V + 1)) >> 20, (cfg["partitions"] * (cfg["part_mb"] << 20)) >> 30, s["cache_slots"]),
+        "layout": "vertex index on the device (%d MiB) inside the %d MiB graph budget: %d partition slots"
+                  % ((8 * (V + 1)) >> 20, cfg["partitions"] * cfg["part_mb"], s["cache_slots"]),
         # the resource an out-of-core run spends: host-link bytes (graph
         # loads and walker spills counted exactly, zero-copy reads at the
         # bytes per hop measured with ncu) over the run time, against the
