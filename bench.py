@@ -467,7 +467,14 @@ def gb300_ooc(args, cfg):
                      "iterations": st["iterations"], "partition_loads": st["partition_loads"],
                      "zerocopy_groups": st["zerocopy_groups"], "zerocopy_sweeps": st["zerocopy_sweeps"],
                      "overlap_computes": st["overlap_computes"], "cache_slots": st["cache_slots"],
-                     "index_on_device": bool(st["index_on_device"]), "step_s": spread(times[name])}
+                     "index_on_device": bool(st["index_on_device"]), "step_s": spread(times[name]),
+                     # where one run's time goes (last run): CUDA-event time of
+                     # the step kernels on cached queues / zero-copy sets, of
+                     # the bucketing kernels and of the partition copies; host
+                     # time blocked on each iteration's step kernel; wall time
+                     "run_ms": {"computing": st["computing_ms"], "zero_copy": st["zerocopy_ms"],
+                                "bucketing": st["bucket_ms"], "graph_loading": st["graph_loading_ms"],
+                                "host_wait": st["host_wait_ms"], "running": st["running_ms"]}}
         if pstats[name]["name"] in ("learned", "frequency"):
             res[name]["policy"] = pstats[name]
 

@@ -144,6 +144,8 @@ typedef struct lt_stats {
                                   zero-copy to finish the last walkers */
     uint64_t cache_slots;      /* out of core: partition slots on the device */
     uint64_t index_on_device;  /* out of core: 1 when the vertex index is resident on the device */
+    double bucket_ms;          /* CUDA-event time of the bucketing (scatter) kernels */
+    double host_wait_ms;       /* host time blocked waiting for each iteration's step kernel */
 } lt_stats;
 
 const char *lt_strerror(lt_status s);
@@ -175,6 +177,20 @@ lt_status lt_graph_from_csr(uint32_t num_nodes, uint64_t num_edges, const uint64
 lt_status lt_graph_generate_rmat(int device, uint32_t scale, uint64_t num_edges, double a, double b,
                                  double c, double d, uint64_t seed, uint64_t part_bytes,
                                  lt_graph **out);
+
+/* Build a graph from a text edge list (the reference's converter_txt,
+ * tools/convert_from_txt.cc:66-218) and partition it with part_bytes-byte
+ * partitions.  By default as the reference: lines not starting with a digit
+ * are skipped, each line gives "source destination" (unsigned ids), self
+ * loops are dropped, ids that appear in no edge are removed and the rest
+ * renumbered in order, every edge is added in both directions, and the list
+ * is sorted by (source, destination) with duplicates removed.  The flags
+ * below switch steps off.  Write the result with lt_graph_write_bcsr. */
+#define LT_EDGES_DIRECTED 1        /* keep edges one-way (no reverse edges) */
+#define LT_EDGES_KEEP_DUPLICATES 2 /* keep repeated (source, destination) pairs */
+#define LT_EDGES_KEEP_SELF_LOOPS 4
+#define LT_EDGES_KEEP_ISOLATED 8   /* keep ids as given (below 2^32 - 1); V = largest id + 1 */
+lt_status lt_graph_from_edge_list(const char *path, int flags, uint64_t part_bytes, lt_graph **out);
 
 lt_status lt_graph_info_get(const lt_graph *g, lt_graph_info *out);
 /* Copy the partition table: node_off[P+1], edge_off[P+1] (either may be NULL). */

@@ -83,7 +83,8 @@ class Stats(C.Structure):
                 ("walker_evicting_calls", C.c_uint64), ("step_kernel_ms", C.c_double),
                 ("handoffs", C.c_uint64), ("overlap_computes", C.c_uint64),
                 ("zerocopy_groups", C.c_uint64), ("zerocopy_sweeps", C.c_uint64),
-                ("cache_slots", C.c_uint64), ("index_on_device", C.c_uint64)]
+                ("cache_slots", C.c_uint64), ("index_on_device", C.c_uint64),
+                ("bucket_ms", C.c_double), ("host_wait_ms", C.c_double)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -101,6 +102,7 @@ def _load():
         "lt_version": ([], C.c_char_p),
         "lt_graph_open": ([C.c_char_p, C.c_int, C.c_uint64, C.POINTER(vp)], C.c_int),
         "lt_graph_from_csr": ([C.c_uint32, C.c_uint64, u64p, u32p, C.c_uint64, C.POINTER(vp)], C.c_int),
+        "lt_graph_from_edge_list": ([C.c_char_p, C.c_int, C.c_uint64, C.POINTER(vp)], C.c_int),
         "lt_graph_generate_rmat": ([C.c_int, C.c_uint32, C.c_uint64, C.c_double, C.c_double, C.c_double,
                                     C.c_double, C.c_uint64, C.c_uint64, C.POINTER(vp)], C.c_int),
         "lt_graph_info_get": ([vp, C.POINTER(GraphInfo)], C.c_int),
@@ -231,6 +233,19 @@ class Graph:
         h = C.c_void_p()
         check(lib.lt_graph_from_csr(len(rowptr) - 1, len(col), _ptr(rowptr, C.c_uint64),
                                     _ptr(col, C.c_uint32), part_bytes, C.byref(h)))
+        return cls(h)
+
+    @classmethod
+    def from_edge_list(cls, path, part_bytes: int = 1 << 62, directed: bool = False,
+                       keep_duplicates: bool = False, keep_self_loops: bool = False,
+                       keep_isolated: bool = False) -> "Graph":
+        """Text edge list -> graph, as the reference's converter_txt
+        (symmetrised, deduplicated, self loops and isolated ids removed,
+        unless the flags say otherwise)."""
+        flags = (1 if directed else 0) | (2 if keep_duplicates else 0) | (4 if keep_self_loops else 0) | \
+            (8 if keep_isolated else 0)
+        h = C.c_void_p()
+        check(lib.lt_graph_from_edge_list(os.fsencode(path), flags, part_bytes, C.byref(h)))
         return cls(h)
 
     @classmethod

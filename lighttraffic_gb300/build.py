@@ -4,7 +4,7 @@
 
 Produces
   lighttraffic_gb300/liblighttraffic.so   (C ABI of include/lighttraffic.h)
-  lighttraffic_gb300/bin/{ppr,pagerank,genericwalk}
+  lighttraffic_gb300/bin/{ppr,pagerank,genericwalk,converter_txt}
 
 Every CUDA translation unit is compiled for sm_103a only
 (-gencode arch=compute_103a,code=sm_103a); translation units are compiled in
@@ -90,7 +90,12 @@ def build(verbose: bool = False, jobs: int | None = None) -> str:
         if _newer(out, [cli, LIB, *headers]):
             cmds.append(["g++", "-std=c++17", "-O2", f"-DLT_CLI_APP={app}", f"-I{INCLUDE}", cli, "-o", out,
                          f"-L{PKG}", "-llighttraffic", "-Wl,-rpath,$ORIGIN/.."])
-    with cf.ThreadPoolExecutor(max_workers=3) as ex:
+    conv = os.path.join(APPS, "lt_convert.cpp")
+    out = os.path.join(BIN, "converter_txt")
+    if _newer(out, [conv, LIB, *headers]):
+        cmds.append(["g++", "-std=c++17", "-O2", f"-I{INCLUDE}", conv, "-o", out, f"-L{PKG}", "-llighttraffic",
+                     "-Wl,-rpath,$ORIGIN/.."])
+    with cf.ThreadPoolExecutor(max_workers=4) as ex:
         list(ex.map(_run, cmds))
     return LIB
 

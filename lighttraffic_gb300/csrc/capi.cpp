@@ -72,6 +72,28 @@ lt_status lt_graph_open(const char *bcsr_path, int materialize, uint64_t part_mb
     return LT_OK;
 }
 
+lt_status lt_graph_from_edge_list(const char *path, int flags, uint64_t part_bytes, lt_graph **out)
+{
+    if (!path || !out) return fail(LT_ERR_INVALID, "null argument");
+    if (flags & ~(LT_EDGES_DIRECTED | LT_EDGES_KEEP_DUPLICATES | LT_EDGES_KEEP_SELF_LOOPS | LT_EDGES_KEEP_ISOLATED))
+        return fail(LT_ERR_INVALID, "unknown edge-list flags %d", flags);
+    lt_graph *g = new (std::nothrow) lt_graph();
+    if (!g) return fail(LT_ERR_NOMEM, "graph allocation failed");
+    lt_status s = read_edge_list(path, flags, *g);
+    if (s == LT_OK) {
+        g->part_bytes = part_bytes;
+        s = partition_equal_size(g->rowptr(), g->V, part_bytes, g->node_off, g->edge_off);
+    }
+    if (s == LT_OK) s = finish_partitions(*g);
+    if (s != LT_OK) {
+        graph_free(*g);
+        delete g;
+        return s;
+    }
+    *out = g;
+    return LT_OK;
+}
+
 lt_status lt_graph_from_csr(uint32_t num_nodes, uint64_t num_edges, const uint64_t *rowptr, const uint32_t *col,
                             uint64_t part_bytes, lt_graph **out)
 {

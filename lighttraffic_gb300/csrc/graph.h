@@ -35,6 +35,8 @@ namespace lt {
 lt_status partition_equal_size(const uint64_t *rowptr, uint32_t V, uint64_t max_bytes,
                                std::vector<uint32_t> &node_off, std::vector<uint64_t> &edge_off);
 lt_status read_bcsr(const char *path, lt_graph &g);
+// Text edge list -> CSR (tools/convert_from_txt.cc); flags LT_EDGES_*.
+lt_status read_edge_list(const char *path, int flags, lt_graph &g);
 lt_status write_bcsr(const lt_graph &g, const char *path);
 lt_status read_part(const char *bcsr_path, lt_graph &g);
 lt_status write_part(const lt_graph &g, const char *bcsr_path);

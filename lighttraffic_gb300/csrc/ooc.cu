@@ -64,7 +64,7 @@ lt_status dalloc(T **p, uint64_t count)
     return LT_OK;
 }
 
-enum TimerKind { kTGraph = 0, kTCompute = 1, kTZero = 2 };
+enum TimerKind { kTGraph = 0, kTCompute = 1, kTZero = 2, kTBucket = 3 };
 
 // Host-link bytes per zero-copy hop: measured with ncu (sectors the
 // system-memory L2 filled from host memory) on the 2^33-edge graph, 0.244 of
@@ -190,9 +190,11 @@ void drain_timers(Ooc &o, bool all)
             e.stats.graph_loading_ms += ms;
         else if (t.kind == kTCompute)
             e.stats.computing_ms += ms;
-        else
+        else if (t.kind == kTZero)
             e.stats.zerocopy_ms += ms;
-        if (t.kind != kTGraph) e.stats.step_kernel_ms += ms;
+        else
+            e.stats.bucket_ms += ms;
+        if (t.kind == kTCompute || t.kind == kTZero) e.stats.step_kernel_ms += ms;
         o.ev_free.push_back(t.a);
         o.ev_free.push_back(t.b);
     }
@@ -612,7 +614,9 @@ lt_status step_and_bucket_parts(Ooc &o, const RunParams &rp, const std::vector<u
     }
     uint32_t *h_hist = (uint32_t *)o.h_ctl.ptr;
     LT_CUDA_TRY(cudaMemcpyAsync(h_hist, o.d_ctl, 4ull * o.hist_words() + 8, cudaMemcpyDeviceToHost, e.s_compute));
+    const double w0 = now_ms();
     LT_CUDA_TRY(cudaStreamSynchronize(e.s_compute));
+    e.stats.host_wait_ms += now_ms() - w0;
     const uint64_t staged = *(const unsigned long long *)(h_hist + o.hist_words());
     // the drained queues' chunks return to the pool
     for (uint32_t x : parts) {
@@ -683,7 +687,11 @@ lt_status step_and_bucket_parts(Ooc &o, const RunParams &rp, const std::vector<u
     sa.win_off = o.d_planbuf + o.P;
     sa.plan_chunks = o.d_planbuf + 2ull * o.P;
     sa.P = o.P;
+    Ooc::Timed tb{ev_get(o), ev_get(o), kTBucket};
+    LT_CUDA_TRY(cudaEventRecord(tb.a, e.s_compute));
     LT_CUDA_TRY(launch_scatter(sa, e.device, e.s_compute));
+    LT_CUDA_TRY(cudaEventRecord(tb.b, e.s_compute));
+    o.timed.push_back(tb);
     e.stats.kernel_launches++;
     return LT_OK;
 }

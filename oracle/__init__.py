@@ -283,3 +283,51 @@ def mlp_forward_backward(x, y, params):
     gb1 = da.sum(axis=0)
     grad = np.concatenate([gW1.ravel(), gb1, gW2, [gb2]])
     return pred, grad, loss
+
+
+# ------------------------------------------------------ edge-list converter
+
+EDGES_DIRECTED, EDGES_KEEP_DUPLICATES, EDGES_KEEP_SELF_LOOPS, EDGES_KEEP_ISOLATED = 1, 2, 4, 8
+
+
+def convert_edge_list(path, flags=0):
+    """Text edge list -> (rowptr u64[V+1], col u32[E]), restating the
+    reference's converter_txt (tools/convert_from_txt.cc:66-218) in numpy:
+    a line is used only if its first character is a digit and it holds two
+    unsigned ids (read_txt, :66-103); self loops are dropped (:88-91); ids
+    that appear in no edge are removed, the rest renumbered in order
+    (remove_isolated_vertices, :105-140); every edge is added in both
+    directions, the list sorted by (source, destination) and deduplicated
+    (to_undirected, :142-166).  `flags` (EDGES_*) switch steps off."""
+    src, dst = [], []
+    with open(path, "rb") as f:
+        for line in f:
+            if not line[:1].isdigit():
+                continue
+            parts = line.split()
+            if len(parts) < 2 or not parts[0].isdigit() or not parts[1].isdigit():
+                continue
+            a, b = int(parts[0]), int(parts[1])
+            if a == b and not flags & EDGES_KEEP_SELF_LOOPS:
+                continue
+            src.append(a)
+            dst.append(b)
+    if not src:
+        raise ValueError("no edges")
+    s = np.array(src, dtype=np.uint64)
+    d = np.array(dst, dtype=np.uint64)
+    if flags & EDGES_KEEP_ISOLATED:
+        V = int(max(s.max(), d.max())) + 1
+    else:
+        ids = np.unique(np.concatenate([s, d]))
+        V = len(ids)
+        s = np.searchsorted(ids, s).astype(np.uint64)
+        d = np.searchsorted(ids, d).astype(np.uint64)
+    if not flags & EDGES_DIRECTED:
+        s, d = np.concatenate([s, d]), np.concatenate([d, s])
+    key = (s << np.uint64(32)) | d
+    key = np.sort(key) if flags & EDGES_KEEP_DUPLICATES else np.unique(key)
+    rows = (key >> np.uint64(32)).astype(np.int64)
+    rowptr = np.zeros(V + 1, dtype=np.uint64)
+    np.add.at(rowptr, rows + 1, 1)
+    return np.cumsum(rowptr).astype(np.uint64), (key & np.uint64(0xFFFFFFFF)).astype(np.uint32)

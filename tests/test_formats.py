@@ -1,9 +1,11 @@
 """bcsr / .part formats and the partitioner: the product and the oracle are
 both checked against the reference's own EqualSizeStrategy outputs
 (tests/golden/graphs/*.part, made by tests/golden/make_golden.py)."""
+import hashlib
 import json
 import os
 import shutil
+import subprocess
 
 import numpy as np
 import pytest
@@ -132,3 +134,70 @@ def test_oversize_vertex_is_an_error(lt, tmp_path):
         lt.Graph.open(path, materialize=True, part_mb=0)
     assert ei.value.status == 6
     assert "cannot fit" in str(ei.value)
+
+
+# ------------------------------------------------------ edge-list converter
+
+with open(os.path.join(GOLDEN, "edgelists.json")) as _f:
+    EDGELISTS = json.load(_f)["bcsr"]
+
+
+def _bcsr_bytes(rp, col):
+    rp = np.ascontiguousarray(rp, np.uint64)
+    col = np.ascontiguousarray(col, np.uint32)
+    return (np.array([len(rp) - 1], np.uint32).tobytes() + np.array([len(col)], np.uint64).tobytes()
+            + rp.tobytes() + col.tobytes())
+
+
+@pytest.mark.parametrize("name", sorted(EDGELISTS))
+def test_oracle_converter_matches_reference(name):
+    """The oracle's restatement of converter_txt writes the bytes the
+    reference's own tools/convert_from_txt.cc wrote."""
+    rp, col = oracle.convert_edge_list(os.path.join(GOLDEN, "edgelists", name + ".el"))
+    assert hashlib.sha256(_bcsr_bytes(rp, col)).hexdigest() == EDGELISTS[name]["sha256"]
+
+
+@pytest.mark.parametrize("name", sorted(EDGELISTS))
+def test_product_converter_matches_reference(lt, name, tmp_path):
+    """lt_graph_from_edge_list + lt_graph_write_bcsr, and the converter_txt
+    binary, write the reference converter's bytes."""
+    src = os.path.join(GOLDEN, "edgelists", name + ".el")
+    g = lt.Graph.from_edge_list(src)
+    out = tmp_path / "g.bcsr"
+    g.write_bcsr(str(out))
+    assert hashlib.sha256(out.read_bytes()).hexdigest() == EDGELISTS[name]["sha256"]
+    el = tmp_path / (name + ".el")
+    el.write_bytes(open(src, "rb").read())
+    r = subprocess.run([os.path.join(lt.BIN_DIR, "converter_txt"), str(el)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    assert f"nodes: {EDGELISTS[name]['V']} edges: {EDGELISTS[name]['E']}" in r.stdout
+    assert hashlib.sha256((tmp_path / (name + ".bcsr")).read_bytes()).hexdigest() == EDGELISTS[name]["sha256"]
+
+
+@pytest.mark.parametrize("flags", [1, 2, 4, 8, 3, 15])
+@pytest.mark.parametrize("name", ["tiny", "sparse3000"])
+def test_converter_options_match_oracle(lt, name, flags):
+    """Each step the reference always takes (symmetrise, dedup, drop self
+    loops, drop isolated ids) can be switched off; product and oracle agree."""
+    src = os.path.join(GOLDEN, "edgelists", name + ".el")
+    if flags & 8 and name == "sparse3000":
+        flags &= ~8          # ids up to 10^6: keeping them all is fine but slow in the oracle's add.at
+    g = lt.Graph.from_edge_list(src, directed=bool(flags & 1), keep_duplicates=bool(flags & 2),
+                                keep_self_loops=bool(flags & 4), keep_isolated=bool(flags & 8))
+    rp, col = g.csr()
+    wrp, wcol = oracle.convert_edge_list(src, flags)
+    assert (rp == wrp).all() and (col == wcol).all()
+
+
+def test_converter_rejects_bad_input(lt, tmp_path):
+    empty = tmp_path / "empty.el"
+    empty.write_text("# nothing but comments\n\n")
+    with pytest.raises(lt.LTError) as ei:
+        lt.Graph.from_edge_list(str(empty))
+    assert ei.value.status == 3
+    with pytest.raises(lt.LTError) as ei:
+        lt.Graph.from_edge_list(str(tmp_path / "missing.el"))
+    assert ei.value.status == 2
+    r = subprocess.run([os.path.join(lt.BIN_DIR, "converter_txt"), str(tmp_path / "x.txt")],
+                       capture_output=True, text=True)
+    assert r.returncode == 2 and "not supported" in r.stderr
