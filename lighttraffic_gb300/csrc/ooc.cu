@@ -1858,6 +1858,7 @@ struct lt_server {
     unsigned long long *d_done = nullptr, *d_err = nullptr, *d_outn = nullptr;
     uint32_t *d_out_v = nullptr, *d_out_c = nullptr;
     uint64_t out_cap = 0;
+    uint64_t *d_meta = nullptr;  // extraction metadata: table base, size, output base and count per finished query
     lt::HostBuf h_done;
     std::vector<Query *> slots;
     std::deque<Query *> pending;
@@ -2049,14 +2050,17 @@ lt_status serve_complete(lt_server &s, uint32_t &completed)
         obase += fin[k]->walkers;
     }
     if (obase > s.out_cap) {
+        // the output staging grows geometrically (rarely: to the largest
+        // batch of finished walkers seen so far)
         for (void *p : {(void *)s.d_out_v, (void *)s.d_out_c})
             if (p) cudaFree(p);
         s.out_cap = std::max<uint64_t>(obase, 2 * s.out_cap);
         LT_CUDA_TRY(cudaMalloc(&s.d_out_v, 4 * s.out_cap));
         LT_CUDA_TRY(cudaMalloc(&s.d_out_c, 4 * s.out_cap));
     }
-    uint64_t *d_meta = nullptr;
-    LT_CUDA_TRY(cudaMalloc(&d_meta, 8 * meta.size() + 8 * fin.size()));
+    // at most max_active queries finish in one step: the metadata block
+    // allocated at serve_open always holds them
+    uint64_t *d_meta = s.d_meta;
     unsigned long long *d_n = (unsigned long long *)(d_meta + meta.size());
     LT_CUDA_TRY(cudaMemcpyAsync(d_meta, meta.data(), 8 * meta.size(), cudaMemcpyHostToDevice, e.s_compute));
     LT_CUDA_TRY(cudaMemsetAsync(d_n, 0, 8 * fin.size(), e.s_compute));
@@ -2078,7 +2082,6 @@ lt_status serve_complete(lt_server &s, uint32_t &completed)
                                     cudaMemcpyDeviceToHost, e.s_compute));
     }
     LT_CUDA_TRY(cudaStreamSynchronize(e.s_compute));
-    cudaFree(d_meta);
     for (lt_server::Query *q : fin) {
         q->state = 2;
         q->t_done = now;
@@ -2122,6 +2125,7 @@ lt_status serve_open(lt_engine *e, uint32_t max_active, uint64_t table_slots, fl
     if (st == LT_OK) st = dalloc(&s->d_err, 1);
     if (st == LT_OK) st = dalloc(&s->d_keys, table_slots);
     if (st == LT_OK) st = dalloc(&s->d_cnt, table_slots);
+    if (st == LT_OK) st = dalloc(&s->d_meta, 4ull * max_active);
     if (st == LT_OK) st = host_alloc(s->h_done, 8ull * max_active, true);
     if (st != LT_OK) return bail(st);
     if (cudaMemset(s->d_done, 0, 8ull * max_active) != cudaSuccess || cudaMemset(s->d_err, 0, 8) != cudaSuccess)
@@ -2242,7 +2246,7 @@ void serve_close(lt_server *s)
         refresh_all(*s->o);
     }
     for (void *p : {(void *)s->d_seed, (void *)s->d_toff, (void *)s->d_tlog, (void *)s->d_keys, (void *)s->d_cnt,
-                    (void *)s->d_done, (void *)s->d_err, (void *)s->d_out_v, (void *)s->d_out_c})
+                    (void *)s->d_done, (void *)s->d_err, (void *)s->d_out_v, (void *)s->d_out_c, (void *)s->d_meta})
         if (p) cudaFree(p);
     host_free(s->h_done);
     delete s->wave;
