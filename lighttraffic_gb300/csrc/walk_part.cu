@@ -21,8 +21,11 @@
 // counts its tile per destination in shared memory and reserves one range per
 // destination with one global atomic (the two-level scheme of
 // src/WalkManager.h:122-190), into chunks the host allocated beforehand.
+#include <algorithm>
+
 #include "lt_core.cuh"
 #include "mem.cuh"
+#include "scan.cuh"
 #include "walk_part.h"
 
 namespace lt {
@@ -406,6 +409,95 @@ __global__ void __launch_bounds__(kPartBlock) scatter_kernel(ScatterArgs a)
     }
 }
 
+// Bucketing by a block-local counting sort (P <= kSmemPartMax).  A tile of
+// kBucketTile staged walkers is ranked per destination in shared memory
+// (shared atomics), the per-destination counts are scanned across the block
+// and reserved in the destination windows with one global atomic per
+// (tile, destination) -- the two-level scheme of insertToQueueKernel
+// (src/WalkManager.h:122-190) -- and the walkers are laid out sorted by
+// destination in shared memory, so that the write-back is a sequence of
+// per-destination runs: consecutive threads write consecutive queue slots.
+// The plain scatter above wrote each walker with four isolated 4-byte stores
+// and made one global atomic per (1024-walker tile, destination), i.e.
+// nearly one per walker when the walkers spread over ~1000 partitions.
+constexpr int kBucketItems = 16;
+constexpr int kBucketTile = kPartBlock * kBucketItems;  // 4096 walkers
+constexpr int kBucketFields = 5;                         // cur, step, idx, query, dest
+
+size_t bucket_smem(uint32_t P) { return sizeof(uint32_t) * (2ull * P + (uint64_t)kBucketFields * kBucketTile); }
+
+__global__ void __launch_bounds__(kPartBlock, 2) bucket_sort_kernel(ScatterArgs a)
+{
+    extern __shared__ uint32_t smem[];
+    __shared__ uint32_t warp_tot[kPartBlock / 32];
+    __shared__ uint32_t tile_total;
+    const uint32_t P = a.P;
+    uint32_t *s_cnt = smem;       // P: walkers of the tile per destination, then their offsets in the sorted tile
+    uint32_t *s_base = smem + P;  // P: first reserved slot of the destination's window
+    uint32_t *s_cur = s_base + P;
+    uint32_t *s_step = s_cur + kBucketTile;
+    uint32_t *s_idx = s_step + kBucketTile;
+    uint32_t *s_q = s_idx + kBucketTile;
+    uint32_t *s_dest = s_q + kBucketTile;
+    const uint32_t per = (P + kPartBlock - 1) / kPartBlock;  // destinations a thread reserves and scans
+    for (uint64_t t0 = (uint64_t)blockIdx.x * kBucketTile; t0 < a.n; t0 += (uint64_t)gridDim.x * kBucketTile) {
+        for (uint32_t i = threadIdx.x; i < P; i += blockDim.x) s_cnt[i] = 0;
+        __syncthreads();
+        uint32_t dest[kBucketItems], rank[kBucketItems];
+#pragma unroll
+        for (int k = 0; k < kBucketItems; k++) {
+            const uint64_t i = t0 + (uint64_t)k * kPartBlock + threadIdx.x;
+            dest[k] = i < a.n ? a.in_dest[i] : 0xFFFFFFFFu;
+            rank[k] = dest[k] != 0xFFFFFFFFu ? atomicAdd(&s_cnt[dest[k]], 1u) : 0u;
+        }
+        __syncthreads();
+        uint32_t mine = 0;
+        for (uint32_t j = 0; j < per; j++) {
+            const uint32_t d = threadIdx.x * per + j;
+            if (d < P) {
+                const uint32_t c = s_cnt[d];
+                if (c) s_base[d] = atomicAdd(&a.cursor[d], c);
+                mine += c;
+            }
+        }
+        uint32_t off = scan_detail::block_exclusive<uint32_t>(mine, warp_tot, &tile_total);
+        for (uint32_t j = 0; j < per; j++) {
+            const uint32_t d = threadIdx.x * per + j;
+            if (d < P) {
+                const uint32_t c = s_cnt[d];
+                s_cnt[d] = off;
+                off += c;
+            }
+        }
+        __syncthreads();
+#pragma unroll
+        for (int k = 0; k < kBucketItems; k++) {
+            if (dest[k] == 0xFFFFFFFFu) continue;
+            const uint64_t i = t0 + (uint64_t)k * kPartBlock + threadIdx.x;
+            const uint32_t pos = s_cnt[dest[k]] + rank[k];
+            s_cur[pos] = a.in_cur[i];
+            s_step[pos] = a.in_step[i];
+            s_idx[pos] = a.in_idx[i];
+            s_q[pos] = a.in_q[i];
+            s_dest[pos] = dest[k];
+        }
+        __syncthreads();
+        const uint32_t m = (uint32_t)min((uint64_t)kBucketTile, a.n - t0);
+        for (uint32_t j = threadIdx.x; j < m; j += blockDim.x) {
+            const uint32_t d = s_dest[j];
+            const uint32_t g = s_base[d] + (j - s_cnt[d]);
+            const uint32_t chunk = a.plan_chunks[a.win_off[d] + g / kChunk];
+            uint32_t *c = reinterpret_cast<uint32_t *>(a.arena + (uint64_t)chunk * kChunkBytes);
+            const uint32_t jj = g % kChunk;
+            c[jj] = s_cur[j];
+            c[kChunk + jj] = s_step[j];
+            c[2 * kChunk + jj] = s_idx[j];
+            c[3 * kChunk + jj] = s_q[j];
+        }
+        __syncthreads();
+    }
+}
+
 __global__ void inject_kernel(InjectArgs a)
 {
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
@@ -471,6 +563,20 @@ cudaError_t launch_scatter(const ScatterArgs &a, int device, cudaStream_t st)
     if (a.n == 0) return cudaSuccess;
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+    if (a.P <= kSmemPartMax) {
+        const size_t smem = bucket_smem(a.P);
+        static thread_local int configured_device = -1;
+        if (configured_device != device) {
+            const cudaError_t e = cudaFuncSetAttribute(bucket_sort_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                       (int)bucket_smem(kSmemPartMax));
+            if (e != cudaSuccess) return e;
+            configured_device = device;
+        }
+        const uint64_t tiles = (a.n + kBucketTile - 1) / kBucketTile;
+        const uint64_t blocks = std::min<uint64_t>(tiles, (uint64_t)sms * (smem <= 110 * 1024 ? 2 : 1));
+        bucket_sort_kernel<<<(unsigned)blocks, kPartBlock, smem, st>>>(a);
+        return cudaGetLastError();
+    }
     const uint64_t tile = (uint64_t)kPartBlock * kScatterItems;
     uint64_t blocks = (a.n + tile - 1) / tile;
     const uint64_t cap = (uint64_t)sms * 8;
