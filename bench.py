@@ -533,8 +533,9 @@ def gb300_ooc(args, cfg):
         "data": "synthetic RMAT (seeded), stand-in for the reference datasets",
         "config": workload_config(args.config, cfg, V, E, P),
         "scheduler": "learned (wave runs, cache slots by the online-trained network's predicted visits)",
-        "layout": "vertex index on the device (%d MiB) inside the %d MiB graph budget: %d partition slots"
-                  % ((8 * (V + 1)) >> 20, cfg["partitions"] * cfg["part_mb"], s["cache_slots"]),
+        "layout": "compact vertex index on the device (u32 offsets within each partition, %d MiB) inside "
+                  "the %d MiB graph budget: %d partition slots"
+                  % ((4 * (V + 1)) >> 20, cfg["partitions"] * cfg["part_mb"], s["cache_slots"]),
         # The dominant kernel of an out-of-core run is the step kernel on
         # zero-copy sets: each zero-copy hop reads one 4-byte column entry
         # from pinned host memory, and the link moves its 32-byte sector

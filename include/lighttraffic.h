@@ -101,8 +101,9 @@ typedef struct lt_engine_cfg {
     uint64_t seed;                   /* Philox key */
     int block_size;                  /* threads per CTA of the step kernel (0 = tuned default) */
     int ctas_per_sm;                 /* resident CTAs per SM (0 = occupancy maximum) */
-    int resident_index;              /* out-of-core: keep the vertex index (rowptr, 8 (V+1) bytes) on
-                                        the device, so partition loads copy only edges and zero-copy
+    int resident_index;              /* out-of-core: keep the vertex index on the device (4 (V+1)
+                                        bytes: each vertex's first edge as a u32 offset from its
+                                        partition's first edge), so partition loads copy only edges and zero-copy
                                         hops read only col over the host link (1 = on, the default,
                                         falling back to 0 when the index does not fit in the -p
                                         budget with at least one slot beside it; 0 = the

@@ -126,7 +126,7 @@ struct Ooc {
     // vertex index (rowptr, V+1 u64) resident on the device: slots then hold
     // only col slices and zero-copy hops read rowptr here; null: the
     // reference's layout, rowptr slice then col slice in every slot
-    uint64_t *d_index = nullptr;
+    uint32_t *d_index = nullptr;
     // zero-copy set of the next step kernel (wave runs)
     uint32_t zc_mask[kZcMaskWords] = {};
     bool zc_mask_any = false;
@@ -585,12 +585,13 @@ lt_status step_and_bucket_parts(Ooc &o, const RunParams &rp, const std::vector<u
     a.stats = o.d_stats;
     a.zc_part = kNoPart;
     a.zc_rp_base = o.zc_rp_base;
+    a.rp32 = o.d_index != nullptr;
     a.zc_col_base = o.zc_col_base;
     if (o.zc_mask_any) std::memcpy(a.zc_mask, o.zc_mask, sizeof a.zc_mask);
     if (o.serve) serve_args(o, a);
     if (zero_copy) {
         a.zc_part = (uint32_t)p;
-        a.zc_rp = o.zc_rp_base + 8ull * g.node_off[p];
+        a.zc_rp = o.zc_rp_base + (o.d_index ? 4ull : 8ull) * g.node_off[p];
         a.zc_col = o.zc_col_base + 4ull * g.edge_off[p];
     }
 
@@ -1136,11 +1137,19 @@ lt_status ooc_create(lt_engine *e, Ooc **out)
         ooc_destroy(o);
         return s;
     };
-    // The vertex index goes to the device first (8 (V+1) bytes, 2.9 GB at
-    // 2^30 vertices); where it does not fit, the slots carry rowptr slices.
-    if (e->cfg.resident_index) {
+    // The vertex index goes to the device first, compact: 4 (V+1) bytes
+    // (1.46 GB at 2^30 vertices), each vertex's first edge as a u32 offset
+    // from its partition's first edge (a partition's edges fit 32 bits); the
+    // partition's edge count ends its last row.  Where it does not fit, the
+    // slots carry rowptr slices.
+    if (e->cfg.resident_index && g.max_edges < (1ull << 32)) {
+        std::vector<uint32_t> idx((uint64_t)g.V + 1, 0);
+        const uint64_t *rp = g.rowptr();
+#pragma omp parallel for schedule(dynamic, 1)
+        for (int64_t p = 0; p < (int64_t)o->P; p++)
+            for (uint64_t v = g.node_off[p]; v < g.node_off[p + 1]; v++) idx[v] = (uint32_t)(rp[v] - g.edge_off[p]);
         if (dalloc(&o->d_index, (uint64_t)g.V + 1) != LT_OK ||
-            cudaMemcpy(o->d_index, g.rowptr(), 8ull * ((uint64_t)g.V + 1), cudaMemcpyHostToDevice) != cudaSuccess) {
+            cudaMemcpy(o->d_index, idx.data(), 4ull * ((uint64_t)g.V + 1), cudaMemcpyHostToDevice) != cudaSuccess) {
             cudaGetLastError();
             clear_error();
             if (o->d_index) cudaFree(o->d_index);
@@ -1151,11 +1160,11 @@ lt_status ooc_create(lt_engine *e, Ooc **out)
     for (uint32_t p = 0; p < o->P; p++) max_slot = std::max<uint64_t>(max_slot, host_part_bytes(*o, p) + 16);
     o->slot_stride = (max_slot + 255) & ~255ull;
     // -p P gives the graph P x partitionSize bytes of device memory, as the
-    // reference allocates (src/GraphLoader.h:176-190); a resident vertex
+    // reference allocates (src/GraphLoader.h:175-178); a resident vertex
     // index is paid from that budget, leaving fewer slots.  Where it leaves
     // none, the slots carry rowptr slices instead.
     if (o->d_index) {
-        const uint64_t budget = (uint64_t)o->K * g.part_bytes, index_bytes = 8ull * ((uint64_t)g.V + 1);
+        const uint64_t budget = (uint64_t)o->K * g.part_bytes, index_bytes = 4ull * ((uint64_t)g.V + 1);
         const uint64_t fit = budget > index_bytes ? (budget - index_bytes) / o->slot_stride : 0;
         if (fit >= 1) {
             o->K = (uint32_t)std::min<uint64_t>(o->K, fit);

@@ -61,6 +61,30 @@ __device__ __forceinline__ uint32_t ld_u32(unsigned long long addr, uint64_t str
     return ld_nc_stream_u32(reinterpret_cast<const void *>(addr), stream);
 }
 
+// Row of vertex cur in the lane's readable partition [nb, ne): the address of
+// its first column entry and its degree.  Row offsets are u64 global edge
+// offsets (rowptr slices in the slots, the reference's layout), or, with the
+// compact device-resident index (a.rp32), u32 offsets relative to the
+// partition's first edge; eb is then the partition's edge count, which ends
+// the last vertex's row.
+__device__ __forceinline__ void row_at(bool rp32, unsigned long long rp, unsigned long long col, uint64_t eb,
+                                       uint32_t cur, uint32_t nb, uint32_t ne, uint64_t keep,
+                                       unsigned long long &first_addr, uint64_t &deg)
+{
+    const uint32_t rel = cur - nb;
+    if (rp32) {
+        const uint32_t lo = ld_nc_u32(reinterpret_cast<const void *>(rp + 4ull * rel), keep);
+        const uint32_t hi =
+            cur + 1 < ne ? ld_nc_u32(reinterpret_cast<const void *>(rp + 4ull * (rel + 1)), keep) : (uint32_t)eb;
+        first_addr = col + 4ull * lo;
+        deg = hi - lo;
+    } else {
+        const uint64_t first = ld_u64(rp + 8ull * rel, keep);
+        deg = ld_u64(rp + 8ull * (rel + 1), keep) - first;
+        first_addr = col + 4ull * (first - eb);
+    }
+}
+
 // A PPR walk ends at v: count it (single run) or add it to the query's table
 // (linear probing, u32 counts) and mark one more walker of the query done.
 __device__ __forceinline__ void ppr_count(const StepArgs &a, uint32_t qs, uint32_t v)
@@ -220,7 +244,7 @@ __global__ void __launch_bounds__(kPartBlock, part_min_blocks<APP>()) walk_part_
                     if (rp != 0ull) {
                         col = *(volatile const unsigned long long *)&a.t.col_addr[p];
                     } else if (in_smem && ((s_zc[p >> 5] >> (p & 31)) & 1u)) {
-                        rp = (a.zc_rp_base + 8ull * off[p]) | 1ull;
+                        rp = (a.zc_rp_base + (a.rp32 ? 4ull : 8ull) * off[p]) | 1ull;
                         col = a.zc_col_base + 4ull * a.t.edge_off[p];
                     }
                 }
@@ -232,7 +256,7 @@ __global__ void __launch_bounds__(kPartBlock, part_min_blocks<APP>()) walk_part_
                     cp_ne = off[p + 1];
                     cp_rp = rp & ~1ull;
                     cp_col = col;
-                    cp_eb = a.t.edge_off[p];
+                    cp_eb = a.rp32 ? a.t.edge_off[p + 1] - a.t.edge_off[p] : a.t.edge_off[p];
                     cp_zc = (rp & 1ull) != 0;
                 }
             }
@@ -267,11 +291,12 @@ __global__ void __launch_bounds__(kPartBlock, part_min_blocks<APP>()) walk_part_
                 done = true;
             } else {
                 step = s - 1;
-                const uint64_t first = ld_u64(cp_rp + 8ull * (cur - cp_nb), keep);
-                const uint64_t deg = ld_u64(cp_rp + 8ull * (cur - cp_nb + 1), keep) - first;
+                unsigned long long fa;
+                uint64_t deg;
+                row_at(a.rp32, cp_rp, cp_col, cp_eb, cur, cp_nb, cp_ne, keep, fa, deg);
                 if (deg > 0) {
                     const Rand4 q = walk_draw(seed, s, kTagStep, a.run, idx);
-                    cur = ld_u32(cp_col + 4ull * (first + mod_u64(r64_of(q), deg) - cp_eb), stream);
+                    cur = ld_u32(fa + 4ull * mod_u64(r64_of(q), deg), stream);
                     n_mov++;
                     n_zc += cp_zc;
                 } else {
@@ -289,10 +314,11 @@ __global__ void __launch_bounds__(kPartBlock, part_min_blocks<APP>()) walk_part_
                 const uint64_t r64 = r64_of(r);
                 bool tele = !need_graph;
                 if (!tele) {
-                    const uint64_t first = ld_u64(cp_rp + 8ull * (cur - cp_nb), keep);
-                    const uint64_t deg = ld_u64(cp_rp + 8ull * (cur - cp_nb + 1), keep) - first;
+                    unsigned long long fa;
+                    uint64_t deg;
+                    row_at(a.rp32, cp_rp, cp_col, cp_eb, cur, cp_nb, cp_ne, keep, fa, deg);
                     if (deg > 0) {
-                        cur = ld_u32(cp_col + 4ull * (first + mod_u64(r64, deg) - cp_eb), stream);
+                        cur = ld_u32(fa + 4ull * mod_u64(r64, deg), stream);
                         n_mov++;
                         n_zc += cp_zc;
                     } else {
@@ -306,12 +332,13 @@ __global__ void __launch_bounds__(kPartBlock, part_min_blocks<APP>()) walk_part_
             }
         } else {
             // app/genericwalk.cu:22-32
-            const uint64_t first = ld_u64(cp_rp + 8ull * (cur - cp_nb), keep);
-            const uint64_t deg = ld_u64(cp_rp + 8ull * (cur - cp_nb + 1), keep) - first;
+            unsigned long long fa;
+            uint64_t deg;
+            row_at(a.rp32, cp_rp, cp_col, cp_eb, cur, cp_nb, cp_ne, keep, fa, deg);
             uint32_t *path = a.paths ? a.paths + (uint64_t)idx * (a.length + 1) : nullptr;
             if (deg > 0) {
                 const Rand4 q = walk_draw(seed, s, kTagStep, a.run, idx);
-                cur = ld_u32(cp_col + 4ull * (first + mod_u64(r64_of(q), deg) - cp_eb), stream);
+                cur = ld_u32(fa + 4ull * mod_u64(r64_of(q), deg), stream);
                 n_mov++;
                 n_zc += cp_zc;
                 hop++;

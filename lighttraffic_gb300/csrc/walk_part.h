@@ -71,9 +71,14 @@ struct StepArgs {
     unsigned long long zc_rp, zc_col;
     // further partitions read zero-copy in this launch (wave runs): bit p of
     // zc_mask (P <= kSmemPartMax only), read at zc_rp_base + 8 node_off[p]
+    // (4 node_off[p] with rp32)
     // and zc_col_base + 4 edge_off[p] when the table marks p unreadable
     unsigned long long zc_rp_base, zc_col_base;
     uint32_t zc_mask[kZcMaskWords];
+    // row offsets of every readable partition are u32 offsets relative to
+    // the partition's first edge (the compact device-resident vertex index);
+    // 0: u64 global edge offsets
+    int rp32;
     // query mode (serving many PPR queries): per query slot its key, table and
     // finished-walker counter; endpoints go to the query's table instead of
     // `counts`.  q_seed == null: single-run mode.
