@@ -478,6 +478,13 @@ def gb300_ooc(args, cfg):
                                 "host_wait": st["host_wait_ms"], "running": st["running_ms"]}}
         if pstats[name]["name"] in ("learned", "frequency"):
             res[name]["policy"] = pstats[name]
+        ps = engines[name].partition_stats()
+        vis, cvis = ps["visits"].astype(np.float64), ps["cached_visits"].astype(np.float64)
+        top = np.sort(vis)[::-1][: st["cache_slots"]].sum()
+        # share of partition entries that found their partition cached, and
+        # what the best fixed set of cache_slots partitions would have caught
+        res[name]["cache"] = {"entries": int(vis.sum()), "cached_share": float(cvis.sum() / max(1.0, vis.sum())),
+                              "best_fixed_set_share": float(top / max(1.0, vis.sum()))}
 
     # serving latency on the same graph and cache (the c4 workload at 1 000
     # queries/s), learned against the reference loop

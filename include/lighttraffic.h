@@ -405,6 +405,14 @@ typedef struct lt_policy_stats {
  * counterpart in the reference. */
 lt_status lt_engine_policy_stats(const lt_engine *e, lt_policy_stats *out);
 
+/* Per partition, over the engine's last out-of-core run: walkers that
+ * entered it, those that entered while it was cached, and step-kernel
+ * launches during which it was cached (P entries each; any may be NULL).
+ * What a cache policy could gain is read off these.  No counterpart in the
+ * reference. */
+lt_status lt_engine_partition_stats(const lt_engine *e, uint64_t *visits, uint64_t *cached_visits,
+                                    uint64_t *cached_launches);
+
 /* Forward and backward pass (and, when lr > 0, one SGD-with-momentum step) of
  * the learned prefetcher's network on caller data, on `device`: a 2-layer FP32
  * MLP with 16 inputs, 64 ReLU units and one output, mean squared error loss.

@@ -122,6 +122,7 @@ def _load():
         "lt_engine_stats": ([vp, C.POINTER(Stats)], C.c_int),
         "lt_walk_scratch_bytes": ([], C.c_size_t),
         "lt_engine_policy_stats": ([vp, C.POINTER(PolicyStats)], C.c_int),
+        "lt_engine_partition_stats": ([vp, u64p, u64p, u64p], C.c_int),
         "lt_mod_check": ([C.c_uint64, u64p, u64p, u64p], C.c_int),
         "lt_mod_check_device": ([C.c_uint64, vp, vp, vp, vp], C.c_int),
         "lt_host_link_gbs": ([C.c_int, C.POINTER(C.c_double)], C.c_int),
@@ -518,6 +519,15 @@ class Engine:
         check(lib.lt_engine_policy_stats(self._h, C.byref(s)))
         return {"name": s.name.decode(), "train_steps": s.train_steps, "net_loss": s.net_loss,
                 "baseline_loss": s.baseline_loss, "predictions": s.predictions}
+
+    def partition_stats(self) -> dict:
+        """Per partition over the last out-of-core run: walkers entering it,
+        those entering while it was cached, launches it was cached for."""
+        P = self.graph.num_partitions
+        v, cv, cl = (np.zeros(P, np.uint64) for _ in range(3))
+        check(lib.lt_engine_partition_stats(self._h, _ptr(v, C.c_uint64), _ptr(cv, C.c_uint64),
+                                            _ptr(cl, C.c_uint64)))
+        return {"visits": v, "cached_visits": cv, "cached_launches": cl}
 
     def drop_cache(self):
         check(lib.lt_engine_drop_cache(self._h))

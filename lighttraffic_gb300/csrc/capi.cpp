@@ -271,6 +271,15 @@ lt_status lt_engine_policy_stats(const lt_engine *e, lt_policy_stats *out)
     return LT_OK;
 }
 
+lt_status lt_engine_partition_stats(const lt_engine *e, uint64_t *visits, uint64_t *cached_visits,
+                                    uint64_t *cached_launches)
+{
+    if (!e) return fail(LT_ERR_INVALID, "null argument");
+    if (!e->ooc) return fail(LT_ERR_UNSUPPORTED, "partition statistics are kept by out-of-core engines");
+    ooc_partition_stats(e->ooc, visits, cached_visits, cached_launches);
+    return LT_OK;
+}
+
 size_t lt_walk_scratch_bytes(void) { return walk_scratch_bytes(); }
 
 lt_status lt_host_link_gbs(int device, double *gbs)

@@ -115,6 +115,9 @@ struct Ooc {
     // device views of h_plan / h_work (null: not mapped, upload by copy)
     uint8_t *h_plan_dev = nullptr, *h_work_dev = nullptr;
     std::vector<uint32_t> arrivals, visits;
+    // per partition over the current run: walkers entering it, those that
+    // entered while it was cached, and step-kernel launches it was cached for
+    std::vector<uint64_t> run_visits, run_cached_visits, run_cached_launches;
     std::vector<uint64_t> waiting, lazy_left, dev_waiting;
 
     std::vector<Queue> q;
@@ -633,6 +636,12 @@ lt_status step_and_bucket_parts(Ooc &o, const RunParams &rp, const std::vector<u
     }
     std::memcpy(o.arrivals.data(), h_hist, 4ull * o.P);
     std::memcpy(o.visits.data(), h_hist + o.P, 4ull * o.P);
+    for (uint32_t x = 0; x < o.P; x++) {
+        const bool cached = o.slot_of[x] >= 0;
+        o.run_visits[x] += o.visits[x];
+        o.run_cached_visits[x] += cached ? o.visits[x] : 0;
+        o.run_cached_launches[x] += cached;
+    }
     if (staged == 0) return LT_OK;
 
     // Plan the append of h_hist[d] walkers to each destination queue.
@@ -1199,6 +1208,9 @@ lt_status ooc_create(lt_engine *e, Ooc **out)
     o->waiting.assign(o->P, 0);
     o->lazy_left.assign(o->P, 0);
     o->dev_waiting.assign(o->P, 0);
+    o->run_visits.assign(o->P, 0);
+    o->run_cached_visits.assign(o->P, 0);
+    o->run_cached_launches.assign(o->P, 0);
     o->q.assign(o->P, Queue{});
     if (e->cfg.sched == LT_SCHED_FIFO) {
         o->policy.reset(new FifoPolicy());
@@ -1247,6 +1259,15 @@ void ooc_destroy(Ooc *o)
 }
 
 void ooc_policy_stats(const Ooc *o, lt_policy_stats &s) { o->policy->stats(s); }
+
+void ooc_partition_stats(const Ooc *o, uint64_t *visits, uint64_t *cached_visits, uint64_t *cached_launches)
+{
+    for (uint32_t p = 0; p < o->P; p++) {
+        if (visits) visits[p] = o->run_visits[p];
+        if (cached_visits) cached_visits[p] = o->run_cached_visits[p];
+        if (cached_launches) cached_launches[p] = o->run_cached_launches[p];
+    }
+}
 
 lt_status ooc_drop_cache(Ooc *o)
 {
@@ -1639,6 +1660,9 @@ lt_status run_setup(lt_engine *e, RunParams &rp, int app, int start, uint32_t so
     e->stats = lt_stats{};
     e->stats.cache_slots = o.K;
     e->stats.index_on_device = o.d_index != nullptr;
+    std::fill(o.run_visits.begin(), o.run_visits.end(), 0);
+    std::fill(o.run_cached_visits.begin(), o.run_cached_visits.end(), 0);
+    std::fill(o.run_cached_launches.begin(), o.run_cached_launches.end(), 0);
     cudaStream_t st = e->s_compute;
     if (app != kWalk) LT_CUDA_TRY(cudaMemsetAsync(e->d_counts, 0, 8ull * g.V, st));
     LT_CUDA_TRY(cudaMemsetAsync(o.d_stats, 0, 64, st));
