@@ -109,6 +109,10 @@ typedef struct lt_engine_cfg {
                                         budget with at least one slot beside it; 0 = the
                                         reference's layout, rowptr slices in the slots,
                                         src/GraphLoader.h:193-214) */
+    uint64_t zc_group_bytes;         /* wave runs: estimated host bytes the partitions of one zero-copy
+                                        group may touch (0 = 512 MiB; 128 MiB while serving) */
+    uint64_t sweep_walkers;          /* wave runs: walkers left outside the cache at or below which one
+                                        kernel reads every uncached partition zero-copy (0 = 2^18) */
 } lt_engine_cfg;
 
 typedef struct lt_stats {

@@ -50,7 +50,8 @@ class EngineCfg(C.Structure):
     _fields_ = [("device", C.c_int), ("num_device_partitions", C.c_uint32),
                 ("num_device_walkers", C.c_uint64), ("sched", C.c_int), ("pipeline", C.c_int),
                 ("zerocopy_threshold", C.c_uint64), ("seed", C.c_uint64), ("block_size", C.c_int),
-                ("ctas_per_sm", C.c_int), ("resident_index", C.c_int)]
+                ("ctas_per_sm", C.c_int), ("resident_index", C.c_int), ("zc_group_bytes", C.c_uint64),
+                ("sweep_walkers", C.c_uint64)]
 
 
 class BatchTune(C.Structure):
@@ -418,7 +419,8 @@ class Engine:
 
     def __init__(self, graph: Graph, partitions: int = 0, batch: int = 0, seed: int = 0x5EED5EED,
                  sched: int = SCHED_PLAIN, pipeline: bool = True, zerocopy_threshold=None,
-                 device: int = 0, ctas_per_sm: int = 0, resident_index: bool = True):
+                 device: int = 0, ctas_per_sm: int = 0, resident_index: bool = True, zc_group_bytes: int = 0,
+                 sweep_walkers: int = 0):
         cfg = EngineCfg()
         lib.lt_engine_cfg_default(C.byref(cfg))
         cfg.device = device
@@ -431,6 +433,8 @@ class Engine:
             cfg.zerocopy_threshold = zerocopy_threshold
         cfg.ctas_per_sm = ctas_per_sm
         cfg.resident_index = int(resident_index)
+        cfg.zc_group_bytes = zc_group_bytes
+        cfg.sweep_walkers = sweep_walkers
         self.graph = graph
         self._h = C.c_void_p()
         check(lib.lt_engine_create(graph._h, C.byref(cfg), C.byref(self._h)))

@@ -895,7 +895,9 @@ lt_status wave_step(Ooc &o, const RunParams &rp, WaveState &w, bool &done)
     const uint64_t load_min = !zc_ok ? 1
                               : o.zc_threshold > UINT64_MAX / load_factor ? UINT64_MAX
                                                                           : o.zc_threshold * load_factor;
-    const uint64_t zc_group_bytes = o.serve ? kZcGroupBytesServe : kZcGroupBytes;
+    const uint64_t zc_group_bytes =
+        e.cfg.zc_group_bytes ? e.cfg.zc_group_bytes : o.serve ? kZcGroupBytesServe : kZcGroupBytes;
+    const uint64_t sweep_walkers = e.cfg.sweep_walkers ? e.cfg.sweep_walkers : kSweepWalkers;
     const uint64_t reserve = (uint64_t)o.P + 2;
     auto &inflight = w.inflight;
     auto &parts = w.parts;
@@ -1041,7 +1043,7 @@ lt_status wave_step(Ooc &o, const RunParams &rp, WaveState &w, bool &done)
                     outside += o.waiting[p];
                     group.push_back(p);
                 }
-            const bool sweep = outside <= kSweepWalkers;
+            const bool sweep = outside <= sweep_walkers;
             if (!sweep) {
                 std::sort(group.begin(), group.end(), [&](uint32_t a, uint32_t b) {
                     return o.waiting[a] != o.waiting[b] ? o.waiting[a] > o.waiting[b] : a < b;
