@@ -400,13 +400,20 @@ def gb300_ooc(args, cfg):
                 "batched": dict(sched=lt.SCHED_BATCHED), "frequency": dict(sched=lt.SCHED_FREQUENCY),
                 "learned_host_index": dict(sched=lt.SCHED_LEARNED, resident_index=False),
                 "plain_host_index": dict(sched=lt.SCHED_PLAIN, resident_index=False)}
+    # named only through --variants: wave runs that read every uncached
+    # partition zero-copy in each kernel (no bounded groups), and bounded
+    # groups of other footprints
+    extra = {"learned_sweep": dict(sched=lt.SCHED_LEARNED, zc_group_bytes=1 << 62, sweep_walkers=1 << 62),
+             "learned_zc2g": dict(sched=lt.SCHED_LEARNED, zc_group_bytes=2 << 30),
+             "learned_zc8g": dict(sched=lt.SCHED_LEARNED, zc_group_bytes=8 << 30)}
     if args.variants:
         keep = args.variants.split(",")
-        variants = {k: v for k, v in variants.items() if k in keep}
+        variants = {k: v for k, v in {**variants, **extra}.items() if k in keep}
         assert variants, f"no variant among {keep}"
     K = args.steps
     n_timed = {"learned": K, "batched": K, "frequency": K, "plain": min(K, 5), "plain_x8": min(K, 5),
                "learned_host_index": min(K, 3), "plain_host_index": min(K, 3)}
+    n_timed.update({k: K for k in extra})
     engines = {}
     ref_counts = [None]
     checked = [0]
