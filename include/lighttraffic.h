@@ -149,6 +149,8 @@ typedef struct lt_stats {
                                   zero-copy to finish the last walkers */
     uint64_t cache_slots;      /* out of core: partition slots on the device */
     uint64_t index_on_device;  /* out of core: 1 when the vertex index is resident on the device */
+    uint64_t refill_loads;     /* wave runs: loads that swapped a cached partition for one the
+                                  policy forecasts more entries for */
     double bucket_ms;          /* CUDA-event time of the bucketing (scatter) kernels */
     double host_wait_ms;       /* host time blocked waiting for each iteration's step kernel */
 } lt_stats;

@@ -541,6 +541,13 @@ public:
         return ready_ ? demand_[p] + (double)v.waiting[p] : (double)static_mass_[p];
     }
 
+    // Forecast entries per iteration: the network's (learned) or the moving
+    // average's (frequency) prediction over the label horizon, per iteration.
+    double visit_rate(const SchedView &, uint32_t p) override
+    {
+        return ready_ ? demand_[p] / (double)kLabelHorizon : -1.0;
+    }
+
 private:
 
     // A CUDA error in the policy's own work: keep the last forecasts and stop

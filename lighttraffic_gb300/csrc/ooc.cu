@@ -998,6 +998,49 @@ lt_status wave_step(Ooc &o, const RunParams &rp, WaveState &w, bool &done)
                 started++;
             }
         }
+        // Refill by forecast: with the cache full and no partition worth a
+        // load by its waiting walkers, swap an idle cached partition for an
+        // uncached one when the policy forecasts enough more entries for it
+        // over the rest of the run: (rate_in - rate_out) x remaining
+        // iterations x bytes per zero-copy hop must pay for the copy twice
+        // (the factor keeps forecast noise from thrashing the cache).
+        // Remaining iterations are estimated from the walkers still to be
+        // created.  Policies without a forecast (batched) never refill.
+        if (zc_ok && cand.empty() && started < m && free_slot(o) < 0 && n_idle < idle.size() && !o.serve) {
+            uint64_t left = 0;
+            for (uint32_t p = 0; p < o.P; p++) left += o.lazy_left[p];
+            const double made = (double)rp.W - (double)left;
+            const double rest_it = made > 0 ? std::max(16.0, (double)o.iteration * (double)left / made) : 16.0;
+            std::vector<std::pair<double, uint32_t>> in, out;
+            bool have = true;
+            for (uint32_t p = 0; p < o.P && have; p++) {
+                const double r = o.policy->visit_rate(v, p);
+                if (r < 0) have = false;
+                else if (o.slot_of[p] < 0 && !loading[p]) in.push_back({r, p});
+            }
+            if (have) {
+                for (size_t k = n_idle; k < idle.size(); k++) out.push_back({o.policy->visit_rate(v, idle[k]), idle[k]});
+                std::sort(in.begin(), in.end(), [](const std::pair<double, uint32_t> &a, const std::pair<double, uint32_t> &b) {
+                    return a.first != b.first ? a.first > b.first : a.second < b.second;
+                });
+                std::sort(out.begin(), out.end(), [](const std::pair<double, uint32_t> &a, const std::pair<double, uint32_t> &b) {
+                    return a.first != b.first ? a.first < b.first : a.second < b.second;
+                });
+                const double hop = (double)zc_bytes_per_hop(o);
+                for (size_t k = 0; k < in.size() && k < out.size() && started < m; k++) {
+                    const uint32_t pin = in[k].second, pout = out[k].second;
+                    const double gain = (in[k].first - out[k].first) * rest_it * hop;
+                    if (gain < 2.0 * (double)host_part_bytes(o, pin)) break;
+                    const int32_t slot = o.slot_of[pout];
+                    LT_TRY(evict_partition(o, pout));
+                    LT_TRY(start_load(o, pin, slot, &inflight));
+                    loading[pin] = 1;
+                    o.last_used[pin] = o.iteration;
+                    started++;
+                    e.stats.refill_loads++;
+                }
+            }
+        }
         if (started) e.stats.explicit_iterations++;
         if (!e.cfg.pipeline) {
             // no pipelining (--no-pipeline): the loads finish before this

@@ -69,6 +69,9 @@ public:
     virtual void observe(const SchedView &v) {}
     // Wave runs: higher = better kept in the cache (victims have the lowest).
     virtual double cache_score(const SchedView &v, uint32_t p) { return 0.0; }
+    // Wave runs: forecast walkers entering p per iteration, or < 0 when the
+    // policy has no forecast (then the cache is never refilled by forecast).
+    virtual double visit_rate(const SchedView &v, uint32_t p) { return -1.0; }
     // Wave runs: each step kernel drains every readable queue (all cached
     // partitions with walkers, plus a zero-copy set in the final phase) while
     // the loads for the next kernel run on the copy stream.  At most
