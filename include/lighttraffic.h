@@ -405,6 +405,8 @@ typedef struct lt_policy_stats {
     double net_loss;        /* mean squared error of the network on the last half of its training batches */
     double baseline_loss;   /* the same for the moving-average predictor on those batches */
     uint64_t predictions;   /* prediction passes consumed by the policy */
+    uint64_t net_used;      /* of those, passes that used the network's forecast (its running validation
+                               loss below the moving average's); the others used the moving average */
 } lt_policy_stats;
 
 /* Scheduling-policy statistics of the engine's last out-of-core runs.  No

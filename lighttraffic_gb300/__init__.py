@@ -60,7 +60,7 @@ class BatchTune(C.Structure):
 
 class PolicyStats(C.Structure):
     _fields_ = [("name", C.c_char * 16), ("train_steps", C.c_uint64), ("net_loss", C.c_double),
-                ("baseline_loss", C.c_double), ("predictions", C.c_uint64)]
+                ("baseline_loss", C.c_double), ("predictions", C.c_uint64), ("net_used", C.c_uint64)]
 
 
 class CheckpointInfo(C.Structure):
@@ -522,7 +522,7 @@ class Engine:
         s = PolicyStats()
         check(lib.lt_engine_policy_stats(self._h, C.byref(s)))
         return {"name": s.name.decode(), "train_steps": s.train_steps, "net_loss": s.net_loss,
-                "baseline_loss": s.baseline_loss, "predictions": s.predictions}
+                "baseline_loss": s.baseline_loss, "predictions": s.predictions, "net_used": s.net_used}
 
     def partition_stats(self) -> dict:
         """Per partition over the last out-of-core run: walkers entering it,

@@ -293,6 +293,7 @@ constexpr int kEvery = 2;  // features, training and prediction every kEvery ite
 constexpr float kLearningRate = 0.02f;
 constexpr float kMomentum = 0.9f;
 constexpr float kEmaKeep = 0.95f;
+constexpr double kGateKeep = 0.8;  // running average of the validation losses the gate compares
 constexpr int kRing = kHist + kLabelHorizon + 1;    // visit history ring (iterations)
 constexpr int kSnaps = kLabelHorizon / kEvery + 2;  // feature snapshots awaiting labels
 constexpr int kStage = 4;                           // host staging slots (iterations in flight)
@@ -356,11 +357,15 @@ __global__ void __launch_bounds__(256) pol_labels(float *Y, float *base, const f
     if (threadIdx.x == 0) *base = sh[0] / (float)P;
 }
 
-// demand = predicted visits over the label horizon.
-__global__ void pol_demand(float *demand, const float *pred, const float *X, uint32_t P)
+// demand = visits over the label horizon as the network predicts them;
+// base_demand = the same from the moving-average forecast alone.
+__global__ void pol_demand(float *demand, float *base_demand, const float *pred, const float *X, uint32_t P)
 {
-    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < P; p += gridDim.x * blockDim.x)
-        demand[p] = expm1f(fmaxf(0.f, X[(uint64_t)p * kMlpIn + 15] + pred[p]) * 16.0f);
+    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < P; p += gridDim.x * blockDim.x) {
+        const float f = X[(uint64_t)p * kMlpIn + 15];
+        demand[p] = expm1f(fmaxf(0.f, f + pred[p]) * 16.0f);
+        base_demand[p] = expm1f(fmaxf(0.f, f) * 16.0f);
+    }
 }
 
 __global__ void pol_copy(float *dst, const float *src, uint32_t n)
@@ -418,14 +423,14 @@ public:
         LT_CUDA_TRY(cudaMalloc(&d_stat_, 8ull * P_));
         LT_CUDA_TRY(cudaMalloc(&d_X_, 4ull * kSnaps * P_ * kMlpIn));
         LT_CUDA_TRY(cudaMalloc(&d_Y_, 4ull * P_));
-        LT_CUDA_TRY(cudaMalloc(&d_out_, 4ull * (P_ + 2)));
+        LT_CUDA_TRY(cudaMalloc(&d_out_, 4ull * (2 * P_ + 2)));
         LT_CUDA_TRY(cudaMalloc(&d_pred_, 4ull * P_));
         LT_CUDA_TRY(cudaMemset(d_ring_, 0, 4ull * kRing * P_));
         LT_CUDA_TRY(cudaMemset(d_ema_, 0, 4ull * P_));
-        LT_CUDA_TRY(cudaMemset(d_out_, 0, 4ull * (P_ + 2)));
+        LT_CUDA_TRY(cudaMemset(d_out_, 0, 4ull * (2 * P_ + 2)));
         LT_CUDA_TRY(cudaMemcpy(d_stat_, stat_.data(), 8ull * P_, cudaMemcpyHostToDevice));
         LT_TRY(host_alloc(h_stage_, 16ull * P_ * kStage, true));
-        LT_TRY(host_alloc(h_out_, 4ull * (P_ + 2), true));
+        LT_TRY(host_alloc(h_out_, 4ull * (2 * P_ + 2), true));
         if (!h_stage_.pinned || !h_out_.pinned) return fail(LT_ERR_NOMEM, "pinned staging for the prefetcher");
         void *dv = nullptr;
         LT_CUDA_TRY(cudaHostGetDevicePointer(&dv, h_stage_.ptr, 0));
@@ -473,13 +478,23 @@ public:
             const float *out = (const float *)h_out_.ptr;
             if (train_enqueued_) {
                 losses_.push_back({out[P_], out[P_ + 1]});
+                // running validation of the network against the moving
+                // average it corrects (each loss is taken before the SGD
+                // step on that batch, i.e. on data not yet trained on)
+                net_avg_ = kGateKeep * net_avg_ + (1.0 - kGateKeep) * out[P_];
+                base_avg_ = kGateKeep * base_avg_ + (1.0 - kGateKeep) * out[P_ + 1];
                 train_enqueued_ = false;
             }
             if (pred_enqueued_) {
-                for (uint32_t p = 0; p < P_; p++) demand_[p] = out[p];
+                // act on the network only while it forecasts better than
+                // the moving average; otherwise on the moving average
+                const bool net = net_avg_ < base_avg_;
+                const float *src = net ? out : out + P_ + 2;
+                for (uint32_t p = 0; p < P_; p++) demand_[p] = src[p];
                 pred_enqueued_ = false;
                 ready_ = true;
                 predictions_++;
+                net_used_ += net;
             }
         }
         float *dyn = (float *)(stage + 4ull * P_);
@@ -504,10 +519,10 @@ public:
         }
         if (trained_ >= 4) {
             if (net_.forward_dev(Xs, P_, d_pred_) != LT_OK) return fail_net();
-            pol_demand<<<blocks, 256, 0, st>>>(d_out_, d_pred_, Xs, P_);
+            pol_demand<<<blocks, 256, 0, st>>>(d_out_, d_out_ + P_ + 2, d_pred_, Xs, P_);
             pred_enqueued_ = true;
         }
-        pol_copy<<<blocks, 256, 0, st>>>(out_dev_, d_out_, P_ + 2);
+        pol_copy<<<(2 * P_ + 2 + 255) / 256, 256, 0, st>>>(out_dev_, d_out_, 2 * P_ + 2);
         if (cudaEventRecord(ev_, st) != cudaSuccess || cudaEventRecord(stage_ev_[slot], st) != cudaSuccess)
             return fail_net();
         inflight_ = true;
@@ -532,6 +547,7 @@ public:
         const size_t n = losses_.size() - from;
         st.net_loss = n ? a / n : 0.0;
         st.baseline_loss = n ? b / n : 0.0;
+        st.net_used = net_used_;
     }
 
     // Predicted visits once the predictor is trained; before that, the
@@ -561,7 +577,8 @@ private:
     uint32_t P_;
     bool use_net_;
     Mlp net_;
-    uint64_t t_ = 0, trained_ = 0, skipped_ = 0, predictions_ = 0;
+    uint64_t t_ = 0, trained_ = 0, skipped_ = 0, predictions_ = 0, net_used_ = 0;
+    double net_avg_ = 1e30, base_avg_ = 0.0;  // validation gate (running losses)
     bool ready_ = false, inflight_ = false, pred_enqueued_ = false, train_enqueued_ = false, failed_ = false;
     std::vector<std::pair<double, double>> losses_;  // (network, moving average) per training batch
     cudaEvent_t ev_ = nullptr;
