@@ -113,6 +113,10 @@ typedef struct lt_engine_cfg {
                                         group may touch (0 = 512 MiB; 128 MiB while serving) */
     uint64_t sweep_walkers;          /* wave runs: walkers left outside the cache at or below which one
                                         kernel reads every uncached partition zero-copy (0 = 2^18) */
+    uint32_t load_factor;            /* wave runs: a partition is loaded once its waiting walkers reach
+                                        load_factor x zerocopy_threshold (0 = 256 / host bytes per
+                                        zero-copy hop: 8 with the device index, 4 without) */
+    int bucket_items;                /* walkers per thread of a bucketing tile: 16 (0) or 8 */
 } lt_engine_cfg;
 
 typedef struct lt_stats {
@@ -367,9 +371,25 @@ typedef struct lt_batch_tune {
     int tuned;        /* 1 once lt_engine_autotune ran */
 } lt_batch_tune;
 
-/* Time the batch pipeline on a synthetic batch for each block size and table
- * load factor and keep the fastest for this engine. */
+/* Resident engine: time the batch pipeline on a synthetic batch for each
+ * block size and table load factor and keep the fastest.  Out-of-core
+ * engine: time cold-cache PPR trial runs and tune, one knob at a time, the
+ * zero-copy group footprint, the load threshold factor, the step kernel's
+ * CTAs per SM and the bucketing tile (lt_engine_ooc_tune reports them).
+ * Results never depend on these choices. */
 lt_status lt_engine_autotune(lt_engine *e);
+
+typedef struct lt_ooc_tune {
+    int tuned;                /* 1 once lt_engine_autotune ran on an out-of-core engine */
+    uint64_t trial_walkers;   /* walkers of each trial run */
+    uint64_t zc_group_bytes;  /* chosen lt_engine_cfg values (0 = default) */
+    uint32_t load_factor;
+    int ctas_per_sm;
+    int bucket_items;
+    double default_ms;        /* trial run time with the values before tuning */
+    double tuned_ms;          /* with the chosen values */
+} lt_ooc_tune;
+lt_status lt_engine_ooc_tune(const lt_engine *e, lt_ooc_tune *out);
 lt_status lt_engine_batch_tune(const lt_engine *e, lt_batch_tune *out);
 
 /* ------------------------------------------------------------------ serving */

@@ -51,11 +51,17 @@ class EngineCfg(C.Structure):
                 ("num_device_walkers", C.c_uint64), ("sched", C.c_int), ("pipeline", C.c_int),
                 ("zerocopy_threshold", C.c_uint64), ("seed", C.c_uint64), ("block_size", C.c_int),
                 ("ctas_per_sm", C.c_int), ("resident_index", C.c_int), ("zc_group_bytes", C.c_uint64),
-                ("sweep_walkers", C.c_uint64)]
+                ("sweep_walkers", C.c_uint64), ("load_factor", C.c_uint32), ("bucket_items", C.c_int)]
 
 
 class BatchTune(C.Structure):
     _fields_ = [("block", C.c_int), ("ctas_per_sm", C.c_int), ("load_shift", C.c_int), ("tuned", C.c_int)]
+
+
+class OocTune(C.Structure):
+    _fields_ = [("tuned", C.c_int), ("trial_walkers", C.c_uint64), ("zc_group_bytes", C.c_uint64),
+                ("load_factor", C.c_uint32), ("ctas_per_sm", C.c_int), ("bucket_items", C.c_int),
+                ("default_ms", C.c_double), ("tuned_ms", C.c_double)]
 
 
 class PolicyStats(C.Structure):
@@ -131,6 +137,7 @@ def _load():
         "lt_ppr_batch": ([vp, C.c_uint32, u32p, u64p, u64p, C.c_float, u64p, u32p, u32p, C.c_uint64], C.c_int),
         "lt_ppr_batch_device": ([vp, C.c_uint32, vp, vp, vp, C.c_float, vp, vp, vp, C.c_uint64, vp], C.c_int),
         "lt_engine_autotune": ([vp], C.c_int),
+        "lt_engine_ooc_tune": ([vp, C.POINTER(OocTune)], C.c_int),
         "lt_serve_open": ([vp, C.c_uint32, C.c_uint64, C.c_float, C.POINTER(vp)], C.c_int),
         "lt_serve_submit": ([vp, C.c_uint32, C.c_uint64, C.c_uint64, C.c_double, C.POINTER(C.c_uint64)], C.c_int),
         "lt_serve_step": ([vp, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)], C.c_int),
@@ -420,7 +427,7 @@ class Engine:
     def __init__(self, graph: Graph, partitions: int = 0, batch: int = 0, seed: int = 0x5EED5EED,
                  sched: int = SCHED_PLAIN, pipeline: bool = True, zerocopy_threshold=None,
                  device: int = 0, ctas_per_sm: int = 0, resident_index: bool = True, zc_group_bytes: int = 0,
-                 sweep_walkers: int = 0):
+                 sweep_walkers: int = 0, load_factor: int = 0, bucket_items: int = 0):
         cfg = EngineCfg()
         lib.lt_engine_cfg_default(C.byref(cfg))
         cfg.device = device
@@ -435,6 +442,8 @@ class Engine:
         cfg.resident_index = int(resident_index)
         cfg.zc_group_bytes = zc_group_bytes
         cfg.sweep_walkers = sweep_walkers
+        cfg.load_factor = load_factor
+        cfg.bucket_items = bucket_items
         self.graph = graph
         self._h = C.c_void_p()
         check(lib.lt_engine_create(graph._h, C.byref(cfg), C.byref(self._h)))
@@ -486,8 +495,26 @@ class Engine:
         return off, v[:tot], c[:tot]
 
     def autotune(self) -> dict:
+        """Resident engine: tune the batch pipeline (block size, table load
+        factor).  Out-of-core engine: tune the zero-copy group footprint,
+        load threshold factor, step-kernel CTAs per SM and bucketing tile on
+        cold-cache PPR trial runs.  Returns the chosen values."""
         check(lib.lt_engine_autotune(self._h))
+        if self.graph.num_partitions > 0 and self._ooc():
+            return self.ooc_tune()
         return self.batch_tune()
+
+    def _ooc(self) -> bool:
+        return bool(self.ooc_tune_raw().tuned)
+
+    def ooc_tune_raw(self):
+        t = OocTune()
+        check(lib.lt_engine_ooc_tune(self._h, C.byref(t)))
+        return t
+
+    def ooc_tune(self) -> dict:
+        t = self.ooc_tune_raw()
+        return {k: getattr(t, k) for k, _ in t._fields_}
 
     def batch_tune(self) -> dict:
         t = BatchTune()

@@ -382,7 +382,18 @@ double lt_serve_now_ms(void) { return serve_now_ms(); }
 lt_status lt_engine_autotune(lt_engine *e)
 {
     if (!e) return fail(LT_ERR_INVALID, "null engine");
+    if (e->ooc) {
+        LT_CUDA_TRY(cudaSetDevice(e->device));
+        return ooc_autotune(e, &e->ooc_tune);
+    }
     return batch_autotune(e);
+}
+
+lt_status lt_engine_ooc_tune(const lt_engine *e, lt_ooc_tune *out)
+{
+    if (!e || !out) return fail(LT_ERR_INVALID, "null argument");
+    *out = e->ooc_tune;
+    return LT_OK;
 }
 
 lt_status lt_engine_batch_tune(const lt_engine *e, lt_batch_tune *out)

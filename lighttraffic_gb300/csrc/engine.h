@@ -46,6 +46,7 @@ struct lt_engine {
     lt::BatchState *batch = nullptr;  // batched multi-source PPR buffers and captured graph
 
     lt_stats stats{};
+    lt_ooc_tune ooc_tune{};  // what lt_engine_autotune chose for the out-of-core engine
 };
 
 namespace lt {

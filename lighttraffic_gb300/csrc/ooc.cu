@@ -697,6 +697,7 @@ lt_status step_and_bucket_parts(Ooc &o, const RunParams &rp, const std::vector<u
     sa.win_off = o.d_planbuf + o.P;
     sa.plan_chunks = o.d_planbuf + 2ull * o.P;
     sa.P = o.P;
+    sa.items = e.cfg.bucket_items;
     Ooc::Timed tb{ev_get(o), ev_get(o), kTBucket};
     LT_CUDA_TRY(cudaEventRecord(tb.a, e.s_compute));
     LT_CUDA_TRY(launch_scatter(sa, e.device, e.s_compute));
@@ -891,7 +892,7 @@ lt_status wave_step(Ooc &o, const RunParams &rp, WaveState &w, bool &done)
     // 1.20-1.25 s (3 100 / 256 loads).  Serving keeps the reference
     // threshold and smaller zero-copy groups: shorter steps matter more
     // there than fewer loads.
-    const uint64_t load_factor = o.serve ? 1 : 256 / zc_bytes_per_hop(o);
+    const uint64_t load_factor = o.serve ? 1 : e.cfg.load_factor ? e.cfg.load_factor : 256 / zc_bytes_per_hop(o);
     const uint64_t load_min = !zc_ok ? 1
                               : o.zc_threshold > UINT64_MAX / load_factor ? UINT64_MAX
                                                                           : o.zc_threshold * load_factor;
@@ -1282,7 +1283,7 @@ lt_status ooc_create(lt_engine *e, Ooc **out)
     }
     const size_t smem = part_smem(o->P);
     if (smem > 64 * 1024) return bail(fail(LT_ERR_UNSUPPORTED, "partition count %u needs %zu bytes of shared memory", o->P, smem));
-    for (int app = 0; app < 3; app++) o->grid[app] = part_grid(app, 0, e->device, smem);
+    for (int app = 0; app < 3; app++) o->grid[app] = part_grid(app, 0, e->device, smem, e->cfg.ctas_per_sm);
     *out = o;
     return LT_OK;
 }
@@ -1304,6 +1305,91 @@ void ooc_destroy(Ooc *o)
 }
 
 void ooc_policy_stats(const Ooc *o, lt_policy_stats &s) { o->policy->stats(s); }
+
+// Autotuner of the out-of-core engine.  It times cold-cache PPR trial runs
+// (from the vertex with the most out-edges, as many walkers as the device
+// pool holds, at most 2^26) and walks the runtime knobs one at a time,
+// keeping each value that shortens the trial (coordinate descent): the
+// zero-copy group footprint and the load threshold factor of wave runs, the
+// step kernel's resident CTAs per SM and the bucketing tile.  Every knob
+// changes only the schedule, so results are unchanged.  The walker chunk
+// (8192 walkers) is not tuned: it is the unit of the host spill slabs and of
+// the checkpoint file.
+lt_status ooc_autotune(lt_engine *e, lt_ooc_tune *out)
+{
+    Ooc &o = *e->ooc;
+    lt_graph &g = *e->g;
+    if (o.serve) return fail(LT_ERR_INVALID, "the engine is serving");
+    uint32_t src = 0;
+    for (uint32_t v = 0; v < g.V; v++)
+        if (g.rowptr()[v + 1] - g.rowptr()[v] > g.rowptr()[src + 1] - g.rowptr()[src]) src = v;
+    const uint64_t pool = e->cfg.num_device_walkers ? e->cfg.num_device_walkers : (1ull << 26);
+    const uint64_t W = std::max<uint64_t>(1, std::min<uint64_t>(std::min<uint64_t>(pool, 1ull << 26), 2ull * g.V));
+    const int occ = part_grid(kPPR, 0, e->device, part_smem(o.P), 0) / std::max(1, e->sms);
+    const lt_engine_cfg keep = e->cfg;
+    auto trial = [&](double &ms) -> lt_status {
+        for (int app = 0; app < 3; app++) o.grid[app] = part_grid(app, 0, e->device, part_smem(o.P), e->cfg.ctas_per_sm);
+        ms = 1e30;
+        for (int rep = 0; rep < 2; rep++) {
+            LT_TRY(ooc_drop_cache(&o));
+            LT_TRY(ooc_run(e, kPPR, kStartSource, src, W, 0, 1, 0, 0.15f, nullptr, nullptr, nullptr));
+            ms = std::min(ms, e->stats.running_ms);
+        }
+        return LT_OK;
+    };
+    double best = 0;
+    lt_status st = trial(best);
+    const double first = best;
+    struct Knob {
+        uint64_t *u64;
+        uint32_t *u32;
+        int *i32;
+        std::vector<uint64_t> values;
+    };
+    std::vector<Knob> knobs;
+    knobs.push_back({&e->cfg.zc_group_bytes, nullptr, nullptr, {256ull << 20, 512ull << 20, 1024ull << 20}});
+    knobs.push_back({nullptr, &e->cfg.load_factor, nullptr, {4, 8, 16}});
+    std::vector<uint64_t> ctas;
+    for (int c = occ; c >= 1 && c >= occ - 2; c--) ctas.push_back((uint64_t)c);
+    knobs.push_back({nullptr, nullptr, &e->cfg.ctas_per_sm, ctas});
+    knobs.push_back({nullptr, nullptr, &e->cfg.bucket_items, {16, 8}});
+    for (const Knob &k : knobs) {
+        if (st != LT_OK) break;
+        const uint64_t was = k.u64 ? *k.u64 : k.u32 ? *k.u32 : (uint64_t)*k.i32;
+        uint64_t pick = was;
+        for (uint64_t val : k.values) {
+            if (k.u64) *k.u64 = val;
+            if (k.u32) *k.u32 = (uint32_t)val;
+            if (k.i32) *k.i32 = (int)val;
+            double ms = 0;
+            st = trial(ms);
+            if (st != LT_OK) break;
+            if (ms < best * 0.99) {
+                best = ms;
+                pick = val;
+            }
+        }
+        if (k.u64) *k.u64 = pick;
+        if (k.u32) *k.u32 = (uint32_t)pick;
+        if (k.i32) *k.i32 = (int)pick;
+    }
+    if (st != LT_OK) {
+        e->cfg = keep;
+        for (int app = 0; app < 3; app++) o.grid[app] = part_grid(app, 0, e->device, part_smem(o.P), e->cfg.ctas_per_sm);
+        return st;
+    }
+    for (int app = 0; app < 3; app++) o.grid[app] = part_grid(app, 0, e->device, part_smem(o.P), e->cfg.ctas_per_sm);
+    LT_TRY(ooc_drop_cache(&o));
+    out->tuned = 1;
+    out->trial_walkers = W;
+    out->zc_group_bytes = e->cfg.zc_group_bytes;
+    out->load_factor = e->cfg.load_factor;
+    out->ctas_per_sm = e->cfg.ctas_per_sm;
+    out->bucket_items = e->cfg.bucket_items;
+    out->default_ms = first;
+    out->tuned_ms = best;
+    return LT_OK;
+}
 
 void ooc_partition_stats(const Ooc *o, uint64_t *visits, uint64_t *cached_visits, uint64_t *cached_launches)
 {

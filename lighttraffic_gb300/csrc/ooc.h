@@ -36,6 +36,7 @@ lt_status ooc_create(lt_engine *e, Ooc **out);
 void ooc_destroy(Ooc *o);
 lt_status ooc_drop_cache(Ooc *o);
 void ooc_policy_stats(const Ooc *o, lt_policy_stats &s);
+lt_status ooc_autotune(lt_engine *e, lt_ooc_tune *out);
 void ooc_partition_stats(const Ooc *o, uint64_t *visits, uint64_t *cached_visits, uint64_t *cached_launches);
 lt_status ooc_run(lt_engine *e, int app, int start, uint32_t source, uint64_t W, uint32_t length, uint32_t runs,
                   uint32_t run_base, float prob, uint64_t *counts_out, uint32_t *endpoints_out, uint32_t *paths_out);

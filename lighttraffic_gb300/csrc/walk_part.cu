@@ -447,14 +447,21 @@ __global__ void __launch_bounds__(kPartBlock) scatter_kernel(ScatterArgs a)
 // The plain scatter above wrote each walker with four isolated 4-byte stores
 // and made one global atomic per (1024-walker tile, destination), i.e.
 // nearly one per walker when the walkers spread over ~1000 partitions.
-constexpr int kBucketItems = 16;
-constexpr int kBucketTile = kPartBlock * kBucketItems;  // 4096 walkers
-constexpr int kBucketFields = 5;                         // cur, step, idx, query, dest
+// The tile is kPartBlock x ITEMS walkers (ITEMS 16: 4096, the default; 8:
+// 2048, chosen by the autotuner when it is faster).
+constexpr int kBucketFields = 5;  // cur, step, idx, query, dest
 
-size_t bucket_smem(uint32_t P) { return sizeof(uint32_t) * (2ull * P + (uint64_t)kBucketFields * kBucketTile); }
+template <int ITEMS>
+size_t bucket_smem(uint32_t P)
+{
+    return sizeof(uint32_t) * (2ull * P + (uint64_t)kBucketFields * kPartBlock * ITEMS);
+}
 
+template <int ITEMS>
 __global__ void __launch_bounds__(kPartBlock, 2) bucket_sort_kernel(ScatterArgs a)
 {
+    constexpr int kBucketItems = ITEMS;
+    constexpr int kBucketTile = kPartBlock * ITEMS;
     extern __shared__ uint32_t smem[];
     __shared__ uint32_t warp_tot[kPartBlock / 32];
     __shared__ uint32_t tile_total;
@@ -554,11 +561,12 @@ int occ_part(size_t smem)
 
 size_t part_smem(uint32_t P) { return P <= kSmemPartMax ? sizeof(uint32_t) * (3ull * P + 1 + (P + 31) / 32) : 0; }
 
-int part_grid(int app, int /*start*/, int device, size_t smem)
+int part_grid(int app, int /*start*/, int device, size_t smem, int ctas_per_sm)
 {
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
     int occ = app == kPPR ? occ_part<kPPR>(smem) : app == kPageRank ? occ_part<kPageRank>(smem) : occ_part<kWalk>(smem);
+    if (ctas_per_sm > 0 && ctas_per_sm < occ) occ = ctas_per_sm;
     if (occ < 1) occ = 1;
     return sms * occ;
 }
@@ -591,17 +599,26 @@ cudaError_t launch_scatter(const ScatterArgs &a, int device, cudaStream_t st)
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
     if (a.P <= kSmemPartMax) {
-        const size_t smem = bucket_smem(a.P);
         static thread_local int configured_device = -1;
         if (configured_device != device) {
-            const cudaError_t e = cudaFuncSetAttribute(bucket_sort_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                       (int)bucket_smem(kSmemPartMax));
+            cudaError_t e = cudaFuncSetAttribute(bucket_sort_kernel<16>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                 (int)bucket_smem<16>(kSmemPartMax));
+            if (e == cudaSuccess)
+                e = cudaFuncSetAttribute(bucket_sort_kernel<8>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)bucket_smem<8>(kSmemPartMax));
             if (e != cudaSuccess) return e;
             configured_device = device;
         }
-        const uint64_t tiles = (a.n + kBucketTile - 1) / kBucketTile;
-        const uint64_t blocks = std::min<uint64_t>(tiles, (uint64_t)sms * (smem <= 110 * 1024 ? 2 : 1));
-        bucket_sort_kernel<<<(unsigned)blocks, kPartBlock, smem, st>>>(a);
+        const int items = a.items == 8 ? 8 : 16;
+        const size_t smem = items == 8 ? bucket_smem<8>(a.P) : bucket_smem<16>(a.P);
+        const uint64_t tile = (uint64_t)kPartBlock * items;
+        const uint64_t tiles = (a.n + tile - 1) / tile;
+        const uint64_t per_sm = smem <= 72 * 1024 ? 3 : smem <= 110 * 1024 ? 2 : 1;
+        const uint64_t blocks = std::min<uint64_t>(tiles, (uint64_t)sms * per_sm);
+        if (items == 8)
+            bucket_sort_kernel<8><<<(unsigned)blocks, kPartBlock, smem, st>>>(a);
+        else
+            bucket_sort_kernel<16><<<(unsigned)blocks, kPartBlock, smem, st>>>(a);
         return cudaGetLastError();
     }
     const uint64_t tile = (uint64_t)kPartBlock * kScatterItems;

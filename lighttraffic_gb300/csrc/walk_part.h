@@ -99,6 +99,7 @@ struct ScatterArgs {
     const uint32_t *win_off;       // P: start of the destination's window in plan_chunks
     const uint32_t *plan_chunks;   // chunk ids of every window
     uint32_t P;
+    int items;                     // walkers per thread of a bucketing tile (8 or 16; 0 = 16)
 };
 
 // Walkers of newly admitted queries: walker i of query slot q (i < n) goes to
@@ -112,7 +113,8 @@ struct InjectArgs {
     uint64_t seed, thr;
 };
 
-int part_grid(int app, int start, int device, size_t smem);
+// Step-kernel grid: SMs x resident CTAs (capped at ctas_per_sm when > 0).
+int part_grid(int app, int start, int device, size_t smem, int ctas_per_sm);
 cudaError_t launch_inject(const InjectArgs &a, int device, cudaStream_t st);
 size_t part_smem(uint32_t P);
 cudaError_t launch_walk_part(const StepArgs &a, int app, int grid, cudaStream_t st);

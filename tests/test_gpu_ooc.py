@@ -222,3 +222,21 @@ def test_c2s_scale_ooc(lt, require_gpu, c2s, sched, pipeline):
     if not pipeline:
         assert s["overlap_computes"] == 0
     e.close()
+
+
+@pytest.mark.parametrize("sched", [0, 2])
+def test_ooc_autotune_keeps_results(lt, require_gpu, g16, sched):
+    """The out-of-core autotuner changes only the schedule: after tuning, and
+    with either bucketing tile and a capped step-kernel grid, the counts are
+    the oracle's."""
+    rp, col = g16
+    want, _, _ = oracle.ppr(rp, col, 0, 200000, prob=0.15, seed=3)
+    g, e = _eng(lt, rp, col, 256 << 10, partitions=4, sched=sched, seed=3)
+    t = e.autotune()
+    assert t["tuned"] == 1 and t["trial_walkers"] > 0 and t["bucket_items"] in (0, 8, 16)
+    assert t["tuned_ms"] <= t["default_ms"]
+    assert (e.ppr(0, 200000, 0.15) == want).all()
+    for items, ctas in ((8, 1), (16, 2)):
+        g, e = _eng(lt, rp, col, 256 << 10, partitions=4, sched=sched, seed=3, bucket_items=items, ctas_per_sm=ctas,
+                    load_factor=2, zc_group_bytes=1 << 20)
+        assert (e.ppr(0, 200000, 0.15) == want).all()
