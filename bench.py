@@ -103,6 +103,8 @@ def parse():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--cpu-seconds", type=float, default=12.0,
                    help="target CPU time of the cpu_baseline sample")
+    p.add_argument("--no-autotune", action="store_true",
+                   help="out-of-core configs: run with the default knobs instead of the autotuner's")
     p.add_argument("--variants", default="",
                    help="out-of-core configs: comma-separated subset of the variants to run (profiler "
                         "captures; the line then carries no comparisons and no serving)")
@@ -445,6 +447,20 @@ def gb300_ooc(args, cfg):
                              zero_copy_bytes=st["zerocopy_bytes"])
         return (t1 - t0, st, e.policy_stats())
 
+    # the out-of-core autotuner on the headline engine; the ablations get the
+    # same wave knobs and every variant the same grid and bucketing tile, so
+    # the comparisons differ only in the policy
+    tune = None
+    if "learned" in variants and not args.no_autotune:
+        engines["learned"] = lt.Engine(g, partitions=cfg["partitions"], batch=cfg["batch"], seed=SEED_WALK,
+                                       device=local, **variants["learned"])
+        tune = engines["learned"].autotune()
+        shared = dict(ctas_per_sm=tune["ctas_per_sm"], bucket_items=tune["bucket_items"])
+        wave = dict(zc_group_bytes=tune["zc_group_bytes"], load_factor=tune["load_factor"])
+        for name in variants:
+            if name == "learned":
+                continue
+            variants[name] = {**variants[name], **shared, **(wave if name in ("batched", "frequency") else {})}
     for i in range(args.warmup):
         for name in variants:
             if i == 0 or name == "learned":
@@ -504,7 +520,7 @@ def gb300_ooc(args, cfg):
     clk = clocks.summary(wall0 - 0.5, wall1)
     if args.variants:
         print(json.dumps({"profile_run": True, "config": workload_config(args.config, cfg, V, E, P),
-                          "variants": res, "first_run": first_run}), flush=True)
+                          "variants": res, "autotune": tune, "first_run": first_run}), flush=True)
         for e in engines.values():
             e.close()
         return 0
@@ -586,6 +602,7 @@ def gb300_ooc(args, cfg):
                       "zerocopy_bytes": "32 B per zero-copy hop with the vertex index on the device (62 B "
                                         "without), measured with ncu"},
         "variants": res,
+        "autotune": tune,
         "learned_over_plain": {
             "vs_plain": {"steps_per_s": value / Pn["value"], "bytes_per_step": L["bytes_per_step"] / Pn["bytes_per_step"]},
             "vs_plain_x8": {"steps_per_s": value / P8["value"], "bytes_per_step": L["bytes_per_step"] / P8["bytes_per_step"]},
