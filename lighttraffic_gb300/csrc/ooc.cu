@@ -83,7 +83,7 @@ struct Ooc {
     uint64_t slot_stride = 0;
     uint8_t *d_slots = nullptr;
     std::vector<int32_t> slot_of, part_in_slot;
-    std::vector<uint64_t> last_used;
+    std::vector<uint64_t> last_used, loaded_at;
     std::vector<unsigned long long> h_rp, h_col;
 
     uint32_t *d_node_off = nullptr;
@@ -342,6 +342,7 @@ lt_status start_load(Ooc &o, uint32_t p, int32_t slot, std::vector<std::pair<uin
     o.timed.push_back(t);
     o.h_rp[p] = (unsigned long long)(uintptr_t)(o.d_index ? (uint8_t *)(o.d_index + n0) : base);
     o.h_col[p] = (unsigned long long)(uintptr_t)(base + col_off);
+    o.loaded_at[p] = o.iteration;
     o.slot_of[p] = slot;
     o.part_in_slot[slot] = (int32_t)p;
     if (deferred) {
@@ -851,6 +852,9 @@ uint64_t wave_lazy_budget(Ooc &o, uint64_t chunks, uint64_t walkers, uint64_t le
 }
 
 constexpr uint64_t kSweepWalkers = 1ull << 18;    // about one walker per resident lane
+constexpr double kRefillHorizon = 512.0;          // iterations a refill is credited with at most
+constexpr uint64_t kRefillHold = 64;              // iterations a partition stays before a refill may evict it
+constexpr int kRefillMax = 2;                     // refill swaps started per iteration
 // zero-copy group: estimated host bytes its walkers touch.  Measured on the
 // 2^33-edge graph: 128 MB 1.73 s, 256 MB 1.67 s, 512 MB 1.65 s per run (one
 // kernel over every partition with tens of millions of walkers: 6.9 s)
@@ -1003,15 +1007,21 @@ lt_status wave_step(Ooc &o, const RunParams &rp, WaveState &w, bool &done)
         // load by its waiting walkers, swap an idle cached partition for an
         // uncached one when the policy forecasts enough more entries for it
         // over the rest of the run: (rate_in - rate_out) x remaining
-        // iterations x bytes per zero-copy hop must pay for the copy twice
-        // (the factor keeps forecast noise from thrashing the cache).
-        // Remaining iterations are estimated from the walkers still to be
-        // created.  Policies without a forecast (batched) never refill.
+        // iterations x bytes per zero-copy hop must pay for the copy four
+        // times over, the victim must have been cached for kRefillHold
+        // iterations, and at most kRefillMax swaps start per iteration --
+        // per-iteration forecasts are noisy, and a first version (margin 2,
+        // no hold, up to 8 swaps per iteration) made 3 000 swaps per c2 run
+        // and doubled its host-link bytes.  Remaining iterations are
+        // estimated from the walkers still to be created (at most
+        // kRefillHorizon).  Policies without a forecast (batched) never
+        // refill.
         if (zc_ok && cand.empty() && started < m && free_slot(o) < 0 && n_idle < idle.size() && !o.serve) {
             uint64_t left = 0;
             for (uint32_t p = 0; p < o.P; p++) left += o.lazy_left[p];
             const double made = (double)rp.W - (double)left;
-            const double rest_it = made > 0 ? std::max(16.0, (double)o.iteration * (double)left / made) : 16.0;
+            const double rest_it =
+                std::min(kRefillHorizon, made > 0 ? std::max(16.0, (double)o.iteration * (double)left / made) : 16.0);
             std::vector<std::pair<double, uint32_t>> in, out;
             bool have = true;
             for (uint32_t p = 0; p < o.P && have; p++) {
@@ -1020,7 +1030,9 @@ lt_status wave_step(Ooc &o, const RunParams &rp, WaveState &w, bool &done)
                 else if (o.slot_of[p] < 0 && !loading[p]) in.push_back({r, p});
             }
             if (have) {
-                for (size_t k = n_idle; k < idle.size(); k++) out.push_back({o.policy->visit_rate(v, idle[k]), idle[k]});
+                for (size_t k = n_idle; k < idle.size(); k++)
+                    if (o.iteration >= o.loaded_at[idle[k]] + kRefillHold)
+                        out.push_back({o.policy->visit_rate(v, idle[k]), idle[k]});
                 std::sort(in.begin(), in.end(), [](const std::pair<double, uint32_t> &a, const std::pair<double, uint32_t> &b) {
                     return a.first != b.first ? a.first > b.first : a.second < b.second;
                 });
@@ -1028,10 +1040,12 @@ lt_status wave_step(Ooc &o, const RunParams &rp, WaveState &w, bool &done)
                     return a.first != b.first ? a.first < b.first : a.second < b.second;
                 });
                 const double hop = (double)zc_bytes_per_hop(o);
-                for (size_t k = 0; k < in.size() && k < out.size() && started < m; k++) {
+                int swaps = 0;
+                for (size_t k = 0; k < in.size() && k < out.size() && started < m && swaps < kRefillMax; k++) {
                     const uint32_t pin = in[k].second, pout = out[k].second;
                     const double gain = (in[k].first - out[k].first) * rest_it * hop;
-                    if (gain < 2.0 * (double)host_part_bytes(o, pin)) break;
+                    if (gain < 4.0 * (double)host_part_bytes(o, pin)) break;
+                    swaps++;
                     const int32_t slot = o.slot_of[pout];
                     LT_TRY(evict_partition(o, pout));
                     LT_TRY(start_load(o, pin, slot, &inflight));
@@ -1247,6 +1261,7 @@ lt_status ooc_create(lt_engine *e, Ooc **out)
     o->slot_of.assign(o->P, -1);
     o->part_in_slot.assign(o->K, -1);
     o->last_used.assign(o->P, 0);
+    o->loaded_at.assign(o->P, 0);
     o->h_rp.assign(o->P, 0);
     o->h_col.assign(o->P, 0);
     o->arrivals.assign(o->P, 0);
@@ -1728,6 +1743,7 @@ lt_status ckpt_point(Ooc &o, const RunParams &rp, bool &stop)
 lt_status run_prepare(Ooc &o, const RunParams &rp)
 {
     lt_graph &g = *o.g;
+    o.policy->run_start();
     reset_queues(o);
     refresh_all(o);
     o.prev_computed = -1;

@@ -83,6 +83,8 @@ public:
     virtual size_t wave_loads() const { return 8; }
     // Cache emptied (the learned state of a policy survives).
     virtual void reset() {}
+    // A new run starts (its walkers are about to be created).
+    virtual void run_start() {}
     virtual void stats(lt_policy_stats &s) const
     {
         std::memset(&s, 0, sizeof s);
