@@ -489,7 +489,8 @@ def gb300_ooc(args, cfg):
                      "bytes_per_step": link_bytes(st) / st["moves"],
                      "ms_per_step": el / len(times[name]) * 1e3, "runs": len(times[name]),
                      "iterations": st["iterations"], "partition_loads": st["partition_loads"],
-                     "refill_loads": st["refill_loads"], "zerocopy_groups": st["zerocopy_groups"], "zerocopy_sweeps": st["zerocopy_sweeps"],
+                     "refill_loads": st["refill_loads"], "prefill_loads": st["prefill_loads"],
+                     "zerocopy_groups": st["zerocopy_groups"], "zerocopy_sweeps": st["zerocopy_sweeps"],
                      "overlap_computes": st["overlap_computes"], "cache_slots": st["cache_slots"],
                      "index_on_device": bool(st["index_on_device"]), "step_s": spread(times[name]),
                      # where one run's time goes (last run): CUDA-event time of

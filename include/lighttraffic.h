@@ -155,6 +155,8 @@ typedef struct lt_stats {
     uint64_t index_on_device;  /* out of core: 1 when the vertex index is resident on the device */
     uint64_t refill_loads;     /* wave runs: loads that swapped a cached partition for one the
                                   policy forecasts more entries for */
+    uint64_t prefill_loads;    /* wave runs: loads into a cold cache at a run's start, in the order of
+                                  the policy's forecast (entries of its previous runs) */
     double bucket_ms;          /* CUDA-event time of the bucketing (scatter) kernels */
     double host_wait_ms;       /* host time blocked waiting for each iteration's step kernel */
 } lt_stats;

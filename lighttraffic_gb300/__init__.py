@@ -91,6 +91,7 @@ class Stats(C.Structure):
                 ("handoffs", C.c_uint64), ("overlap_computes", C.c_uint64),
                 ("zerocopy_groups", C.c_uint64), ("zerocopy_sweeps", C.c_uint64),
                 ("cache_slots", C.c_uint64), ("index_on_device", C.c_uint64), ("refill_loads", C.c_uint64),
+                ("prefill_loads", C.c_uint64),
                 ("bucket_ms", C.c_double), ("host_wait_ms", C.c_double)]
 
     def as_dict(self):

@@ -574,6 +574,18 @@ public:
 
     // Predicted visits once the predictor is trained; before that, the
     // partition's edge count (a hub-heavy RMAT prior).
+    // The partitions that drew the most entries in the previous runs.
+    bool prefill(const SchedView &v, std::vector<uint32_t> &order) override
+    {
+        if (!have_history_ || t_run_ > 0) return false;
+        order.resize(P_);
+        for (uint32_t p = 0; p < P_; p++) order[p] = p;
+        std::sort(order.begin(), order.end(), [&](uint32_t a, uint32_t b) {
+            return history_[a] != history_[b] ? history_[a] > history_[b] : a < b;
+        });
+        return true;
+    }
+
     double cache_score(const SchedView &v, uint32_t p) override
     {
         if (have_history_ && t_run_ < (uint64_t)kRunWarm) return history_[p] + (double)v.waiting[p];

@@ -85,6 +85,10 @@ public:
     virtual void reset() {}
     // A new run starts (its walkers are about to be created).
     virtual void run_start() {}
+    // Wave runs, cold cache at a run's start: partitions to load into the
+    // free slots before any walker queues, best first (false: none; the
+    // slots then fill as walkers arrive).
+    virtual bool prefill(const SchedView &v, std::vector<uint32_t> &order) { return false; }
     virtual void stats(lt_policy_stats &s) const
     {
         std::memset(&s, 0, sizeof s);
