@@ -463,10 +463,11 @@ lt_status lt_host_link_gbs(int device, double *gbs);
  * instead of through the driver's staging copies into pageable memory.  No
  * counterpart in the reference. */
 lt_status lt_host_alloc(uint64_t bytes, void **out);
-/* Random-read rate of the GPU from mapped pinned host memory, in GB/s of the
- * 32-byte sectors the link moves (one per zero-copy hop): the ceiling of the
- * zero-copy step kernels.  No counterpart in the reference. */
-lt_status lt_host_gather_gbs(int device, double *gbs);
+/* Random-read rate of the GPU from a mapped pinned host buffer of `bytes`
+ * (0 = 2 GiB), in GB/s of the 32-byte sectors the link moves (one per
+ * zero-copy hop): the ceiling of the zero-copy step kernels.  No counterpart
+ * in the reference. */
+lt_status lt_host_gather_gbs(int device, uint64_t bytes, double *gbs);
 void lt_host_free(void *p);
 
 /* The remainder x[i] % d[i] as the walk kernels compute it (host build of the

@@ -134,7 +134,7 @@ def _load():
         "lt_mod_check": ([C.c_uint64, u64p, u64p, u64p], C.c_int),
         "lt_mod_check_device": ([C.c_uint64, vp, vp, vp, vp], C.c_int),
         "lt_host_link_gbs": ([C.c_int, C.POINTER(C.c_double)], C.c_int),
-        "lt_host_gather_gbs": ([C.c_int, C.POINTER(C.c_double)], C.c_int),
+        "lt_host_gather_gbs": ([C.c_int, C.c_uint64, C.POINTER(C.c_double)], C.c_int),
         "lt_ppr_batch": ([vp, C.c_uint32, u32p, u64p, u64p, C.c_float, u64p, u32p, u32p, C.c_uint64], C.c_int),
         "lt_ppr_batch_device": ([vp, C.c_uint32, vp, vp, vp, C.c_float, vp, vp, vp, C.c_uint64, vp], C.c_int),
         "lt_engine_autotune": ([vp], C.c_int),
@@ -188,11 +188,11 @@ def host_link_gbs(device: int = 0) -> float:
     return v.value
 
 
-def host_gather_gbs(device: int = 0) -> float:
-    """Random 32-byte-sector reads from mapped pinned host memory (GB/s of
-    sectors): the ceiling of zero-copy hops."""
+def host_gather_gbs(device: int = 0, nbytes: int = 0) -> float:
+    """Random 32-byte-sector reads from a mapped pinned host buffer of nbytes
+    (0 = 2 GiB), GB/s of sectors: the ceiling of zero-copy hops."""
     v = C.c_double(0)
-    check(lib.lt_host_gather_gbs(device, C.byref(v)))
+    check(lib.lt_host_gather_gbs(device, nbytes, C.byref(v)))
     return v.value
 
 

@@ -39,14 +39,19 @@ __global__ void __launch_bounds__(256) host_gather_kernel(const uint32_t *host, 
 }  // namespace lt
 
 // Random 32-byte-sector read rate from mapped pinned host memory, in GB/s of
-// sectors (best of 5 launches over a 2 GiB buffer, far beyond L2; the column
-// loads of the step kernels, evict-first and not allocated in L1).
-extern "C" lt_status lt_host_gather_gbs(int device, double *gbs)
+// sectors (best of 5 launches over a buffer of `bytes`, 0 = 2 GiB, far beyond
+// L2; the column loads of the step kernels, evict-first and not allocated in
+// L1).  The rate depends on how much host memory the reads spread over (on
+// this machine about 130 GB/s up to 16 GiB, 1-2 GB/s at 32 GiB), which is
+// why zero-copy reads go in bounded groups.
+extern "C" lt_status lt_host_gather_gbs(int device, uint64_t bytes, double *gbs)
 {
     using namespace lt;
     if (!gbs) return fail(LT_ERR_INVALID, "null argument");
     LT_CUDA_TRY(cudaSetDevice(device));
-    const uint64_t bytes = 2ull << 30, n_words = bytes / 4;
+    if (bytes == 0) bytes = 2ull << 30;
+    if (bytes < (64ull << 20)) return fail(LT_ERR_INVALID, "gather probe buffer below 64 MiB");
+    const uint64_t n_words = bytes / 4;
     void *h = nullptr, *hd = nullptr;
     unsigned long long *sink = nullptr;
     LT_CUDA_TRY(cudaHostAlloc(&h, bytes, cudaHostAllocMapped | cudaHostAllocPortable));
@@ -58,7 +63,9 @@ extern "C" lt_status lt_host_gather_gbs(int device, double *gbs)
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
     const unsigned blocks = (unsigned)std::max(1, sms * 8);
-    const uint32_t iters = 64;  // 152 x 8 x 256 threads x 64 x 8 reads = 160 M sectors per launch
+    // 152 x 8 x 256 threads x 16 x 8 reads = 40 M sectors (1.3 GB) per launch:
+    // 10 ms at 130 GB/s, under a second at the slowest rate measured
+    const uint32_t iters = 16;
     double best = 0;
     cudaEvent_t a = nullptr, b = nullptr;
     if (st == LT_OK) {
