@@ -192,6 +192,14 @@ __global__ void __launch_bounds__(kPartBlock, part_min_blocks<APP>()) walk_part_
                     step = c[kChunk + j];
                     idx = c[2 * kChunk + j];
                     qs = c[3 * kChunk + j];
+                    // A walker taken from a queue chunk was counted as
+                    // entering its partition when it was staged there; the
+                    // empty range (2, 1) forces its lookup and marks it as
+                    // not a new entry (counting it again would rank uncached
+                    // partitions by the walkers that queued at them, i.e.
+                    // by the cache state).  (1, 0) is the plain empty range.
+                    cp_nb = 2;
+                    cp_ne = 1;
                     if (a.q_seed) seed = a.q_seed[qs];
                     active = true;
                 } else if (my < total) {
@@ -234,7 +242,7 @@ __global__ void __launch_bounds__(kPartBlock, part_min_blocks<APP>()) walk_part_
             }
             if (need_graph && (cur < cp_nb || cur >= cp_ne)) {
                 const uint32_t p = find_part(off, P, cur);
-                atomicAdd(&visit[p], 1u);
+                if (!(cp_nb == 2 && cp_ne == 1)) atomicAdd(&visit[p], 1u);
                 unsigned long long rp, col = 0;
                 if (p == a.zc_part) {
                     rp = a.zc_rp | 1ull;
@@ -251,6 +259,8 @@ __global__ void __launch_bounds__(kPartBlock, part_min_blocks<APP>()) walk_part_
                 if (rp == 0ull) {
                     emit = true;
                     dest = p;
+                    cp_nb = 1;
+                    cp_ne = 0;
                 } else {
                     cp_nb = off[p];
                     cp_ne = off[p + 1];
