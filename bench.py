@@ -407,7 +407,9 @@ def gb300_ooc(args, cfg):
     # groups of other footprints
     extra = {"learned_sweep": dict(sched=lt.SCHED_LEARNED, zc_group_bytes=1 << 62, sweep_walkers=1 << 62),
              "learned_zc2g": dict(sched=lt.SCHED_LEARNED, zc_group_bytes=2 << 30),
-             "learned_zc8g": dict(sched=lt.SCHED_LEARNED, zc_group_bytes=8 << 30)}
+             "learned_zc8g": dict(sched=lt.SCHED_LEARNED, zc_group_bytes=8 << 30),
+             "learned_noprefill": dict(sched=lt.SCHED_LEARNED, prefill=False),
+             "frequency_noprefill": dict(sched=lt.SCHED_FREQUENCY, prefill=False)}
     if args.variants:
         keep = args.variants.split(",")
         variants = {k: v for k, v in {**variants, **extra}.items() if k in keep}
@@ -460,7 +462,9 @@ def gb300_ooc(args, cfg):
         for name in variants:
             if name == "learned":
                 continue
-            variants[name] = {**variants[name], **shared, **(wave if name in ("batched", "frequency") else {})}
+            variants[name] = {**variants[name], **shared,
+                              **(wave if name.split("_")[0] in ("batched", "frequency", "learned")
+                                 and "host_index" not in name else {})}
     for i in range(args.warmup):
         for name in variants:
             if i == 0 or name == "learned":

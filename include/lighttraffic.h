@@ -117,6 +117,8 @@ typedef struct lt_engine_cfg {
                                         load_factor x zerocopy_threshold (0 = 256 / host bytes per
                                         zero-copy hop: 8 with the device index, 4 without) */
     int bucket_items;                /* walkers per thread of a bucketing tile: 16 (0) or 8 */
+    int no_prefill;                  /* wave runs: 1 = leave a cold cache to fill as walkers arrive
+                                        instead of loading the policy's forecast set at a run's start */
 } lt_engine_cfg;
 
 typedef struct lt_stats {

@@ -51,7 +51,8 @@ class EngineCfg(C.Structure):
                 ("num_device_walkers", C.c_uint64), ("sched", C.c_int), ("pipeline", C.c_int),
                 ("zerocopy_threshold", C.c_uint64), ("seed", C.c_uint64), ("block_size", C.c_int),
                 ("ctas_per_sm", C.c_int), ("resident_index", C.c_int), ("zc_group_bytes", C.c_uint64),
-                ("sweep_walkers", C.c_uint64), ("load_factor", C.c_uint32), ("bucket_items", C.c_int)]
+                ("sweep_walkers", C.c_uint64), ("load_factor", C.c_uint32), ("bucket_items", C.c_int),
+                ("no_prefill", C.c_int)]
 
 
 class BatchTune(C.Structure):
@@ -428,7 +429,7 @@ class Engine:
     def __init__(self, graph: Graph, partitions: int = 0, batch: int = 0, seed: int = 0x5EED5EED,
                  sched: int = SCHED_PLAIN, pipeline: bool = True, zerocopy_threshold=None,
                  device: int = 0, ctas_per_sm: int = 0, resident_index: bool = True, zc_group_bytes: int = 0,
-                 sweep_walkers: int = 0, load_factor: int = 0, bucket_items: int = 0):
+                 sweep_walkers: int = 0, load_factor: int = 0, bucket_items: int = 0, prefill: bool = True):
         cfg = EngineCfg()
         lib.lt_engine_cfg_default(C.byref(cfg))
         cfg.device = device
@@ -445,6 +446,7 @@ class Engine:
         cfg.sweep_walkers = sweep_walkers
         cfg.load_factor = load_factor
         cfg.bucket_items = bucket_items
+        cfg.no_prefill = 0 if prefill else 1
         self.graph = graph
         self._h = C.c_void_p()
         check(lib.lt_engine_create(graph._h, C.byref(cfg), C.byref(self._h)))

@@ -977,7 +977,7 @@ lt_status wave_step(Ooc &o, const RunParams &rp, WaveState &w, bool &done)
         // every free slot at once (the copies overlap this iteration's kernel)
         {
             std::vector<uint32_t> order;
-            if (free_slot(o) >= 0 && o.policy->prefill(v, order)) {
+            if (!e.cfg.no_prefill && free_slot(o) >= 0 && o.policy->prefill(v, order)) {
                 for (uint32_t p : order) {
                     const int32_t slot = free_slot(o);
                     if (slot < 0) break;
