@@ -863,7 +863,8 @@ uint64_t wave_lazy_budget(Ooc &o, uint64_t chunks, uint64_t walkers, uint64_t le
 constexpr uint64_t kSweepWalkers = 1ull << 18;    // about one walker per resident lane
 constexpr double kRefillHorizon = 512.0;          // iterations a refill is credited with at most
 constexpr uint64_t kRefillHold = 128;             // iterations a partition stays before a refill may evict it
-constexpr int kRefillMax = 2;                     // refill swaps started per iteration
+constexpr int kRefillMax = 2;                     // refill swaps started per check
+constexpr uint64_t kRefillEvery = 4;              // iterations between refill checks
 // zero-copy group: estimated host bytes its walkers touch.  Measured on the
 // 2^33-edge graph: 128 MB 1.73 s, 256 MB 1.67 s, 512 MB 1.65 s per run (one
 // kernel over every partition with tens of millions of walkers: 6.9 s)
@@ -1034,7 +1035,8 @@ lt_status wave_step(Ooc &o, const RunParams &rp, WaveState &w, bool &done)
         // over the rest of the run: (rate_in - rate_out) x remaining
         // iterations x bytes per zero-copy hop must pay for the copy eight
         // times over, the victim must have been cached for kRefillHold
-        // iterations, and at most kRefillMax swaps start per iteration --
+        // iterations, and at most kRefillMax swaps start per check (one
+        // every kRefillEvery iterations) --
         // per-iteration forecasts are noisy: a first version (margin 2, no
         // hold, up to 8 swaps per iteration) made 3 000 swaps per c2 run and
         // doubled its host-link bytes, margin 4 with a 64-iteration hold
@@ -1042,7 +1044,8 @@ lt_status wave_step(Ooc &o, const RunParams &rp, WaveState &w, bool &done)
         // estimated from the walkers still to be created (at most
         // kRefillHorizon).  Policies without a forecast (batched) never
         // refill.
-        if (zc_ok && cand.empty() && started < m && free_slot(o) < 0 && n_idle < idle.size() && !o.serve) {
+        if (zc_ok && cand.empty() && started < m && free_slot(o) < 0 && n_idle < idle.size() && !o.serve &&
+            o.iteration % kRefillEvery == 0) {
             uint64_t left = 0;
             for (uint32_t p = 0; p < o.P; p++) left += o.lazy_left[p];
             const double made = (double)rp.W - (double)left;
@@ -1059,12 +1062,19 @@ lt_status wave_step(Ooc &o, const RunParams &rp, WaveState &w, bool &done)
                 for (size_t k = n_idle; k < idle.size(); k++)
                     if (o.iteration >= o.loaded_at[idle[k]] + kRefillHold)
                         out.push_back({o.policy->visit_rate(v, idle[k]), idle[k]});
-                std::sort(in.begin(), in.end(), [](const std::pair<double, uint32_t> &a, const std::pair<double, uint32_t> &b) {
-                    return a.first != b.first ? a.first > b.first : a.second < b.second;
-                });
-                std::sort(out.begin(), out.end(), [](const std::pair<double, uint32_t> &a, const std::pair<double, uint32_t> &b) {
-                    return a.first != b.first ? a.first < b.first : a.second < b.second;
-                });
+                // at most kRefillMax swaps: only the best candidates and the
+                // weakest victims need ordering
+                const size_t kin = std::min<size_t>(kRefillMax, in.size()), kout = std::min<size_t>(kRefillMax, out.size());
+                std::partial_sort(in.begin(), in.begin() + kin, in.end(),
+                                  [](const std::pair<double, uint32_t> &a, const std::pair<double, uint32_t> &b) {
+                                      return a.first != b.first ? a.first > b.first : a.second < b.second;
+                                  });
+                std::partial_sort(out.begin(), out.begin() + kout, out.end(),
+                                  [](const std::pair<double, uint32_t> &a, const std::pair<double, uint32_t> &b) {
+                                      return a.first != b.first ? a.first < b.first : a.second < b.second;
+                                  });
+                in.resize(kin);
+                out.resize(kout);
                 const double hop = (double)zc_bytes_per_hop(o);
                 int swaps = 0;
                 for (size_t k = 0; k < in.size() && k < out.size() && started < m && swaps < kRefillMax; k++) {
