@@ -669,6 +669,15 @@ def gb300_resident(args, cfg):
                                        ctypes.c_float(prob), 0, SEED_WALK, d_cnt.data_ptr(), None, None,
                                        d_scr.data_ptr(), d_st.data_ptr(), stream.cuda_stream))
 
+    # packed layout: row offset and counter of a vertex side by side
+    d_rows = torch.zeros(2 * (V + 1), dtype=torch.int32, device=dev)
+
+    def launch_packed():
+        lt.check(lt.lib.lt_rows_pack(d_rp.data_ptr(), d_rows.data_ptr(), V, stream.cuda_stream))
+        lt.check(lt.lib.lt_walk_device_packed(app, start, d_rows.data_ptr(), d_col.data_ptr(), V, 0, W, length,
+                                              ctypes.c_float(prob), 0, SEED_WALK, None, None, d_scr.data_ptr(),
+                                              d_st.data_ptr(), stream.cuda_stream))
+
     def launch_compact():
         d_cnt32.zero_()
         lt.check(lt.lib.lt_walk_device_compact(app, start, d_rp32.data_ptr(), d_col.data_ptr(), V, 0, W, length,
@@ -703,10 +712,18 @@ def gb300_resident(args, cfg):
     wall0 = time.time()
     std_ms, std_kern, std_st = timed(launch_std)
     std_total = int(d_cnt.sum().item())
+    packed = None
     if compact_ok:
         elapsed_ms, kern_ms, st = timed(launch_compact)
         total = int(d_cnt32.to(torch.int64).sum().item())
         assert (std_st == st).all(), "compact and u64 layouts took different steps"
+        p_ms, p_kern, p_st = timed(launch_packed)
+        assert (p_st == st).all(), "packed and compact layouts took different steps"
+        assert torch.equal(d_rows[1::2][:V].to(torch.int64), d_cnt32.to(torch.int64)), "packed counts differ"
+        packed = {"value": (int(p_st[0]) if app == 1 else int(p_st[1])) * args.steps * ws / (p_ms / 1e3),
+                  "ms_per_step": p_ms / args.steps, "mean_launch_ms": statistics.mean(p_kern),
+                  "note": "lt_walk_device_packed: rows[2v] first edge, rows[2v+1] counter (the pack kernel is "
+                          "inside each timed step: it also clears the counters)"}
     else:
         elapsed_ms, kern_ms, st, total = std_ms, std_kern, std_st, std_total
     updates, moves, tele = (int(x) for x in st)
@@ -758,6 +775,7 @@ def gb300_resident(args, cfg):
         "layout": "compact (u32 row offsets and counters)" if compact_ok else "u64 row offsets and counters",
         "u64_layout": {"value": steps_per_pass * args.steps * ws / (std_ms / 1e3), "ms_per_step": std_ms / args.steps,
                        "mean_launch_ms": statistics.mean(std_kern)},
+        "packed_layout": packed,
         "e2e": {"value": steps_per_pass * ws / e2e_s, "unit": "steps/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": 8 * V, "ms_per_step": e2e_s * 1e3},
         "gpu_launches": args.steps,

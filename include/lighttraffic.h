@@ -328,6 +328,24 @@ lt_status lt_walk_device_compact(int app, int start_mode, const uint32_t *d_rowp
  * on `stream`. */
 lt_status lt_rowptr_narrow(const uint64_t *d_rowptr, uint32_t *d_rowptr32, uint32_t num_nodes, void *stream);
 
+/* lt_walk_device on the packed layout: d_rows = u32[2 (num_nodes + 1)],
+ * d_rows[2v] the first edge of v (edge offsets below 2^32) and d_rows[2v+1]
+ * v's counter (u32, added to; the same u32 overflow rule as
+ * lt_walk_device_compact).  The row offsets an update reads and the counter
+ * it increments share one 32-byte sector, so an update touches one sector
+ * of vertex data instead of two.  Build d_rows with lt_rows_pack (counters
+ * zeroed), read the counters with lt_rows_counts.  Same semantics as
+ * randomWalkKernel (src/WalkManager.h:229-246); the layout has no
+ * counterpart in the reference. */
+lt_status lt_walk_device_packed(int app, int start_mode, uint32_t *d_rows, const uint32_t *d_col, uint32_t num_nodes,
+                                uint32_t source, uint64_t num_walkers, uint32_t length, float prob, uint32_t run,
+                                uint64_t seed, uint32_t *d_endpoints, uint32_t *d_paths, void *d_scratch,
+                                uint64_t *d_stats, void *stream);
+/* d_rows[2i] = d_rowptr[i] (i <= num_nodes), d_rows[2i+1] = 0, on `stream`. */
+lt_status lt_rows_pack(const uint64_t *d_rowptr, uint32_t *d_rows, uint32_t num_nodes, void *stream);
+/* d_counts[v] = d_rows[2v+1] (v < num_nodes), widened to u64, on `stream`. */
+lt_status lt_rows_counts(const uint32_t *d_rows, uint64_t *d_counts, uint32_t num_nodes, void *stream);
+
 /* lt_walk_device without the scratch argument, for callers that cannot
  * allocate device memory: a plugin whose host framework owns every device
  * allocation and hands over only inputs and outputs, or a process whose

@@ -157,6 +157,10 @@ def _load():
         "lt_walk_device_compact": ([C.c_int, C.c_int, vp, vp, C.c_uint32, C.c_uint32, C.c_uint64, C.c_uint32,
                                     C.c_float, C.c_uint32, C.c_uint64, vp, vp, vp, vp, vp, vp], C.c_int),
         "lt_rowptr_narrow": ([vp, vp, C.c_uint32, vp], C.c_int),
+        "lt_walk_device_packed": ([C.c_int, C.c_int, vp, vp, C.c_uint32, C.c_uint32, C.c_uint64, C.c_uint32,
+                                   C.c_float, C.c_uint32, C.c_uint64, vp, vp, vp, vp, vp], C.c_int),
+        "lt_rows_pack": ([vp, vp, C.c_uint32, vp], C.c_int),
+        "lt_rows_counts": ([vp, vp, C.c_uint32, vp], C.c_int),
         "lt_host_alloc": ([C.c_uint64, C.POINTER(vp)], C.c_int),
         "lt_engine_checkpoint": ([vp, C.c_char_p, C.c_uint64, C.c_int], C.c_int),
         "lt_checkpoint_read_info": ([C.c_char_p, C.POINTER(CheckpointInfo)], C.c_int),

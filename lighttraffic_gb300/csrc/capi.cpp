@@ -426,6 +426,25 @@ lt_status lt_walk_device_compact(int app, int start_mode, const uint32_t *d_rowp
                                seed, d_counts32, d_endpoints, d_paths, d_scratch, d_stats, (cudaStream_t)stream, 0);
 }
 
+lt_status lt_walk_device_packed(int app, int start_mode, uint32_t *d_rows, const uint32_t *d_col, uint32_t num_nodes,
+                                uint32_t source, uint64_t num_walkers, uint32_t length, float prob, uint32_t run,
+                                uint64_t seed, uint32_t *d_endpoints, uint32_t *d_paths, void *d_scratch,
+                                uint64_t *d_stats, void *stream)
+{
+    return walk_device_packed(app, start_mode, d_rows, d_col, num_nodes, source, num_walkers, length, prob, run, seed,
+                              d_endpoints, d_paths, d_scratch, d_stats, (cudaStream_t)stream, 0);
+}
+
+lt_status lt_rows_pack(const uint64_t *d_rowptr, uint32_t *d_rows, uint32_t num_nodes, void *stream)
+{
+    return rows_pack(d_rowptr, d_rows, num_nodes, (cudaStream_t)stream);
+}
+
+lt_status lt_rows_counts(const uint32_t *d_rows, uint64_t *d_counts, uint32_t num_nodes, void *stream)
+{
+    return rows_counts(d_rows, d_counts, num_nodes, (cudaStream_t)stream);
+}
+
 lt_status lt_engine_checkpoint(lt_engine *e, const char *path, uint64_t every, int stop)
 {
     if (!e) return fail(LT_ERR_INVALID, "null engine");

@@ -70,14 +70,17 @@ uint64_t count_updates(int app, uint64_t W, uint32_t length)
 lt_status walk_launch(int app, int start, const uint64_t *d_rowptr, const uint32_t *d_rowptr32, const uint32_t *d_col,
                       uint32_t V, uint32_t source, uint64_t W, uint32_t length, float prob, uint32_t run,
                       uint64_t seed, uint64_t *d_counts, uint32_t *d_counts32, uint32_t *d_endpoints,
-                      uint32_t *d_paths, void *d_scratch, uint64_t *d_stats, cudaStream_t st, int ctas_per_sm)
+                      uint32_t *d_paths, void *d_scratch, uint64_t *d_stats, cudaStream_t st, int ctas_per_sm,
+                      uint32_t *d_rows = nullptr)
 {
-    const bool compact = d_rowptr32 != nullptr;
+    const int layout = d_rows ? kLayoutPacked : d_rowptr32 ? kLayoutCompact : kLayoutWide;
     if (app < kPPR || app > kWalk) return fail(LT_ERR_INVALID, "unknown app %d", app);
     if (start < kStartSource || start > kStartPerVertex) return fail(LT_ERR_INVALID, "unknown start mode %d", start);
-    if ((!compact && !d_rowptr) || !d_col || V == 0) return fail(LT_ERR_INVALID, "empty graph");
+    if ((layout == kLayoutWide && !d_rowptr) || !d_col || V == 0) return fail(LT_ERR_INVALID, "empty graph");
     if (!d_scratch) return fail(LT_ERR_INVALID, "scratch buffer is required");
-    if (app != kWalk && !(compact ? (void *)d_counts32 : (void *)d_counts))
+    if (app != kWalk && layout == kLayoutWide && !d_counts)
+        return fail(LT_ERR_INVALID, "counts buffer is required for PPR and PageRank");
+    if (app != kWalk && layout == kLayoutCompact && !d_counts32)
         return fail(LT_ERR_INVALID, "counts buffer is required for PPR and PageRank");
     if (app == kPPR && !(prob > 0.0f && prob <= 1.0f)) return fail(LT_ERR_INVALID, "PPR stop probability must be in (0, 1]");
     if (app != kPPR && length == 0) return fail(LT_ERR_INVALID, "walk length must be positive");
@@ -91,6 +94,7 @@ lt_status walk_launch(int app, int start, const uint64_t *d_rowptr, const uint32
     a.rowptr = d_rowptr;
     a.rowptr32 = d_rowptr32;
     a.counts32 = d_counts32;
+    a.rows = d_rows;
     a.col = d_col;
     a.V = V;
     a.source = source;
@@ -105,8 +109,8 @@ lt_status walk_launch(int app, int start, const uint64_t *d_rowptr, const uint32
     a.next = (uint64_t *)d_scratch;
     a.stats = d_stats;
     LT_CUDA_TRY(cudaMemsetAsync(d_scratch, 0, kScratchBytes, st));
-    const int grid = whole_grid(app, start, device, ctas_per_sm, compact);
-    LT_CUDA_TRY(launch_walk_whole(a, app, start, grid, st, compact));
+    const int grid = whole_grid(app, start, device, ctas_per_sm, layout);
+    LT_CUDA_TRY(launch_walk_whole(a, app, start, grid, st, layout));
     return LT_OK;
 }
 
@@ -132,6 +136,59 @@ lt_status walk_device_compact(int app, int start, const uint32_t *d_rowptr32, co
                     app == kPPR ? "PPR" : "PageRank", (unsigned long long)W);
     return walk_launch(app, start, nullptr, d_rowptr32, d_col, V, source, W, length, prob, run, seed, nullptr,
                        d_counts32, d_endpoints, d_paths, d_scratch, d_stats, st, ctas_per_sm);
+}
+
+lt_status walk_device_packed(int app, int start, uint32_t *d_rows, const uint32_t *d_col, uint32_t V, uint32_t source,
+                             uint64_t W, uint32_t length, float prob, uint32_t run, uint64_t seed,
+                             uint32_t *d_endpoints, uint32_t *d_paths, void *d_scratch, uint64_t *d_stats,
+                             cudaStream_t st, int ctas_per_sm)
+{
+    if (!d_rows) return fail(LT_ERR_INVALID, "empty graph");
+    if (count_updates(app, W, length) >= (1ull << 32))
+        return fail(LT_ERR_INVALID, "%s updates of %llu walkers overflow u32 counters: use lt_walk_device",
+                    app == kPPR ? "PPR" : "PageRank", (unsigned long long)W);
+    return walk_launch(app, start, nullptr, nullptr, d_col, V, source, W, length, prob, run, seed, nullptr, nullptr,
+                       d_endpoints, d_paths, d_scratch, d_stats, st, ctas_per_sm, d_rows);
+}
+
+namespace {
+__global__ void pack_kernel(uint32_t *rows, const uint64_t *rowptr, uint64_t n)
+{
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        rows[2 * i] = (uint32_t)rowptr[i];
+        rows[2 * i + 1] = 0;
+    }
+}
+
+__global__ void rows_counts_kernel(uint64_t *counts, const uint32_t *rows, uint64_t n)
+{
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) counts[i] = rows[2 * i + 1];
+}
+}  // namespace
+
+lt_status rows_pack(const uint64_t *d_rowptr, uint32_t *d_rows, uint32_t V, cudaStream_t st)
+{
+    if (!d_rowptr || !d_rows) return fail(LT_ERR_INVALID, "null buffer");
+    int device = 0, sms = 0;
+    LT_CUDA_TRY(cudaGetDevice(&device));
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+    const uint64_t n = (uint64_t)V + 1;
+    pack_kernel<<<stream_blocks(n, sms), 256, 0, st>>>(d_rows, d_rowptr, n);
+    LT_CUDA_TRY(cudaGetLastError());
+    return LT_OK;
+}
+
+lt_status rows_counts(const uint32_t *d_rows, uint64_t *d_counts, uint32_t V, cudaStream_t st)
+{
+    if (!d_rows || !d_counts) return fail(LT_ERR_INVALID, "null buffer");
+    int device = 0, sms = 0;
+    LT_CUDA_TRY(cudaGetDevice(&device));
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+    rows_counts_kernel<<<stream_blocks(V, sms), 256, 0, st>>>(d_counts, d_rows, V);
+    LT_CUDA_TRY(cudaGetLastError());
+    return LT_OK;
 }
 
 lt_status rowptr_narrow(const uint64_t *d_rowptr, uint32_t *d_rowptr32, uint32_t V, cudaStream_t st)

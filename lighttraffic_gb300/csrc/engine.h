@@ -68,4 +68,10 @@ lt_status walk_device_compact(int app, int start, const uint32_t *d_rowptr32, co
                               uint32_t *d_counts32, uint32_t *d_endpoints, uint32_t *d_paths, void *d_scratch,
                               uint64_t *d_stats, cudaStream_t st, int ctas_per_sm);
 lt_status rowptr_narrow(const uint64_t *d_rowptr, uint32_t *d_rowptr32, uint32_t V, cudaStream_t st);
+lt_status walk_device_packed(int app, int start, uint32_t *d_rows, const uint32_t *d_col, uint32_t V, uint32_t source,
+                             uint64_t W, uint32_t length, float prob, uint32_t run, uint64_t seed,
+                             uint32_t *d_endpoints, uint32_t *d_paths, void *d_scratch, uint64_t *d_stats,
+                             cudaStream_t st, int ctas_per_sm);
+lt_status rows_pack(const uint64_t *d_rowptr, uint32_t *d_rows, uint32_t V, cudaStream_t st);
+lt_status rows_counts(const uint32_t *d_rows, uint64_t *d_counts, uint32_t V, cudaStream_t st);
 }  // namespace lt

@@ -39,11 +39,17 @@ struct Hints {
 __device__ __forceinline__ uint32_t ldg_u32(const uint32_t *p, const Hints &h) { return ld_nc_stream_u32(p, h.stream); }
 
 // first edge and degree of v
-template <bool C>
+template <int L>
 __device__ __forceinline__ void row_range(const WholeArgs &a, uint32_t v, const Hints &h, uint64_t &first,
                                           uint64_t &deg)
 {
-    if (C) {
+    if (L == kLayoutPacked) {
+        // the even words never change during a launch (only the counters
+        // beside them do), so the read-only path serves them
+        const uint32_t f = ld_nc_u32(a.rows + 2ull * v, h.keep);
+        first = f;
+        deg = ld_nc_u32(a.rows + 2ull * v + 2, h.keep) - f;
+    } else if (L == kLayoutCompact) {
         const uint32_t f = ld_nc_u32(a.rowptr32 + v, h.keep);
         first = f;
         deg = ld_nc_u32(a.rowptr32 + v + 1, h.keep) - f;
@@ -53,16 +59,18 @@ __device__ __forceinline__ void row_range(const WholeArgs &a, uint32_t v, const 
     }
 }
 
-template <bool C>
+template <int L>
 __device__ __forceinline__ void count1(const WholeArgs &a, uint32_t v, const Hints &h)
 {
-    if (C)
+    if (L == kLayoutPacked)
+        red_add1_u32(a.rows + 2ull * v + 1, h.keep);
+    else if (L == kLayoutCompact)
         red_add1_u32(a.counts32 + v, h.keep);
     else
         red_add1_u64((unsigned long long *)(a.counts + v), h.keep);
 }
 
-template <int APP, int START, bool C>
+template <int APP, int START, int C>
 __global__ void __launch_bounds__(kWholeBlock) walk_whole_kernel(WholeArgs a)
 {
     const int lane = threadIdx.x & 31;
@@ -188,14 +196,14 @@ __global__ void __launch_bounds__(kWholeBlock) walk_whole_kernel(WholeArgs a)
     }
 }
 
-template <int APP, int START, bool C>
+template <int APP, int START, int C>
 cudaError_t launch_t(const WholeArgs &a, int grid, cudaStream_t st)
 {
     walk_whole_kernel<APP, START, C><<<grid, kWholeBlock, 0, st>>>(a);
     return cudaGetLastError();
 }
 
-template <int APP, bool C>
+template <int APP, int C>
 cudaError_t launch_app(const WholeArgs &a, int start, int grid, cudaStream_t st)
 {
     switch (start) {
@@ -205,7 +213,7 @@ cudaError_t launch_app(const WholeArgs &a, int start, int grid, cudaStream_t st)
     }
 }
 
-template <int APP, int START, bool C>
+template <int APP, int START, int C>
 int occupancy_t()
 {
     int n = 0;
@@ -213,7 +221,7 @@ int occupancy_t()
     return n;
 }
 
-template <bool C>
+template <int C>
 int occupancy_c(int app, int start)
 {
     switch (app * 3 + start) {
@@ -231,30 +239,33 @@ int occupancy_c(int app, int start)
 
 }  // namespace
 
-int whole_grid(int app, int start, int device, int ctas_per_sm, bool compact)
+int whole_grid(int app, int start, int device, int ctas_per_sm, int layout)
 {
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
-    int occ = compact ? occupancy_c<true>(app, start) : occupancy_c<false>(app, start);
+    int occ = layout == kLayoutPacked    ? occupancy_c<kLayoutPacked>(app, start)
+              : layout == kLayoutCompact ? occupancy_c<kLayoutCompact>(app, start)
+                                         : occupancy_c<kLayoutWide>(app, start);
     if (occ < 1) occ = 1;
     if (ctas_per_sm > 0 && ctas_per_sm < occ) occ = ctas_per_sm;
     return sms * occ;
 }
 
-cudaError_t launch_walk_whole(const WholeArgs &a, int app, int start, int grid, cudaStream_t st, bool compact)
+template <int C>
+cudaError_t launch_layout(const WholeArgs &a, int app, int start, int grid, cudaStream_t st)
 {
-    if (compact) {
-        switch (app) {
-        case kPPR: return launch_app<kPPR, true>(a, start, grid, st);
-        case kPageRank: return launch_app<kPageRank, true>(a, start, grid, st);
-        default: return launch_app<kWalk, true>(a, start, grid, st);
-        }
-    }
     switch (app) {
-    case kPPR: return launch_app<kPPR, false>(a, start, grid, st);
-    case kPageRank: return launch_app<kPageRank, false>(a, start, grid, st);
-    default: return launch_app<kWalk, false>(a, start, grid, st);
+    case kPPR: return launch_app<kPPR, C>(a, start, grid, st);
+    case kPageRank: return launch_app<kPageRank, C>(a, start, grid, st);
+    default: return launch_app<kWalk, C>(a, start, grid, st);
     }
+}
+
+cudaError_t launch_walk_whole(const WholeArgs &a, int app, int start, int grid, cudaStream_t st, int layout)
+{
+    if (layout == kLayoutPacked) return launch_layout<kLayoutPacked>(a, app, start, grid, st);
+    if (layout == kLayoutCompact) return launch_layout<kLayoutCompact>(a, app, start, grid, st);
+    return launch_layout<kLayoutWide>(a, app, start, grid, st);
 }
 
 namespace {

@@ -29,10 +29,17 @@ struct WholeArgs {
     // update reuses, so that they stay in L2 against the column stream.
     const uint32_t *rowptr32;
     uint32_t *counts32;
+    // Packed layout (launch with layout kLayoutPacked): rows[2v] = first edge
+    // of v (u32), rows[2v+1] = v's counter (u32).  The row offsets an update
+    // reads and the counter it increments share one 32-byte sector.
+    uint32_t *rows;
 };
 
+enum Layout : int { kLayoutWide = 0, kLayoutCompact = 1, kLayoutPacked = 2 };
+
 // Persistent grid size: SMs x resident CTAs (capped by ctas_per_sm when > 0).
-int whole_grid(int app, int start, int device, int ctas_per_sm, bool compact = false);
-cudaError_t launch_walk_whole(const WholeArgs &a, int app, int start, int grid, cudaStream_t st, bool compact = false);
+int whole_grid(int app, int start, int device, int ctas_per_sm, int layout = kLayoutWide);
+cudaError_t launch_walk_whole(const WholeArgs &a, int app, int start, int grid, cudaStream_t st,
+                              int layout = kLayoutWide);
 
 }  // namespace lt

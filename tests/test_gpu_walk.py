@@ -296,3 +296,47 @@ def test_engine_matches_reference_update_vectors(lt, require_gpu, case):
         else:
             got = list(e.walk(W, length=L, run=case["run0"], start=case["start"], paths=True))
         assert digest(got) == case["outputs"], kw
+
+
+@pytest.mark.parametrize("app,start", [(0, 0), (1, 1), (1, 2), (2, 1)])
+def test_packed_layout_matches_oracle(lt, require_gpu, rmat16, app, start):
+    """lt_walk_device_packed (row offset and counter of a vertex side by side)
+    against the oracle: counts, endpoints and paths bit-exact."""
+    import ctypes
+    import torch
+    rp, col = rmat16
+    V = len(rp) - 1
+    dev = torch.device("cuda:0")
+    d_rp = torch.from_numpy(rp.view(np.int64)).to(dev)
+    d_col = torch.from_numpy(col.view(np.int32)).to(dev)
+    d_rows = torch.empty(2 * (V + 1), dtype=torch.int32, device=dev)
+    d_scr = torch.zeros(lt.lib.lt_walk_scratch_bytes() // 8, dtype=torch.int64, device=dev)
+    d_st = torch.zeros(3, dtype=torch.int64, device=dev)
+    st = torch.cuda.current_stream().cuda_stream
+    W, L = 3 * V + 11, 7
+    paths = app == 2
+    d_ep = torch.zeros(W, dtype=torch.int32, device=dev)
+    d_pa = torch.zeros(W * (L + 1), dtype=torch.int32, device=dev) if paths else None
+    lt.check(lt.lib.lt_rows_pack(d_rp.data_ptr(), d_rows.data_ptr(), V, st))
+    lt.check(lt.lib.lt_walk_device_packed(app, start, d_rows.data_ptr(), d_col.data_ptr(), V, 5, W, L if app else 0,
+                                          ctypes.c_float(0.15 if app == 0 else 0.85), 3, 41, d_ep.data_ptr(),
+                                          d_pa.data_ptr() if paths else None, d_scr.data_ptr(), d_st.data_ptr(), st))
+    d_cnt = torch.zeros(V, dtype=torch.int64, device=dev)
+    lt.check(lt.lib.lt_rows_counts(d_rows.data_ptr(), d_cnt.data_ptr(), V, st))
+    torch.cuda.synchronize()
+    got_ep = d_ep.cpu().numpy().view(np.uint32)
+    if app == 0:
+        want, ep, _ = oracle.walk_batch(oracle.APP_PPR, rp, col, start_mode=0, source=5, walkers=W, prob=0.15, run=3,
+                                        seed=41, endpoints=True)[:3]
+    elif app == 1:
+        want, ep, _, _ = oracle.walk_batch(oracle.APP_PAGERANK, rp, col, start_mode=start, walkers=W, length=L,
+                                           prob=0.85, run=3, seed=41, endpoints=True)
+    else:
+        _, ep, pa, _ = oracle.walk_batch(oracle.APP_WALK, rp, col, start_mode=start, walkers=W, length=L, run=3,
+                                         seed=41, endpoints=True, paths=True)
+        assert (d_pa.cpu().numpy().view(np.uint32) == pa).all()
+    assert (got_ep == ep).all()
+    if app != 2:
+        assert (d_cnt.cpu().numpy().view(np.uint64) == want).all()
+    # the row offsets are untouched by the walk
+    assert (d_rows.cpu().numpy().view(np.uint32)[0::2] == rp.astype(np.uint32)).all()
