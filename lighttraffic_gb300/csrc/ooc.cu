@@ -891,6 +891,19 @@ struct WaveState {
     int stalls = 0;
 };
 
+// Publish every load in flight (the compute stream waits for its copy).
+lt_status publish_all(Ooc &o, WaveState &w)
+{
+    lt_engine &e = *o.e;
+    for (auto &d : w.inflight) {
+        LT_CUDA_TRY(cudaStreamWaitEvent(e.s_compute, d.second, 0));
+        LT_TRY(set_entry(o, d.first, e.s_compute));
+        w.loading[d.first] = 0;
+    }
+    w.inflight.clear();
+    return LT_OK;
+}
+
 // One wave iteration (see wave_run); done = nothing waits and nothing loads.
 lt_status wave_step(Ooc &o, const RunParams &rp, WaveState &w, bool &done)
 {
@@ -922,16 +935,28 @@ lt_status wave_step(Ooc &o, const RunParams &rp, WaveState &w, bool &done)
     auto &loading = w.loading;
     done = false;
     {
-        for (auto &d : inflight) {
-            LT_CUDA_TRY(cudaStreamWaitEvent(e.s_compute, d.second, 0));
-            LT_TRY(set_entry(o, d.first, e.s_compute));
-            loading[d.first] = 0;
+        // publish the loads whose copies have finished; the others stay in
+        // flight (not drained, not evicted) until a later iteration
+        {
+            size_t keep = 0;
+            for (auto &d : inflight) {
+                const cudaError_t q = cudaEventQuery(d.second);
+                if (q == cudaSuccess) {
+                    LT_TRY(set_entry(o, d.first, e.s_compute));
+                    loading[d.first] = 0;
+                } else {
+                    if (q != cudaErrorNotReady) LT_CUDA_TRY(q);
+                    cudaGetLastError();
+                    inflight[keep++] = d;
+                }
+            }
+            inflight.resize(keep);
         }
-        inflight.clear();
         refresh_all(o);
         bool any = false;
         for (uint32_t p = 0; p < o.P && !any; p++) any = o.waiting[p] > 0;
         if (!any) {
+            LT_TRY(publish_all(o, w));
             done = true;
             return LT_OK;
         }
@@ -942,7 +967,7 @@ lt_status wave_step(Ooc &o, const RunParams &rp, WaveState &w, bool &done)
         parts.clear();
         for (uint32_t p = 0; p < o.P; p++) {
             draining[p] = 0;
-            if (o.slot_of[p] < 0) continue;
+            if (o.slot_of[p] < 0 || loading[p]) continue;
             Queue &qp = o.q[p];
             if (!qp.host_chunks.empty()) {
                 const uint64_t room = o.free_chunks.size() > reserve ? o.free_chunks.size() - reserve : 0;
@@ -965,7 +990,7 @@ lt_status wave_step(Ooc &o, const RunParams &rp, WaveState &w, bool &done)
         });
         idle.clear();
         for (uint32_t p = 0; p < o.P; p++)
-            if (o.slot_of[p] >= 0 && !draining[p] && o.waiting[p] == 0) idle.push_back(p);
+            if (o.slot_of[p] >= 0 && !draining[p] && !loading[p] && o.waiting[p] == 0) idle.push_back(p);
         std::vector<double> sc(o.P, 0.0);
         for (uint32_t p : idle) sc[p] = o.policy->cache_score(v, p);
         std::sort(idle.begin(), idle.end(), [&](uint32_t a, uint32_t b) {
@@ -974,22 +999,6 @@ lt_status wave_step(Ooc &o, const RunParams &rp, WaveState &w, bool &done)
         });
         size_t n_idle = 0, started = 0;
         const size_t m = std::max<size_t>(1, o.policy->wave_loads());
-        // cold cache at a run's start: the policy's best partitions go into
-        // every free slot at once (the copies overlap this iteration's kernel)
-        {
-            std::vector<uint32_t> order;
-            if (!e.cfg.no_prefill && free_slot(o) >= 0 && o.policy->prefill(v, order)) {
-                for (uint32_t p : order) {
-                    const int32_t slot = free_slot(o);
-                    if (slot < 0) break;
-                    if (o.slot_of[p] >= 0 || loading[p]) continue;
-                    LT_TRY(start_load(o, p, slot, &inflight));
-                    loading[p] = 1;
-                    o.last_used[p] = o.iteration;
-                    e.stats.prefill_loads++;
-                }
-            }
-        }
         for (uint32_t c : cand) {
             if (started >= m) break;
             int32_t slot = free_slot(o);
@@ -1003,6 +1012,24 @@ lt_status wave_step(Ooc &o, const RunParams &rp, WaveState &w, bool &done)
             loading[c] = 1;
             o.last_used[c] = o.iteration;
             started++;
+        }
+        // cold cache at a run's start: after the loads the waiting walkers
+        // ask for (the source partition first), the policy's best partitions
+        // go into every free slot at once; the copies overlap this and the
+        // following kernels and are published as they land
+        {
+            std::vector<uint32_t> order;
+            if (!e.cfg.no_prefill && free_slot(o) >= 0 && o.policy->prefill(v, order)) {
+                for (uint32_t p : order) {
+                    const int32_t slot = free_slot(o);
+                    if (slot < 0) break;
+                    if (o.slot_of[p] >= 0 || loading[p]) continue;
+                    LT_TRY(start_load(o, p, slot, &inflight));
+                    loading[p] = 1;
+                    o.last_used[p] = o.iteration;
+                    e.stats.prefill_loads++;
+                }
+            }
         }
         // Nothing worth a load but slots are free (light load, e.g. serving
         // from a cold cache): fill them with the partitions scoring highest
@@ -1179,6 +1206,16 @@ lt_status wave_step(Ooc &o, const RunParams &rp, WaveState &w, bool &done)
                 }
             }
             if (lazy_p >= 0) G = wave_lazy_budget(o, chunks, walkers, o.lazy_left[lazy_p]);
+        }
+        if (parts.empty() && G == 0 && started == 0 && !inflight.empty()) {
+            // nothing to compute until a load lands: wait for the oldest one
+            // (copies finish in the order they were issued on the copy stream)
+            o.zc_mask_any = false;
+            LT_CUDA_TRY(cudaEventSynchronize(inflight.front().second));
+            LT_TRY(set_entry(o, inflight.front().first, e.s_compute));
+            loading[inflight.front().first] = 0;
+            inflight.erase(inflight.begin());
+            return LT_OK;
         }
         if (parts.empty() && G == 0 && started == 0) {
             // Nothing readable holds walkers, none can be created and nothing
