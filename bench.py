@@ -411,13 +411,15 @@ def gb300_ooc(args, cfg):
                 "learned_host_index": dict(sched=lt.SCHED_LEARNED, resident_index=False),
                 "plain_host_index": dict(sched=lt.SCHED_PLAIN, resident_index=False)}
     # named only through --variants: wave runs that read every uncached
-    # partition zero-copy in each kernel (no bounded groups), and bounded
-    # groups of other footprints
+    # partition zero-copy in each kernel (no bounded groups), bounded groups
+    # of other footprints, no prefill, and every bucketing pass planned by
+    # the host
     extra = {"learned_sweep": dict(sched=lt.SCHED_LEARNED, zc_group_bytes=1 << 62, sweep_walkers=1 << 62),
              "learned_zc2g": dict(sched=lt.SCHED_LEARNED, zc_group_bytes=2 << 30),
              "learned_zc8g": dict(sched=lt.SCHED_LEARNED, zc_group_bytes=8 << 30),
              "learned_noprefill": dict(sched=lt.SCHED_LEARNED, prefill=False),
-             "frequency_noprefill": dict(sched=lt.SCHED_FREQUENCY, prefill=False)}
+             "frequency_noprefill": dict(sched=lt.SCHED_FREQUENCY, prefill=False),
+             "learned_hostplan": dict(sched=lt.SCHED_LEARNED, host_plan=True)}
     if args.variants:
         keep = args.variants.split(",")
         variants = {k: v for k, v in {**variants, **extra}.items() if k in keep}
@@ -503,7 +505,8 @@ def gb300_ooc(args, cfg):
                      "iterations": st["iterations"], "partition_loads": st["partition_loads"],
                      "refill_loads": st["refill_loads"], "prefill_loads": st["prefill_loads"],
                      "zerocopy_groups": st["zerocopy_groups"], "zerocopy_sweeps": st["zerocopy_sweeps"],
-                     "overlap_computes": st["overlap_computes"], "cache_slots": st["cache_slots"],
+                     "overlap_computes": st["overlap_computes"], "device_plans": st["device_plans"],
+                     "cache_slots": st["cache_slots"],
                      "index_on_device": bool(st["index_on_device"]), "step_s": spread(times[name]),
                      # where one run's time goes (last run): CUDA-event time of
                      # the step kernels on cached queues / zero-copy sets, of
@@ -511,7 +514,10 @@ def gb300_ooc(args, cfg):
                      # time blocked on each iteration's step kernel; wall time
                      "run_ms": {"computing": st["computing_ms"], "zero_copy": st["zerocopy_ms"],
                                 "bucketing": st["bucket_ms"], "graph_loading": st["graph_loading_ms"],
-                                "host_wait": st["host_wait_ms"], "running": st["running_ms"]}}
+                                "host_wait": st["host_wait_ms"], "running": st["running_ms"]},
+                     # host time outside waits, by phase (last run)
+                     "host_ms": {"sched": st["host_sched_ms"], "submit": st["host_submit_ms"],
+                                 "replay": st["host_replay_ms"], "observe": st["host_observe_ms"]}}
         if pstats[name]["name"] in ("learned", "frequency"):
             res[name]["policy"] = pstats[name]
         ps = engines[name].partition_stats()

@@ -116,9 +116,13 @@ typedef struct lt_engine_cfg {
     uint32_t load_factor;            /* wave runs: a partition is loaded once its waiting walkers reach
                                         load_factor x zerocopy_threshold (0 = 256 / host bytes per
                                         zero-copy hop: 8 with the device index, 4 without) */
-    int bucket_items;                /* walkers per thread of a bucketing tile: 16 (0) or 8 */
+    int bucket_items;                /* bucketing tile: 16 (0) = 4096 walkers, 8 = 2048 */
     int no_prefill;                  /* wave runs: 1 = leave a cold cache to fill as walkers arrive
                                         instead of loading the policy's forecast set at a run's start */
+    int host_plan;                   /* out-of-core: 1 = the host plans every bucketing pass after
+                                        reading the step kernel's histogram; 0 (default) = a device
+                                        kernel plans it right behind the step kernel whenever the free
+                                        chunks provably hold every arrival (same queues either way) */
 } lt_engine_cfg;
 
 typedef struct lt_stats {
@@ -161,6 +165,12 @@ typedef struct lt_stats {
                                   the policy's forecast (entries of its previous runs) */
     double bucket_ms;          /* CUDA-event time of the bucketing (scatter) kernels */
     double host_wait_ms;       /* host time blocked waiting for each iteration's step kernel */
+    uint64_t device_plans;     /* bucketing passes planned on the device (the others by the host) */
+    /* host time of the out-of-core loop outside waits, by phase (wave runs): */
+    double host_sched_ms;      /* scheduling decisions before each step kernel */
+    double host_submit_ms;     /* work list, plan inputs and launches of each pass */
+    double host_replay_ms;     /* queue bookkeeping after each histogram read-back */
+    double host_observe_ms;    /* kernel timers and the policy's per-iteration update */
 } lt_stats;
 
 const char *lt_strerror(lt_status s);

@@ -52,7 +52,7 @@ class EngineCfg(C.Structure):
                 ("zerocopy_threshold", C.c_uint64), ("seed", C.c_uint64), ("block_size", C.c_int),
                 ("ctas_per_sm", C.c_int), ("resident_index", C.c_int), ("zc_group_bytes", C.c_uint64),
                 ("sweep_walkers", C.c_uint64), ("load_factor", C.c_uint32), ("bucket_items", C.c_int),
-                ("no_prefill", C.c_int)]
+                ("no_prefill", C.c_int), ("host_plan", C.c_int)]
 
 
 class BatchTune(C.Structure):
@@ -93,7 +93,9 @@ class Stats(C.Structure):
                 ("zerocopy_groups", C.c_uint64), ("zerocopy_sweeps", C.c_uint64),
                 ("cache_slots", C.c_uint64), ("index_on_device", C.c_uint64), ("refill_loads", C.c_uint64),
                 ("prefill_loads", C.c_uint64),
-                ("bucket_ms", C.c_double), ("host_wait_ms", C.c_double)]
+                ("bucket_ms", C.c_double), ("host_wait_ms", C.c_double), ("device_plans", C.c_uint64),
+                ("host_sched_ms", C.c_double), ("host_submit_ms", C.c_double), ("host_replay_ms", C.c_double),
+                ("host_observe_ms", C.c_double)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -433,7 +435,8 @@ class Engine:
     def __init__(self, graph: Graph, partitions: int = 0, batch: int = 0, seed: int = 0x5EED5EED,
                  sched: int = SCHED_PLAIN, pipeline: bool = True, zerocopy_threshold=None,
                  device: int = 0, ctas_per_sm: int = 0, resident_index: bool = True, zc_group_bytes: int = 0,
-                 sweep_walkers: int = 0, load_factor: int = 0, bucket_items: int = 0, prefill: bool = True):
+                 sweep_walkers: int = 0, load_factor: int = 0, bucket_items: int = 0, prefill: bool = True,
+                 host_plan: bool = False):
         cfg = EngineCfg()
         lib.lt_engine_cfg_default(C.byref(cfg))
         cfg.device = device
@@ -451,6 +454,7 @@ class Engine:
         cfg.load_factor = load_factor
         cfg.bucket_items = bucket_items
         cfg.no_prefill = 0 if prefill else 1
+        cfg.host_plan = int(host_plan)
         self.graph = graph
         self._h = C.c_void_p()
         check(lib.lt_engine_create(graph._h, C.byref(cfg), C.byref(self._h)))

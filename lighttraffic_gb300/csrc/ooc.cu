@@ -102,7 +102,7 @@ struct Ooc {
     uint64_t staging_cap = 0;
     uint32_t *d_out = nullptr;      // 5 arrays of staging_cap: cur, step, idx, dest, query
     lt_server *serve = nullptr;  // serving state when queries are being served
-    uint32_t *d_ctl = nullptr;      // hist[P] | visits[P] | pad | out_n (u64) | next (u64)
+    uint32_t *d_ctl = nullptr;      // hist[P] | visits[P] | pad | out_n (u64) | next (u64) | bucket_err (u32) | pad
     uint64_t ctl_words = 0;         // u32 words of d_ctl
     uint32_t *d_planbuf = nullptr;  // cursor[P] | win_off[P] | plan chunks
     uint64_t plan_cap = 0;
@@ -111,11 +111,22 @@ struct Ooc {
     uint64_t work_cap = 0;
     unsigned long long *d_stats = nullptr;
 
-    HostBuf h_ctl;   // pinned mirror of d_ctl's hist + out_n
+    HostBuf h_ctl;   // pinned mirror of d_ctl
     HostBuf h_plan;  // pinned plan block
     HostBuf h_work;  // pinned work list
     // device views of h_plan / h_work (null: not mapped, upload by copy)
     uint8_t *h_plan_dev = nullptr, *h_work_dev = nullptr;
+    // inputs of the device-side plan (tail chunk[P] | tail fill[P] | free
+    // stack), two halves used by alternate passes: a pass's plan kernel may
+    // still be queued while the host writes the next pass's inputs
+    HostBuf h_planin;
+    uint8_t *h_planin_dev = nullptr;
+    uint64_t planin_words = 0;  // words of one half
+    uint64_t plan_passes = 0;
+    cudaEvent_t ev_ctl = nullptr;  // the control block's copy to the host has landed
+    // wave runs: the policy has yet to see the last iteration's histograms;
+    // it does while the next step kernel runs (see observe_due_now)
+    bool observe_due = false;
     std::vector<uint32_t> arrivals, visits;
     // per partition over the current run: walkers entering it, those that
     // entered while it was cached, and step-kernel launches it was cached for
@@ -160,6 +171,9 @@ struct Ooc {
     uint32_t *ctl_visits() { return d_ctl + P; }
     unsigned long long *ctl_out_n() { return (unsigned long long *)(d_ctl + hist_words()); }
     unsigned long long *ctl_next() { return ctl_out_n() + 1; }
+    // set by the bucketing kernel, kept across iterations (not cleared with the rest)
+    uint32_t *ctl_bucket_err() { return d_ctl + hist_words() + 4; }
+    uint32_t cleared_words() const { return hist_words() + 4; }
 };
 
 namespace {
@@ -180,6 +194,9 @@ cudaEvent_t ev_get(Ooc &o)
 void drain_timers(Ooc &o, bool all)
 {
     lt_engine &e = *o.e;
+    // every iteration records a few timers: read them in batches (each read
+    // is a few driver calls), and all of them at the end of a run
+    if (!all && o.timed.size() < 48) return;
     size_t keep = 0;
     for (size_t i = 0; i < o.timed.size(); i++) {
         Ooc::Timed &t = o.timed[i];
@@ -269,6 +286,22 @@ void refresh(Ooc &o, uint32_t p)
 void refresh_all(Ooc &o)
 {
     for (uint32_t p = 0; p < o.P; p++) refresh(o, p);
+}
+
+SchedView view(Ooc &o);
+
+// The timers and the policy's per-iteration update of a wave run, deferred
+// from the end of an iteration to the moment the next step kernel has been
+// submitted, so that they overlap it instead of delaying it: the policy's
+// view then lags one iteration behind the queues.
+void observe_due_now(Ooc &o)
+{
+    if (!o.observe_due) return;
+    o.observe_due = false;
+    const double t0 = now_ms();
+    drain_timers(o, false);
+    o.policy->observe(view(o));
+    o.e->stats.host_observe_ms += now_ms() - t0;
 }
 
 SchedView view(Ooc &o)
@@ -512,6 +545,45 @@ Lazy lazy_of(Ooc &o, const RunParams &rp, int32_t p, uint64_t begin, uint64_t co
 lt_status step_and_bucket_parts(Ooc &o, const RunParams &rp, const std::vector<uint32_t> &parts, int32_t p,
                                 const Lazy &lz, bool zero_copy, std::vector<std::pair<uint32_t, cudaEvent_t>> *deferred);
 
+// Appends h_hist[d] walkers to every destination queue: after the walkers of
+// its open tail chunk, then in new chunks popped from the free stack in
+// destination order (plan_kernel's arithmetic).  With h_cursor given, also
+// writes the pass's plan: per destination its first slot in the window and
+// the window's start in h_chunks.  Returns the plan's length.  The caller
+// has made sure the free stack holds every chunk needed.
+uint64_t plan_windows(Ooc &o, const uint32_t *h_hist, uint32_t *h_cursor, uint32_t *h_win, uint32_t *h_chunks)
+{
+    uint64_t n_plan = 0;
+    for (uint32_t d = 0; d < o.P; d++) {
+        if (h_cursor) h_cursor[d] = h_win[d] = 0;
+        if (!h_hist[d]) continue;
+        Queue &qd = o.q[d];
+        if (qd.dev_chunks.empty() || qd.tail_fill == kChunk) {
+            qd.dev_chunks.push_back(o.free_chunks.back());
+            o.free_chunks.pop_back();
+            qd.tail_fill = 0;
+        }
+        if (h_cursor) {
+            h_win[d] = (uint32_t)n_plan;
+            h_cursor[d] = qd.tail_fill;
+            h_chunks[n_plan] = qd.dev_chunks.back();
+        }
+        n_plan++;
+        const uint64_t tot = (uint64_t)qd.tail_fill + h_hist[d];
+        const uint64_t extra = (tot + kChunk - 1) / kChunk - 1;
+        for (uint64_t k = 0; k < extra; k++) {
+            const uint32_t c = o.free_chunks.back();
+            o.free_chunks.pop_back();
+            qd.dev_chunks.push_back(c);
+            if (h_cursor) h_chunks[n_plan] = c;
+            n_plan++;
+        }
+        qd.tail_fill = (uint32_t)(tot - extra * kChunk);
+        refresh(o, d);
+    }
+    return n_plan;
+}
+
 lt_status step_and_bucket(Ooc &o, const RunParams &rp, int32_t p, const Lazy &lz, bool zero_copy,
                           std::vector<std::pair<uint32_t, cudaEvent_t>> *deferred)
 {
@@ -528,6 +600,7 @@ lt_status step_and_bucket_parts(Ooc &o, const RunParams &rp, const std::vector<u
     const uint64_t G = lz.count;
     lt_engine &e = *o.e;
     lt_graph &g = *o.g;
+    const double t_submit = now_ms();
     Queue *qp = p >= 0 ? &o.q[p] : nullptr;
     uint64_t n_chunk_walkers = 0, nw = 0;
     for (uint32_t x : parts) {
@@ -555,7 +628,52 @@ lt_status step_and_bucket_parts(Ooc &o, const RunParams &rp, const std::vector<u
         LT_TRY(upload(o, o.d_work, o.h_work, o.h_work_dev, h_work, nw));
         if (multi) LT_TRY(upload(o, o.d_work_off, o.h_work, o.h_work_dev, h_woff, 2 * nw));
     }
-    LT_CUDA_TRY(cudaMemsetAsync(o.d_ctl, 0, 4 * o.ctl_words, e.s_compute));
+    // Plan the bucketing pass on the device, right behind the step kernel,
+    // when the free chunks provably hold every arrival: at most n_in walkers
+    // leave, which need at most ceil(n_in / kChunk) chunks plus one per
+    // destination.  The drained chunks go back to the pool first (the plan
+    // may reuse them once the step kernel has read them).  Otherwise the
+    // host plans after reading the histogram (and may spill walkers first).
+    const uint64_t n_in = n_chunk_walkers + G;
+    const uint64_t need_max = (n_in + kChunk - 1) / kChunk + std::min<uint64_t>(o.P, n_in);
+    bool dev_plan = false;
+    if (o.P <= kSmemPartMax && o.h_planin_dev && !e.cfg.host_plan) {
+        uint64_t free_after = o.free_chunks.size();
+        for (uint32_t x : parts) free_after += o.q[x].dev_chunks.size();
+        dev_plan = need_max <= free_after && need_max + o.P <= o.plan_cap;
+    }
+    PlanArgs pa{};
+    if (dev_plan) {
+        for (uint32_t x : parts) {
+            Queue &qx = o.q[x];
+            for (uint32_t c : qx.dev_chunks) o.free_chunks.push_back(c);
+            qx.dev_chunks.clear();
+            qx.tail_fill = 0;
+            refresh(o, x);
+        }
+        const uint64_t half = (o.plan_passes++ & 1) * o.planin_words;
+        uint32_t *h_in = (uint32_t *)o.h_planin.ptr + half;
+        for (uint32_t d = 0; d < o.P; d++) {
+            const Queue &qd = o.q[d];
+            h_in[d] = qd.dev_chunks.empty() ? kNoChunk : qd.dev_chunks.back();
+            h_in[o.P + d] = qd.tail_fill;
+        }
+        const uint64_t n_stack = std::min<uint64_t>(need_max, o.free_chunks.size());
+        for (uint64_t i = 0; i < n_stack; i++) h_in[2ull * o.P + i] = o.free_chunks[o.free_chunks.size() - 1 - i];
+        const uint32_t *d_in = (const uint32_t *)(o.h_planin_dev + 4 * half);
+        pa.hist = o.ctl_hist();
+        pa.tail_chunk = d_in;
+        pa.tail_fill = d_in + o.P;
+        pa.stack = d_in + 2ull * o.P;
+        pa.n_stack = (uint32_t)n_stack;
+        pa.P = o.P;
+        pa.cursor = o.d_planbuf;
+        pa.win_off = o.d_planbuf + o.P;
+        pa.plan_chunks = o.d_planbuf + 2ull * o.P;
+        pa.plan_cap = o.plan_cap;
+        pa.err = o.ctl_bucket_err();
+    }
+    LT_CUDA_TRY(cudaMemsetAsync(o.d_ctl, 0, 4ull * o.cleared_words(), e.s_compute));
 
     StepArgs a{};
     a.t = PartTable{o.d_node_off, o.d_edge_off, o.d_rp, o.d_col, o.P};
@@ -624,18 +742,75 @@ lt_status step_and_bucket_parts(Ooc &o, const RunParams &rp, const std::vector<u
         deferred->clear();
     }
     uint32_t *h_hist = (uint32_t *)o.h_ctl.ptr;
-    LT_CUDA_TRY(cudaMemcpyAsync(h_hist, o.d_ctl, 4ull * o.hist_words() + 8, cudaMemcpyDeviceToHost, e.s_compute));
-    const double w0 = now_ms();
-    LT_CUDA_TRY(cudaStreamSynchronize(e.s_compute));
-    e.stats.host_wait_ms += now_ms() - w0;
+    if (dev_plan) {
+        // the control block goes to the host on the copy-back stream as soon
+        // as the step kernel ends; plan and bucketing follow the kernel on the
+        // compute stream while the host reads it
+        if (!o.ev_ctl) LT_CUDA_TRY(cudaEventCreateWithFlags(&o.ev_ctl, cudaEventDisableTiming));
+        LT_CUDA_TRY(cudaStreamWaitEvent(e.s_copyback, t.b, 0));
+        LT_CUDA_TRY(cudaMemcpyAsync(h_hist, o.d_ctl, 4ull * o.ctl_words, cudaMemcpyDeviceToHost, e.s_copyback));
+        LT_CUDA_TRY(cudaEventRecord(o.ev_ctl, e.s_copyback));
+        ScatterArgs sa{};
+        sa.in_cur = a.out_cur;
+        sa.in_step = a.out_step;
+        sa.in_idx = a.out_idx;
+        sa.in_dest = a.out_dest;
+        sa.in_q = a.out_q;
+        sa.n = n_in;
+        sa.n_dev = o.ctl_out_n();
+        sa.arena = o.d_arena;
+        sa.cursor = pa.cursor;
+        sa.win_off = pa.win_off;
+        sa.plan_chunks = pa.plan_chunks;
+        sa.P = o.P;
+        sa.items = e.cfg.bucket_items;
+        sa.err = o.ctl_bucket_err();
+        Ooc::Timed tb{ev_get(o), ev_get(o), kTBucket};
+        LT_CUDA_TRY(cudaEventRecord(tb.a, e.s_compute));
+        nvtxRangePushA("bucketing");
+        cudaError_t bucketed = launch_plan(pa, e.s_compute);
+        if (bucketed == cudaSuccess) bucketed = launch_scatter(sa, e.device, e.s_compute);
+        nvtxRangePop();
+        LT_CUDA_TRY(bucketed);
+        LT_CUDA_TRY(cudaEventRecord(tb.b, e.s_compute));
+        o.timed.push_back(tb);
+        e.stats.kernel_launches += 2;
+        e.stats.device_plans++;
+        e.stats.host_submit_ms += now_ms() - t_submit;
+        observe_due_now(o);
+        const double w0 = now_ms();
+        LT_CUDA_TRY(cudaEventSynchronize(o.ev_ctl));
+        e.stats.host_wait_ms += now_ms() - w0;
+    } else {
+        LT_CUDA_TRY(cudaMemcpyAsync(h_hist, o.d_ctl, 4ull * o.ctl_words, cudaMemcpyDeviceToHost, e.s_compute));
+        e.stats.host_submit_ms += now_ms() - t_submit;
+        observe_due_now(o);
+        const double w0 = now_ms();
+        LT_CUDA_TRY(cudaStreamSynchronize(e.s_compute));
+        e.stats.host_wait_ms += now_ms() - w0;
+    }
+    const double t_replay = now_ms();
+    struct ReplayTimer {
+        lt_stats &st;
+        double t0;
+        ~ReplayTimer() { st.host_replay_ms += now_ms() - t0; }
+    } replay_timer{e.stats, t_replay};
+    // an earlier bucketing pass read a tile from global memory instead of its
+    // bulk copy (no walker lost, but the copy engine did not answer), or its
+    // device plan did not fit (cannot happen under the bound above)
+    const uint32_t bucket_err = h_hist[o.hist_words() + 4];
+    if (bucket_err & 2u) return fail(LT_ERR_CAPACITY, "bucketing: the device plan ran out of free chunks");
+    if (bucket_err & 1u) return fail(LT_ERR_TIMEOUT, "bucketing: a bulk copy into shared memory did not complete");
     const uint64_t staged = *(const unsigned long long *)(h_hist + o.hist_words());
-    // the drained queues' chunks return to the pool
-    for (uint32_t x : parts) {
-        Queue &qx = o.q[x];
-        for (uint32_t c : qx.dev_chunks) o.free_chunks.push_back(c);
-        qx.dev_chunks.clear();
-        qx.tail_fill = 0;
-        refresh(o, x);
+    if (!dev_plan) {
+        // the drained queues' chunks return to the pool
+        for (uint32_t x : parts) {
+            Queue &qx = o.q[x];
+            for (uint32_t c : qx.dev_chunks) o.free_chunks.push_back(c);
+            qx.dev_chunks.clear();
+            qx.tail_fill = 0;
+            refresh(o, x);
+        }
     }
     if (qp) {
         qp->lazy_next += G;
@@ -651,6 +826,12 @@ lt_status step_and_bucket_parts(Ooc &o, const RunParams &rp, const std::vector<u
     }
     if (staged == 0) return LT_OK;
 
+    if (dev_plan) {
+        // the device planned this pass: the same arithmetic on the host
+        // updates the queues' chunk lists
+        plan_windows(o, h_hist, nullptr, nullptr, nullptr);
+        return LT_OK;
+    }
     // Plan the append of h_hist[d] walkers to each destination queue.
     uint64_t need = 0;
     for (uint32_t d = 0; d < o.P; d++) {
@@ -665,31 +846,7 @@ lt_status step_and_bucket_parts(Ooc &o, const RunParams &rp, const std::vector<u
     uint32_t *h_cursor = (uint32_t *)o.h_plan.ptr;
     uint32_t *h_win = h_cursor + o.P;
     uint32_t *h_chunks = h_win + o.P;
-    uint64_t n_plan = 0;
-    for (uint32_t d = 0; d < o.P; d++) {
-        h_cursor[d] = 0;
-        h_win[d] = 0;
-        if (!h_hist[d]) continue;
-        Queue &qd = o.q[d];
-        if (qd.dev_chunks.empty() || qd.tail_fill == kChunk) {
-            qd.dev_chunks.push_back(o.free_chunks.back());
-            o.free_chunks.pop_back();
-            qd.tail_fill = 0;
-        }
-        h_win[d] = (uint32_t)n_plan;
-        h_cursor[d] = qd.tail_fill;
-        h_chunks[n_plan++] = qd.dev_chunks.back();
-        const uint64_t tot = (uint64_t)qd.tail_fill + h_hist[d];
-        const uint64_t extra = (tot + kChunk - 1) / kChunk - 1;
-        for (uint64_t k = 0; k < extra; k++) {
-            const uint32_t c = o.free_chunks.back();
-            o.free_chunks.pop_back();
-            qd.dev_chunks.push_back(c);
-            h_chunks[n_plan++] = c;
-        }
-        qd.tail_fill = (uint32_t)(tot - extra * kChunk);
-        refresh(o, d);
-    }
+    const uint64_t n_plan = plan_windows(o, h_hist, h_cursor, h_win, h_chunks);
     if (n_plan > o.plan_cap) return fail(LT_ERR_CAPACITY, "plan buffer too small");
     LT_TRY(upload(o, o.d_planbuf, o.h_plan, o.h_plan_dev, h_cursor, 2ull * o.P + n_plan));
     ScatterArgs sa{};
@@ -699,12 +856,14 @@ lt_status step_and_bucket_parts(Ooc &o, const RunParams &rp, const std::vector<u
     sa.in_dest = a.out_dest;
     sa.in_q = a.out_q;
     sa.n = staged;
+    sa.n_dev = nullptr;
     sa.arena = o.d_arena;
     sa.cursor = o.d_planbuf;
     sa.win_off = o.d_planbuf + o.P;
     sa.plan_chunks = o.d_planbuf + 2ull * o.P;
     sa.P = o.P;
     sa.items = e.cfg.bucket_items;
+    sa.err = o.ctl_bucket_err();
     Ooc::Timed tb{ev_get(o), ev_get(o), kTBucket};
     LT_CUDA_TRY(cudaEventRecord(tb.a, e.s_compute));
     nvtxRangePushA("bucketing");
@@ -759,8 +918,13 @@ lt_status ensure_pool(Ooc &o, uint64_t W)
     LT_TRY(dalloc(&o.d_work_off, o.work_cap));
     LT_TRY(host_alloc(o.h_plan, 4 * (2ull * o.P + o.plan_cap), true));
     LT_TRY(host_alloc(o.h_work, 12 * o.work_cap + 8, true));
-    o.h_plan_dev = o.h_work_dev = nullptr;
+    host_free(o.h_planin);
+    o.planin_words = 2ull * o.P + o.n_chunks;
+    LT_TRY(host_alloc(o.h_planin, 2 * 4 * o.planin_words, true));
+    o.h_plan_dev = o.h_work_dev = o.h_planin_dev = nullptr;
     void *dv = nullptr;
+    if (o.h_planin.pinned && cudaHostGetDevicePointer(&dv, o.h_planin.ptr, 0) == cudaSuccess)
+        o.h_planin_dev = (uint8_t *)dv;
     if (o.h_plan.pinned && cudaHostGetDevicePointer(&dv, o.h_plan.ptr, 0) == cudaSuccess) o.h_plan_dev = (uint8_t *)dv;
     if (o.h_work.pinned && cudaHostGetDevicePointer(&dv, o.h_work.ptr, 0) == cudaSuccess) o.h_work_dev = (uint8_t *)dv;
     cudaGetLastError();
@@ -884,9 +1048,10 @@ constexpr uint64_t kZcGroupBytesServe = 128ull << 20;
 // read zero-copy in one kernel (the final phase).  Results are those of the
 // reference loop: every draw is keyed by walker and step.
 struct WaveState {
-    explicit WaveState(uint32_t P) : draining(P, 0), loading(P, 0) {}
+    explicit WaveState(uint32_t P) : score(P, 0.0), draining(P, 0), loading(P, 0) {}
     std::vector<std::pair<uint32_t, cudaEvent_t>> inflight;  // loads started, entries not yet published
     std::vector<uint32_t> parts, cand, idle;
+    std::vector<double> score;  // victims' cache scores
     std::vector<char> draining, loading;
     int stalls = 0;
 };
@@ -908,6 +1073,7 @@ lt_status publish_all(Ooc &o, WaveState &w)
 lt_status wave_step(Ooc &o, const RunParams &rp, WaveState &w, bool &done)
 {
     lt_engine &e = *o.e;
+    const double t_sched = now_ms();
     const bool zc_ok = o.zc_rp_base != 0 && o.P <= kSmemPartMax && o.zc_threshold > 0;
     // A wave loads a partition once its waiting walkers would read more host
     // bytes zero-copy than the load copies.  The reference's threshold
@@ -957,6 +1123,7 @@ lt_status wave_step(Ooc &o, const RunParams &rp, WaveState &w, bool &done)
         for (uint32_t p = 0; p < o.P && !any; p++) any = o.waiting[p] > 0;
         if (!any) {
             LT_TRY(publish_all(o, w));
+            observe_due_now(o);
             done = true;
             return LT_OK;
         }
@@ -988,21 +1155,29 @@ lt_status wave_step(Ooc &o, const RunParams &rp, WaveState &w, bool &done)
         std::sort(cand.begin(), cand.end(), [&](uint32_t a, uint32_t b) {
             return o.waiting[a] != o.waiting[b] ? o.waiting[a] > o.waiting[b] : a < b;
         });
-        idle.clear();
-        for (uint32_t p = 0; p < o.P; p++)
-            if (o.slot_of[p] >= 0 && !draining[p] && !loading[p] && o.waiting[p] == 0) idle.push_back(p);
-        std::vector<double> sc(o.P, 0.0);
-        for (uint32_t p : idle) sc[p] = o.policy->cache_score(v, p);
-        std::sort(idle.begin(), idle.end(), [&](uint32_t a, uint32_t b) {
-            if (sc[a] != sc[b]) return sc[a] < sc[b];
-            return o.last_used[a] != o.last_used[b] ? o.last_used[a] < o.last_used[b] : a < b;
-        });
+        // victims in eviction order (lowest cache score first), ordered only
+        // when an eviction is considered: most iterations start no load
+        bool idle_ready = false;
+        auto order_idle = [&]() {
+            if (idle_ready) return;
+            idle_ready = true;
+            idle.clear();
+            for (uint32_t p = 0; p < o.P; p++)
+                if (o.slot_of[p] >= 0 && !draining[p] && !loading[p] && o.waiting[p] == 0) idle.push_back(p);
+            std::vector<double> &sc = w.score;
+            for (uint32_t p : idle) sc[p] = o.policy->cache_score(v, p);
+            std::sort(idle.begin(), idle.end(), [&](uint32_t a, uint32_t b) {
+                if (sc[a] != sc[b]) return sc[a] < sc[b];
+                return o.last_used[a] != o.last_used[b] ? o.last_used[a] < o.last_used[b] : a < b;
+            });
+        };
         size_t n_idle = 0, started = 0;
         const size_t m = std::max<size_t>(1, o.policy->wave_loads());
         for (uint32_t c : cand) {
             if (started >= m) break;
             int32_t slot = free_slot(o);
             if (slot < 0) {
+                order_idle();
                 if (n_idle >= idle.size()) break;
                 const uint32_t w = idle[n_idle++];
                 slot = o.slot_of[w];
@@ -1071,8 +1246,8 @@ lt_status wave_step(Ooc &o, const RunParams &rp, WaveState &w, bool &done)
         // estimated from the walkers still to be created (at most
         // kRefillHorizon).  Policies without a forecast (batched) never
         // refill.
-        if (zc_ok && cand.empty() && started < m && free_slot(o) < 0 && n_idle < idle.size() && !o.serve &&
-            o.iteration % kRefillEvery == 0) {
+        if (zc_ok && cand.empty() && started < m && !o.serve && o.iteration % kRefillEvery == 0 &&
+            free_slot(o) < 0 && (order_idle(), n_idle < idle.size())) {
             uint64_t left = 0;
             for (uint32_t p = 0; p < o.P; p++) left += o.lazy_left[p];
             const double made = (double)rp.W - (double)left;
@@ -1166,19 +1341,28 @@ lt_status wave_step(Ooc &o, const RunParams &rp, WaveState &w, bool &done)
                 }
             const bool sweep = outside <= sweep_walkers;
             if (!sweep) {
-                std::sort(group.begin(), group.end(), [&](uint32_t a, uint32_t b) {
+                auto more = [&](uint32_t a, uint32_t b) {
                     return o.waiting[a] != o.waiting[b] ? o.waiting[a] > o.waiting[b] : a < b;
-                });
+                };
                 // host bytes a partition's walkers touch: at most the partition,
                 // else about two 128-byte lines per hop (one with the index
                 // resident), two hops per walker
                 auto footprint = [&](uint32_t p) {
                     return std::min<uint64_t>(host_part_bytes(o, p), (o.d_index ? 256 : 512) * o.waiting[p]);
                 };
+                // most waiting walkers first; a group holds few partitions,
+                // so only a prefix is ordered (64 at a time)
                 uint64_t bytes = 0;
-                size_t n = 0;
-                while (n < group.size() && (n == 0 || bytes + footprint(group[n]) <= zc_group_bytes))
+                size_t n = 0, sorted = 0;
+                while (n < group.size()) {
+                    if (n == sorted) {
+                        const size_t k = std::min<size_t>(group.size(), sorted + 64);
+                        std::partial_sort(group.begin() + sorted, group.begin() + k, group.end(), more);
+                        sorted = k;
+                    }
+                    if (n > 0 && bytes + footprint(group[n]) > zc_group_bytes) break;
                     bytes += footprint(group[n++]);
+                }
                 group.resize(n);
             } else {
                 group.clear();
@@ -1230,10 +1414,10 @@ lt_status wave_step(Ooc &o, const RunParams &rp, WaveState &w, bool &done)
         }
         w.stalls = 0;
         const Lazy lz = lazy_p >= 0 ? lazy_of(o, rp, lazy_p, o.q[lazy_p].lazy_next, G) : Lazy{};
+        e.stats.host_sched_ms += now_ms() - t_sched;
         LT_TRY(step_and_bucket_parts(o, rp, parts, lazy_p, lz, false, nullptr));
         o.zc_mask_any = false;
-        drain_timers(o, false);
-        o.policy->observe(view(o));
+        o.observe_due = true;
     }
     return LT_OK;
 }
@@ -1250,6 +1434,7 @@ lt_status wave_run(Ooc &o, const RunParams &rp, bool &stop)
         if (done) break;
         LT_TRY(ckpt_point(o, rp, stop));
         if (stop) {
+            observe_due_now(o);
             // leave the cache consistent: loads in flight land and are published
             lt_engine &e = *o.e;
             for (auto &d : w.inflight) {
@@ -1274,7 +1459,7 @@ lt_status ooc_create(lt_engine *e, Ooc **out)
     o->P = g.P();
     o->K = std::min<uint32_t>(e->cfg.num_device_partitions, o->P);
     if (o->K < 1) o->K = 1;
-    o->ctl_words = o->hist_words() + 4;
+    o->ctl_words = o->hist_words() + 6;
     auto bail = [&](lt_status s) {
         ooc_destroy(o);
         return s;
@@ -1329,7 +1514,8 @@ lt_status ooc_create(lt_engine *e, Ooc **out)
     if (s != LT_OK) return bail(s);
     if (cudaMemcpy(o->d_node_off, g.node_off.data(), 4ull * (o->P + 1), cudaMemcpyHostToDevice) != cudaSuccess ||
         cudaMemcpy(o->d_edge_off, g.edge_off.data(), 8ull * (o->P + 1), cudaMemcpyHostToDevice) != cudaSuccess ||
-        cudaMemset(o->d_rp, 0, 8ull * o->P) != cudaSuccess || cudaMemset(o->d_col, 0, 8ull * o->P) != cudaSuccess)
+        cudaMemset(o->d_rp, 0, 8ull * o->P) != cudaSuccess || cudaMemset(o->d_col, 0, 8ull * o->P) != cudaSuccess ||
+        cudaMemset(o->d_ctl, 0, 4ull * o->ctl_words) != cudaSuccess)
         return bail(fail(LT_ERR_CUDA, "partition table upload failed"));
     o->slot_of.assign(o->P, -1);
     o->part_in_slot.assign(o->K, -1);
@@ -1388,6 +1574,8 @@ void ooc_destroy(Ooc *o)
     host_free(o->h_ctl);
     host_free(o->h_plan);
     host_free(o->h_work);
+    host_free(o->h_planin);
+    if (o->ev_ctl) cudaEventDestroy(o->ev_ctl);
     for (cudaEvent_t ev : o->ev_free) cudaEventDestroy(ev);
     delete o;
 }

@@ -13,9 +13,12 @@ constexpr int kScanTile = kScanBlock * kScanItems;
 
 namespace scan_detail {
 
-template <typename T>
+// Exclusive prefix sum of one value per thread over a block of BLOCK threads
+// (a multiple of 32, at most 1024); *total receives the block's sum.
+template <typename T, int BLOCK = kScanBlock>
 __device__ __forceinline__ T block_exclusive(T v, T *warp_tot, T *total)
 {
+    static_assert(BLOCK % 32 == 0 && BLOCK <= 1024, "block of whole warps, at most 1024 threads");
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     T incl = v;
 #pragma unroll
@@ -26,15 +29,15 @@ __device__ __forceinline__ T block_exclusive(T v, T *warp_tot, T *total)
     if (lane == 31) warp_tot[wid] = incl;
     __syncthreads();
     if (wid == 0) {
-        T w = lane < kScanBlock / 32 ? warp_tot[lane] : T(0);
+        T w = lane < BLOCK / 32 ? warp_tot[lane] : T(0);
         T wi = w;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
             const T n = __shfl_up_sync(0xFFFFFFFFu, wi, o);
             if (lane >= o) wi += n;
         }
-        if (lane < kScanBlock / 32) warp_tot[lane] = wi - w;
-        if (lane == kScanBlock / 32 - 1) *total = wi;
+        if (lane < BLOCK / 32) warp_tot[lane] = wi - w;
+        if (lane == BLOCK / 32 - 1) *total = wi;
     }
     __syncthreads();
     const T r = incl - v + warp_tot[wid];

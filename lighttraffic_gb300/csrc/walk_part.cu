@@ -447,98 +447,232 @@ __global__ void __launch_bounds__(kPartBlock) scatter_kernel(ScatterArgs a)
 }
 
 // Bucketing by a block-local counting sort (P <= kSmemPartMax).  A tile of
-// kBucketTile staged walkers is ranked per destination in shared memory
-// (shared atomics), the per-destination counts are scanned across the block
-// and reserved in the destination windows with one global atomic per
+// T = kPartBlock x ITEMS staged walkers is ranked per destination in shared
+// memory (shared atomics), the per-destination counts are scanned across the
+// block and reserved in the destination windows with one global atomic per
 // (tile, destination) -- the two-level scheme of insertToQueueKernel
-// (src/WalkManager.h:122-190) -- and the walkers are laid out sorted by
-// destination in shared memory, so that the write-back is a sequence of
-// per-destination runs: consecutive threads write consecutive queue slots.
-// The plain scatter above wrote each walker with four isolated 4-byte stores
-// and made one global atomic per (1024-walker tile, destination), i.e.
-// nearly one per walker when the walkers spread over ~1000 partitions.
-// The tile is kPartBlock x ITEMS walkers (ITEMS 16: 4096, the default; 8:
-// 2048, chosen by the autotuner when it is faster).
-constexpr int kBucketFields = 5;  // cur, step, idx, query, dest
+// (src/WalkManager.h:122-190) -- and the tile is written back through its
+// sort permutation as per-destination runs: consecutive threads write
+// consecutive queue slots.
+//
+// The CTAs are persistent and double-buffered: while a tile is sorted, the
+// bulk-copy unit (cp.async.bulk, one copy per field, completion counted on an
+// mbarrier) brings the CTA's next tile from the staging area into shared
+// memory, so the kernel issues no global loads of walker fields.  A tile's
+// chunk ids are looked up once per destination, not per walker.  The staged
+// field arrays start 16-byte aligned and hold n rounded up to 4 words (the
+// copies round up to 16 bytes).  If a copy does not complete within a second,
+// the CTA records it in *err and reads the remaining tiles from global memory
+// directly, so no walker is lost.
+// Two shapes, chosen by the autotuner: 1024 threads x 4 walkers (T = 4096,
+// the default; one CTA per SM) and 512 threads x 4 walkers (T = 2048; two
+// CTAs per SM, so that one CTA's barrier waits overlap the other's work).
+// Every phase of a tile ends at a block barrier; 256-thread CTAs of a
+// 4096-walker tile left 8 warps per SM to hide the latencies.
+constexpr int kBucketFields = 5;                    // cur, step, idx, query, dest
+constexpr uint64_t kBulkWaitNs = 1000000000ull;     // bounded wait on one tile's copies
 
-template <int ITEMS>
+template <int BLOCK, int ITEMS>
 size_t bucket_smem(uint32_t P)
 {
-    return sizeof(uint32_t) * (2ull * P + (uint64_t)kBucketFields * kPartBlock * ITEMS);
+    const uint64_t T = (uint64_t)BLOCK * ITEMS;
+    // two tiles of kBucketFields u32 fields | 2 mbarriers | 4 u32 per destination | u16 permutation
+    return 4 * 2 * kBucketFields * T + 16 + 16ull * P + 2 * T;
 }
 
-template <int ITEMS>
-__global__ void __launch_bounds__(kPartBlock, 2) bucket_sort_kernel(ScatterArgs a)
+template <int BLOCK, int ITEMS>
+__global__ void __launch_bounds__(BLOCK, 1024 / BLOCK) bucket_sort_kernel(ScatterArgs a)
 {
-    constexpr int kBucketItems = ITEMS;
-    constexpr int kBucketTile = kPartBlock * ITEMS;
-    extern __shared__ uint32_t smem[];
-    __shared__ uint32_t warp_tot[kPartBlock / 32];
+    constexpr uint32_t T = BLOCK * ITEMS;
+    constexpr uint32_t kPerMax = kSmemPartMax / BLOCK;
+    extern __shared__ __align__(16) uint32_t smem[];
+    __shared__ uint32_t warp_tot[BLOCK / 32];
     __shared__ uint32_t tile_total;
     const uint32_t P = a.P;
-    uint32_t *s_cnt = smem;       // P: walkers of the tile per destination, then their offsets in the sorted tile
-    uint32_t *s_base = smem + P;  // P: first reserved slot of the destination's window
-    uint32_t *s_cur = s_base + P;
-    uint32_t *s_step = s_cur + kBucketTile;
-    uint32_t *s_idx = s_step + kBucketTile;
-    uint32_t *s_q = s_idx + kBucketTile;
-    uint32_t *s_dest = s_q + kBucketTile;
-    const uint32_t per = (P + kPartBlock - 1) / kPartBlock;  // destinations a thread reserves and scans
-    for (uint64_t t0 = (uint64_t)blockIdx.x * kBucketTile; t0 < a.n; t0 += (uint64_t)gridDim.x * kBucketTile) {
-        for (uint32_t i = threadIdx.x; i < P; i += blockDim.x) s_cnt[i] = 0;
-        __syncthreads();
-        uint32_t dest[kBucketItems], rank[kBucketItems];
+    uint64_t *mbar = reinterpret_cast<uint64_t *>(smem + 2 * kBucketFields * T);
+    uint32_t *s_off = reinterpret_cast<uint32_t *>(mbar + 2);  // P: tile count, then offset in the sorted tile
+    uint32_t *s_base = s_off + P;                              // P: first reserved slot of the window
+    uint32_t *s_ch0 = s_base + P;                              // P: chunk holding s_base
+    uint32_t *s_ch1 = s_ch0 + P;                               // P: the next chunk, where the run crosses into it
+    uint16_t *s_inv = reinterpret_cast<uint16_t *>(s_ch1 + P); // T: tile position at sorted position j
+    const uint32_t *src[kBucketFields] = {a.in_cur, a.in_step, a.in_idx, a.in_q, a.in_dest};
+    if (a.err && (*(volatile unsigned int *)a.err & 2u)) return;
+    const uint64_t n = a.n_dev ? *a.n_dev : a.n;
+    const uint64_t tiles = (n + T - 1) / T;
+    bool bulk = true;
 #pragma unroll
-        for (int k = 0; k < kBucketItems; k++) {
-            const uint64_t i = t0 + (uint64_t)k * kPartBlock + threadIdx.x;
-            dest[k] = i < a.n ? a.in_dest[i] : 0xFFFFFFFFu;
-            rank[k] = dest[k] != 0xFFFFFFFFu ? atomicAdd(&s_cnt[dest[k]], 1u) : 0u;
+    for (int f = 0; f < kBucketFields; f++) bulk = bulk && ((uintptr_t)src[f] & 15) == 0;
+    if (threadIdx.x == 0) {
+        mbar_init(&mbar[0], 1);
+        mbar_init(&mbar[1], 1);
+        mbar_init_fence();
+    }
+    __syncthreads();
+    // thread 0: copies of tile `tile` into buffer b
+    auto issue = [&](uint64_t tile, int b) {
+        const uint64_t t0 = tile * T;
+        const uint32_t m = (uint32_t)(n - t0 < T ? n - t0 : T);
+        const uint32_t bytes = (4 * m + 15) & ~15u;
+        mbar_arrive_expect_tx(&mbar[b], kBucketFields * bytes);
+#pragma unroll
+        for (int f = 0; f < kBucketFields; f++) bulk_load_smem(smem + (b * kBucketFields + f) * T, src[f] + t0, bytes, &mbar[b]);
+    };
+    // copies issued into / completions waited for on buffer 0 and buffer 1
+    uint32_t issued0 = 0, issued1 = 0, waited0 = 0, waited1 = 0;
+    uint64_t tile = blockIdx.x;
+    if (bulk && tile < tiles) {
+        if (threadIdx.x == 0) issue(tile, 0);
+        issued0++;
+    }
+    const uint32_t per = (P + BLOCK - 1) / BLOCK;  // destinations a thread reserves and scans
+    for (uint32_t it = 0; tile < tiles; tile += gridDim.x, it++) {
+        const int b = it & 1;
+        const uint64_t t0 = tile * T;
+        const uint32_t m = (uint32_t)(n - t0 < T ? n - t0 : T);
+        if (bulk && tile + gridDim.x < tiles) {
+            // buffer b^1 was last read by the previous tile, which ended at a barrier
+            if (threadIdx.x == 0) issue(tile + gridDim.x, b ^ 1);
+            if (b) issued0++;
+            else issued1++;
+        }
+        for (uint32_t i = threadIdx.x; i < P; i += BLOCK) s_off[i] = 0;
+        if (bulk) {
+            const bool ok = mbar_wait_bounded(&mbar[b], (b ? waited1 : waited0) & 1, kBulkWaitNs);
+            if (ok) {
+                if (b) waited1++;
+                else waited0++;
+            }
+            if (__syncthreads_or(!ok)) {
+                if (threadIdx.x == 0 && a.err) atomicOr(a.err, 1u);
+                bulk = false;
+            }
+        } else {
+            __syncthreads();
+        }
+        const uint32_t *f_cur, *f_step, *f_idx, *f_q, *f_dest;
+        if (bulk) {
+            const uint32_t *buf = smem + b * kBucketFields * T;
+            f_cur = buf, f_step = buf + T, f_idx = buf + 2 * T, f_q = buf + 3 * T, f_dest = buf + 4 * T;
+        } else {
+            f_cur = a.in_cur + t0, f_step = a.in_step + t0, f_idx = a.in_idx + t0, f_q = a.in_q + t0,
+            f_dest = a.in_dest + t0;
+        }
+        uint32_t dest[ITEMS], rank[ITEMS];
+#pragma unroll
+        for (int k = 0; k < ITEMS; k++) {
+            const uint32_t i = k * BLOCK + threadIdx.x;
+            dest[k] = i < m ? f_dest[i] : 0xFFFFFFFFu;
+            rank[k] = dest[k] != 0xFFFFFFFFu ? atomicAdd(&s_off[dest[k]], 1u) : 0u;
         }
         __syncthreads();
+        // reserve each destination's run: window starts and atomics first,
+        // then the chunk lookups that depend on both
+        uint32_t cnt[kPerMax], base[kPerMax], win[kPerMax];
         uint32_t mine = 0;
-        for (uint32_t j = 0; j < per; j++) {
+#pragma unroll
+        for (uint32_t j = 0; j < kPerMax; j++) {
             const uint32_t d = threadIdx.x * per + j;
-            if (d < P) {
-                const uint32_t c = s_cnt[d];
-                if (c) s_base[d] = atomicAdd(&a.cursor[d], c);
-                mine += c;
-            }
+            cnt[j] = j < per && d < P ? s_off[d] : 0;
+            win[j] = cnt[j] ? a.win_off[d] : 0;
         }
-        uint32_t off = scan_detail::block_exclusive<uint32_t>(mine, warp_tot, &tile_total);
-        for (uint32_t j = 0; j < per; j++) {
+#pragma unroll
+        for (uint32_t j = 0; j < kPerMax; j++) {
             const uint32_t d = threadIdx.x * per + j;
-            if (d < P) {
-                const uint32_t c = s_cnt[d];
-                s_cnt[d] = off;
-                off += c;
+            base[j] = cnt[j] ? atomicAdd(&a.cursor[d], cnt[j]) : 0;
+            mine += cnt[j];
+        }
+#pragma unroll
+        for (uint32_t j = 0; j < kPerMax; j++) {
+            if (!cnt[j]) continue;
+            const uint32_t d = threadIdx.x * per + j;
+            const uint32_t w = win[j] + base[j] / kChunk;
+            s_base[d] = base[j];
+            s_ch0[d] = a.plan_chunks[w];
+            // a run (at most T < kChunk walkers) spans one chunk or two
+            s_ch1[d] = (base[j] + cnt[j] - 1) / kChunk != base[j] / kChunk ? a.plan_chunks[w + 1] : 0u;
+        }
+        uint32_t off = scan_detail::block_exclusive<uint32_t, BLOCK>(mine, warp_tot, &tile_total);
+#pragma unroll
+        for (uint32_t j = 0; j < kPerMax; j++) {
+            const uint32_t d = threadIdx.x * per + j;
+            if (j < per && d < P) {
+                s_off[d] = off;
+                off += cnt[j];
             }
         }
         __syncthreads();
 #pragma unroll
-        for (int k = 0; k < kBucketItems; k++) {
-            if (dest[k] == 0xFFFFFFFFu) continue;
-            const uint64_t i = t0 + (uint64_t)k * kPartBlock + threadIdx.x;
-            const uint32_t pos = s_cnt[dest[k]] + rank[k];
-            s_cur[pos] = a.in_cur[i];
-            s_step[pos] = a.in_step[i];
-            s_idx[pos] = a.in_idx[i];
-            s_q[pos] = a.in_q[i];
-            s_dest[pos] = dest[k];
-        }
+        for (int k = 0; k < ITEMS; k++)
+            if (dest[k] != 0xFFFFFFFFu) s_inv[s_off[dest[k]] + rank[k]] = (uint16_t)(k * BLOCK + threadIdx.x);
         __syncthreads();
-        const uint32_t m = (uint32_t)min((uint64_t)kBucketTile, a.n - t0);
-        for (uint32_t j = threadIdx.x; j < m; j += blockDim.x) {
-            const uint32_t d = s_dest[j];
-            const uint32_t g = s_base[d] + (j - s_cnt[d]);
-            const uint32_t chunk = a.plan_chunks[a.win_off[d] + g / kChunk];
+        for (uint32_t j = threadIdx.x; j < m; j += BLOCK) {
+            const uint32_t i = s_inv[j];
+            const uint32_t d = f_dest[i];
+            const uint32_t b0 = s_base[d];
+            const uint32_t g = b0 + (j - s_off[d]);
+            const uint32_t chunk = g / kChunk == b0 / kChunk ? s_ch0[d] : s_ch1[d];
             uint32_t *c = reinterpret_cast<uint32_t *>(a.arena + (uint64_t)chunk * kChunkBytes);
             const uint32_t jj = g % kChunk;
-            c[jj] = s_cur[j];
-            c[kChunk + jj] = s_step[j];
-            c[2 * kChunk + jj] = s_idx[j];
-            c[3 * kChunk + jj] = s_q[j];
+            c[jj] = f_cur[i];
+            c[kChunk + jj] = f_step[i];
+            c[2 * kChunk + jj] = f_idx[i];
+            c[3 * kChunk + jj] = f_q[i];
         }
         __syncthreads();
+    }
+    // copies still in flight exist only after a wait gave up: wait for them
+    // (bounded) before this CTA's shared memory is released
+    while (waited0 < issued0 && mbar_wait_bounded(&mbar[0], waited0 & 1, kBulkWaitNs)) waited0++;
+    while (waited1 < issued1 && mbar_wait_bounded(&mbar[1], waited1 & 1, kBulkWaitNs)) waited1++;
+}
+
+// One CTA plans every destination: per destination the chunks its arrivals
+// need (new ones and, with an open tail chunk, that one), two block scans for
+// the stack and window positions, then the windows in destination order.
+constexpr int kPlanBlock = 1024;
+
+__global__ void __launch_bounds__(kPlanBlock) plan_kernel(PlanArgs a)
+{
+    constexpr uint32_t kPerMax = kSmemPartMax / kPlanBlock;
+    __shared__ uint32_t warp_tot[kPlanBlock / 32];
+    __shared__ uint32_t tot_new, tot_slots;
+    const uint32_t P = a.P;
+    const uint32_t per = (P + kPlanBlock - 1) / kPlanBlock;
+    uint32_t h[kPerMax], fill[kPerMax], tail[kPerMax], nnew[kPerMax];
+    uint32_t my_new = 0, my_slots = 0;
+#pragma unroll
+    for (uint32_t j = 0; j < kPerMax; j++) {
+        const uint32_t d = threadIdx.x * per + j;
+        h[j] = j < per && d < P ? a.hist[d] : 0;
+        fill[j] = 0;
+        tail[j] = kNoChunk;
+        nnew[j] = 0;
+        if (h[j]) {
+            const uint32_t tc = a.tail_chunk[d], tf = a.tail_fill[d];
+            const bool open = tc != kNoChunk && tf < kChunk;
+            fill[j] = open ? tf : 0;
+            tail[j] = open ? tc : kNoChunk;
+            const uint32_t chunks = (uint32_t)(((uint64_t)fill[j] + h[j] + kChunk - 1) / kChunk);
+            nnew[j] = chunks - (open ? 1u : 0u);
+            my_new += nnew[j];
+            my_slots += chunks;
+        }
+    }
+    uint32_t pos_new = scan_detail::block_exclusive<uint32_t, kPlanBlock>(my_new, warp_tot, &tot_new);
+    uint32_t pos_slot = scan_detail::block_exclusive<uint32_t, kPlanBlock>(my_slots, warp_tot, &tot_slots);
+    if (tot_new > a.n_stack || tot_slots > a.plan_cap) {
+        if (threadIdx.x == 0 && a.err) atomicOr(a.err, 2u);
+        return;
+    }
+#pragma unroll
+    for (uint32_t j = 0; j < kPerMax; j++) {
+        const uint32_t d = threadIdx.x * per + j;
+        if (j >= per || d >= P) continue;
+        a.cursor[d] = fill[j];
+        a.win_off[d] = h[j] ? pos_slot : 0;
+        if (!h[j]) continue;
+        if (tail[j] != kNoChunk) a.plan_chunks[pos_slot++] = tail[j];
+        for (uint32_t c = 0; c < nnew[j]; c++) a.plan_chunks[pos_slot++] = a.stack[pos_new++];
     }
 }
 
@@ -592,6 +726,13 @@ cudaError_t launch_walk_part(const StepArgs &a, int app, int grid, cudaStream_t 
     return cudaGetLastError();
 }
 
+cudaError_t launch_plan(const PlanArgs &a, cudaStream_t st)
+{
+    if (a.P > kSmemPartMax) return cudaErrorInvalidValue;
+    plan_kernel<<<1, kPlanBlock, 0, st>>>(a);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_inject(const InjectArgs &a, int device, cudaStream_t st)
 {
     if (a.n == 0) return cudaSuccess;
@@ -606,29 +747,48 @@ cudaError_t launch_inject(const InjectArgs &a, int device, cudaStream_t st)
 cudaError_t launch_scatter(const ScatterArgs &a, int device, cudaStream_t st)
 {
     if (a.n == 0) return cudaSuccess;
-    int sms = 0;
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
-    if (a.P <= kSmemPartMax) {
-        static thread_local int configured_device = -1;
-        if (configured_device != device) {
-            cudaError_t e = cudaFuncSetAttribute(bucket_sort_kernel<16>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                 (int)bucket_smem<16>(kSmemPartMax));
-            if (e == cudaSuccess)
-                e = cudaFuncSetAttribute(bucket_sort_kernel<8>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)bucket_smem<8>(kSmemPartMax));
-            if (e != cudaSuccess) return e;
-            configured_device = device;
+    // per device and partition count: SMs, and the CTAs per SM of both shapes
+    // (one launch per wave iteration: no attribute queries on that path)
+    static thread_local int cached_device = -1;
+    static thread_local uint32_t cached_P = 0;
+    static thread_local int sms = 0, smem_optin = 0, per_sm_big = 0, per_sm_small = 0;
+    if (cached_device != device || (a.P <= kSmemPartMax && cached_P != a.P)) {
+        cudaError_t e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+        if (e == cudaSuccess) e = cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device);
+        // room for the kernels' static shared memory
+        const int dyn = smem_optin - 1024;
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(bucket_sort_kernel<1024, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn);
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(bucket_sort_kernel<512, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn);
+        per_sm_big = per_sm_small = 0;
+        if (e == cudaSuccess && a.P <= kSmemPartMax && bucket_smem<1024, 4>(a.P) + 1024 <= (size_t)smem_optin)
+            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_big, bucket_sort_kernel<1024, 4>, 1024,
+                                                              bucket_smem<1024, 4>(a.P));
+        if (e == cudaSuccess && a.P <= kSmemPartMax)
+            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_small, bucket_sort_kernel<512, 4>, 512,
+                                                              bucket_smem<512, 4>(a.P));
+        if (e != cudaSuccess) {
+            cached_device = -1;
+            return e;
         }
-        const int items = a.items == 8 ? 8 : 16;
-        const size_t smem = items == 8 ? bucket_smem<8>(a.P) : bucket_smem<16>(a.P);
-        const uint64_t tile = (uint64_t)kPartBlock * items;
+        cached_device = device;
+        cached_P = a.P;
+    }
+    if (a.P <= kSmemPartMax) {
+        // 4096-walker tiles unless 2048 are asked for (items 8), or where
+        // 4096 do not fit (P above about 3 700)
+        const bool small = a.items == 8 || per_sm_big == 0;
+        const int block = small ? 512 : 1024;
+        const size_t smem = small ? bucket_smem<512, 4>(a.P) : bucket_smem<1024, 4>(a.P);
+        const uint64_t tile = (uint64_t)block * 4;
         const uint64_t tiles = (a.n + tile - 1) / tile;
-        const uint64_t per_sm = smem <= 72 * 1024 ? 3 : smem <= 110 * 1024 ? 2 : 1;
+        const int per_sm = std::max(1, small ? per_sm_small : per_sm_big);
         const uint64_t blocks = std::min<uint64_t>(tiles, (uint64_t)sms * per_sm);
-        if (items == 8)
-            bucket_sort_kernel<8><<<(unsigned)blocks, kPartBlock, smem, st>>>(a);
+        if (small)
+            bucket_sort_kernel<512, 4><<<(unsigned)blocks, block, smem, st>>>(a);
         else
-            bucket_sort_kernel<16><<<(unsigned)blocks, kPartBlock, smem, st>>>(a);
+            bucket_sort_kernel<1024, 4><<<(unsigned)blocks, block, smem, st>>>(a);
         return cudaGetLastError();
     }
     const uint64_t tile = (uint64_t)kPartBlock * kScatterItems;

@@ -99,8 +99,31 @@ struct ScatterArgs {
     const uint32_t *win_off;       // P: start of the destination's window in plan_chunks
     const uint32_t *plan_chunks;   // chunk ids of every window
     uint32_t P;
-    int items;                     // walkers per thread of a bucketing tile (8 or 16; 0 = 16)
+    int items;                     // bucketing tile: 16 (0) = 4096 walkers, 8 = 2048
+    unsigned int *err;             // bit 0 set when a tile's bulk copy did not complete in time;
+                                   // the pass does nothing while bit 1 (a failed device plan) is set
+    // non-null: the staged count lives here (device memory) and n only bounds it
+    const unsigned long long *n_dev;
 };
+
+// Device-side plan of one bucketing pass, made right after the step kernel
+// from its histogram so that no host round trip separates the two: the
+// arrivals of destination d (hist[d]) go after the walkers of its open tail
+// chunk, then into new chunks popped from the free stack in destination
+// order.  The host replays the same arithmetic afterwards for its own queue
+// bookkeeping.
+struct PlanArgs {
+    const uint32_t *hist;        // P: arrivals per destination
+    const uint32_t *tail_chunk;  // P: last device chunk of d's queue, 0xFFFFFFFF = none
+    const uint32_t *tail_fill;   // P: walkers in it
+    const uint32_t *stack;       // free chunks, the next one to pop first
+    uint32_t n_stack;
+    uint32_t P;
+    uint32_t *cursor, *win_off, *plan_chunks;  // the ScatterArgs plan
+    uint64_t plan_cap;
+    unsigned int *err;           // bit 1 set when the stack or the plan buffer is too small
+};
+constexpr uint32_t kNoChunk = 0xFFFFFFFFu;
 
 // Walkers of newly admitted queries: walker i of query slot q (i < n) goes to
 // position cursor + i of the chunk window, with PPR length from (seed, i).
@@ -119,6 +142,8 @@ cudaError_t launch_inject(const InjectArgs &a, int device, cudaStream_t st);
 size_t part_smem(uint32_t P);
 cudaError_t launch_walk_part(const StepArgs &a, int app, int grid, cudaStream_t st);
 cudaError_t launch_scatter(const ScatterArgs &a, int device, cudaStream_t st);
+// P <= kSmemPartMax
+cudaError_t launch_plan(const PlanArgs &a, cudaStream_t st);
 
 // Ordinal t of the lazily created walkers of partition [nb, ne) under the
 // per-vertex start: walkers j*V + v (v in [nb, ne)), ordered j-major.

@@ -20,7 +20,7 @@ def g16():
 
 def _index_share(rp, part_bytes):
     """Partitions' worth of the -p budget the device-resident vertex index
-    takes (8 (V+1) bytes)."""
+    takes (at most 8 (V+1) bytes; 4 (V+1) in the compact layout)."""
     return -(-8 * len(rp) // part_bytes)
 
 
@@ -200,8 +200,10 @@ def c2s(lt):
     return g, W, want, st
 
 
-@pytest.mark.parametrize("sched,pipeline", [(2, True), (4, True), (3, True), (0, True), (0, False), (1, True)])
-def test_c2s_scale_ooc(lt, require_gpu, c2s, sched, pipeline):
+@pytest.mark.parametrize("sched,pipeline,host_plan", [(2, True, False), (2, True, True), (4, True, False),
+                                                      (3, True, False), (0, True, False), (0, False, False),
+                                                      (1, True, False)])
+def test_c2s_scale_ooc(lt, require_gpu, c2s, sched, pipeline, host_plan):
     """16 of the graph's partitions cached, walker pool 2^22: every scheduler,
     with and without the load/compute overlap, gives the oracle's counts bit
     for bit, and wave runs read bounded zero-copy groups (the path that takes
@@ -209,10 +211,11 @@ def test_c2s_scale_ooc(lt, require_gpu, c2s, sched, pipeline):
     while a load is in flight: its step kernel walks every walker through all
     cached partitions, so none keeps a queue (the reference stops walkers at
     each partition border, src/WalkManager.h:239, and computes the queues
-    that builds up during loads)."""
+    that builds up during loads).  Bucketing passes are planned by a device
+    kernel behind the step kernel, or (host_plan) by the host."""
     g, W, want, st = c2s
     assert g.num_partitions > 16
-    e = lt.Engine(g, partitions=16, batch=1 << 22, seed=1, sched=sched, pipeline=pipeline)
+    e = lt.Engine(g, partitions=16, batch=1 << 22, seed=1, sched=sched, pipeline=pipeline, host_plan=host_plan)
     got = e.ppr(0, W, 0.15)
     assert (got == want).all()
     s = e.stats()
@@ -221,7 +224,32 @@ def test_c2s_scale_ooc(lt, require_gpu, c2s, sched, pipeline):
         assert s["zerocopy_groups"] > 0
     if not pipeline:
         assert s["overlap_computes"] == 0
+    if host_plan:
+        assert s["device_plans"] == 0
+    else:
+        assert s["device_plans"] > 0
     e.close()
+
+
+@pytest.mark.parametrize("sched", [0, 2, 4])
+@pytest.mark.parametrize("host_plan", [False, True])
+@pytest.mark.parametrize("B", [0, 20000])
+def test_bucket_plan_device_or_host(lt, require_gpu, g16, sched, host_plan, B):
+    """A bucketing pass is planned by a device kernel right behind the step
+    kernel (default, whenever the free chunks provably hold every arrival) or
+    by the host after reading the histogram (which may spill walkers first):
+    the queues, and so the counts, are the same.  With a tiny walker pool (B)
+    the two kinds of pass alternate within one run."""
+    rp, col = g16
+    W = 300000
+    want, _, _ = oracle.ppr(rp, col, 0, W, prob=0.15, seed=9)
+    g, e = _eng(lt, rp, col, 256 << 10, partitions=4, batch=B, sched=sched, seed=9, host_plan=host_plan)
+    assert (e.ppr(0, W, 0.15) == want).all()
+    s = e.stats()
+    if host_plan:
+        assert s["device_plans"] == 0
+    elif B == 0:
+        assert s["device_plans"] > 0
 
 
 @pytest.mark.parametrize("sched", [0, 2])
