@@ -233,7 +233,59 @@ def cpu_sample(name, cfg, rp, col, threads):
 def cpu_baseline_leg(name, cfg, rp, col, seconds):
     """cpu_baseline: the oracle sample repeated until about `seconds` of CPU
     work (at least 3 samples), median rate; also returns the sample's
-    outputs for the parity check against the product."""
+    outputs for the parity check against the product.
+
+    The sample runs in a child process that has no CUDA context, as the
+    reference arm's process has none: on the GB300's Grace host a CUDA
+    context in the process slows the oracle's random reads of the graph by
+    about 38 % (the c2 sample: 31 -> 19 M steps/s on the same arrays before
+    and after the context was created).  The graph reaches the child through
+    an in-memory file (memfd); the outputs come back pickled."""
+    import mmap
+    import pickle
+    rp = np.ascontiguousarray(rp, dtype=np.uint64)
+    col = np.ascontiguousarray(col, dtype=np.uint32)
+    nbytes = rp.nbytes + col.nbytes
+    fd = os.memfd_create("lt_cpu_leg")
+    try:
+        os.ftruncate(fd, nbytes)
+        m = mmap.mmap(fd, nbytes)
+        np.frombuffer(m, dtype=np.uint64, count=len(rp))[:] = rp
+        np.frombuffer(m, dtype=np.uint32, count=len(col), offset=rp.nbytes)[:] = col
+        m.close()
+        out = subprocess.run([sys.executable, os.path.abspath(__file__), "--cpu-leg-child", str(fd), str(len(rp)),
+                              str(len(col)), name, repr(seconds)], pass_fds=(fd,), stdout=subprocess.PIPE,
+                             check=True).stdout
+    finally:
+        os.close(fd)
+    cpu, res = pickle.loads(out)
+    if isinstance(res, tuple) and res and res[0] == "sparse":
+        _, n, nz, vals = res
+        res = np.zeros(n, dtype=vals.dtype)
+        res[nz] = vals
+    return cpu, res
+
+
+def cpu_leg_child(argv):
+    """Child side of cpu_baseline_leg (no CUDA, no library of this
+    repository): maps the graph, runs the sample, pickles the result."""
+    import mmap
+    import pickle
+    fd, nrp, ncol, name, seconds = int(argv[0]), int(argv[1]), int(argv[2]), argv[3], float(argv[4])
+    m = mmap.mmap(fd, 8 * nrp + 4 * ncol, prot=mmap.PROT_READ)
+    rp = np.frombuffer(m, dtype=np.uint64, count=nrp)
+    col = np.frombuffer(m, dtype=np.uint32, count=ncol, offset=8 * nrp)
+    cpu, res = _cpu_baseline_here(name, CONFIGS[name], rp, col, seconds)
+    if isinstance(res, np.ndarray):
+        nz = np.nonzero(res)[0]
+        res = ("sparse", len(res), nz, res[nz])
+    sys.stdout.buffer.write(pickle.dumps((cpu, res), protocol=pickle.HIGHEST_PROTOCOL))
+    sys.stdout.flush()
+    return 0
+
+
+def _cpu_baseline_here(name, cfg, rp, col, seconds):
+    """The sample loop of cpu_baseline_leg, in this process."""
     threads = os.cpu_count() or 1
     rates, out, desc, total = [], None, "", 0.0
     while len(rates) < 3 or (total < seconds and len(rates) < 20):
@@ -387,7 +439,7 @@ def gb300_ooc(args, cfg):
     # sample ran 36 % slower than in the reference arm's fresh process)
     cpu, sample_counts = None, None
     if not args.no_cpu_baseline and ws == 1:
-        rp, col = (np.array(a) for a in g.csr_views())
+        rp, col = g.csr_views()
         cpu, sample_counts = cpu_baseline_leg(args.config, cfg, rp, col, args.cpu_seconds)
         del rp, col
     link_peak = lt.host_link_gbs(local)
@@ -968,6 +1020,8 @@ def gb300_serve(args, cfg):
 
 
 def main():
+    if len(sys.argv) > 1 and sys.argv[1] == "--cpu-leg-child":
+        return cpu_leg_child(sys.argv[2:])
     args = parse()
     cfg = CONFIGS[args.config]
     if cfg.get("serving") and args.impl != "reference":
