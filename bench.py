@@ -464,14 +464,15 @@ def gb300_ooc(args, cfg):
                 "plain_host_index": dict(sched=lt.SCHED_PLAIN, resident_index=False)}
     # named only through --variants: wave runs that read every uncached
     # partition zero-copy in each kernel (no bounded groups), bounded groups
-    # of other footprints, no prefill, and every bucketing pass planned by
-    # the host
+    # of other footprints, no prefill, every bucketing pass planned by the
+    # host, and 2048-walker bucketing tiles (two CTAs per SM)
     extra = {"learned_sweep": dict(sched=lt.SCHED_LEARNED, zc_group_bytes=1 << 62, sweep_walkers=1 << 62),
              "learned_zc2g": dict(sched=lt.SCHED_LEARNED, zc_group_bytes=2 << 30),
              "learned_zc8g": dict(sched=lt.SCHED_LEARNED, zc_group_bytes=8 << 30),
              "learned_noprefill": dict(sched=lt.SCHED_LEARNED, prefill=False),
              "frequency_noprefill": dict(sched=lt.SCHED_FREQUENCY, prefill=False),
-             "learned_hostplan": dict(sched=lt.SCHED_LEARNED, host_plan=True)}
+             "learned_hostplan": dict(sched=lt.SCHED_LEARNED, host_plan=True),
+             "learned_tile2k": dict(sched=lt.SCHED_LEARNED, bucket_items=8)}
     if args.variants:
         keep = args.variants.split(",")
         variants = {k: v for k, v in {**variants, **extra}.items() if k in keep}
@@ -524,9 +525,11 @@ def gb300_ooc(args, cfg):
         for name in variants:
             if name == "learned":
                 continue
-            variants[name] = {**variants[name], **shared,
+            # a variant's own knobs (e.g. learned_zc2g's group size) win
+            variants[name] = {**shared,
                               **(wave if name.split("_")[0] in ("batched", "frequency", "learned")
-                                 and "host_index" not in name else {})}
+                                 and "host_index" not in name else {}),
+                              **variants[name]}
     for i in range(args.warmup):
         for name in variants:
             if i == 0 or name == "learned":
@@ -993,7 +996,8 @@ def gb300_serve(args, cfg):
     time.sleep(0.3)
     wall0 = time.time()
     out = {}
-    for name, sched in [("learned", lt.SCHED_LEARNED), ("plain", lt.SCHED_PLAIN), ("batched", lt.SCHED_BATCHED)]:
+    for name, sched in [("learned", lt.SCHED_LEARNED), ("plain", lt.SCHED_PLAIN), ("batched", lt.SCHED_BATCHED),
+                        ("frequency", lt.SCHED_FREQUENCY)]:
         e = lt.Engine(g, partitions=cfg["partitions"], batch=cfg["batch"], seed=SEED_WALK, sched=sched, device=local)
         per_rate = {}
         for rate, seconds in zip(cfg["rates"], cfg["seconds"]):
