@@ -461,25 +461,30 @@ def gb300_ooc(args, cfg):
                 "plain_x8": dict(sched=lt.SCHED_PLAIN, zerocopy_threshold=8 * thr_ref),
                 "batched": dict(sched=lt.SCHED_BATCHED), "frequency": dict(sched=lt.SCHED_FREQUENCY),
                 "learned_host_index": dict(sched=lt.SCHED_LEARNED, resident_index=False),
-                "plain_host_index": dict(sched=lt.SCHED_PLAIN, resident_index=False)}
+                "plain_host_index": dict(sched=lt.SCHED_PLAIN, resident_index=False),
+                "learned_tier50": dict(sched=lt.SCHED_LEARNED, hot_tier=50)}
     # named only through --variants: wave runs that read every uncached
     # partition zero-copy in each kernel (no bounded groups), bounded groups
     # of other footprints, no prefill, every bucketing pass planned by the
-    # host, and 2048-walker bucketing tiles (two CTAs per SM)
+    # host, 2048-walker bucketing tiles (two CTAs per SM), and hot-vertex
+    # tiers of 25-75 % of the graph budget
     extra = {"learned_sweep": dict(sched=lt.SCHED_LEARNED, zc_group_bytes=1 << 62, sweep_walkers=1 << 62),
              "learned_zc2g": dict(sched=lt.SCHED_LEARNED, zc_group_bytes=2 << 30),
              "learned_zc8g": dict(sched=lt.SCHED_LEARNED, zc_group_bytes=8 << 30),
              "learned_noprefill": dict(sched=lt.SCHED_LEARNED, prefill=False),
              "frequency_noprefill": dict(sched=lt.SCHED_FREQUENCY, prefill=False),
              "learned_hostplan": dict(sched=lt.SCHED_LEARNED, host_plan=True),
-             "learned_tile2k": dict(sched=lt.SCHED_LEARNED, bucket_items=8)}
+             "learned_tile2k": dict(sched=lt.SCHED_LEARNED, bucket_items=8),
+             "learned_tier25": dict(sched=lt.SCHED_LEARNED, hot_tier=25),
+             "learned_tier75": dict(sched=lt.SCHED_LEARNED, hot_tier=75),
+             "frequency_tier50": dict(sched=lt.SCHED_FREQUENCY, hot_tier=50)}
     if args.variants:
         keep = args.variants.split(",")
         variants = {k: v for k, v in {**variants, **extra}.items() if k in keep}
         assert variants, f"no variant among {keep}"
     K = args.steps
     n_timed = {"learned": K, "batched": K, "frequency": K, "plain": min(K, 5), "plain_x8": min(K, 5),
-               "learned_host_index": min(K, 3), "plain_host_index": min(K, 3)}
+               "learned_host_index": min(K, 3), "plain_host_index": min(K, 3), "learned_tier50": min(K, 5)}
     n_timed.update({k: K for k in extra})
     engines = {}
     ref_counts = [None]
@@ -561,6 +566,7 @@ def gb300_ooc(args, cfg):
                      "refill_loads": st["refill_loads"], "prefill_loads": st["prefill_loads"],
                      "zerocopy_groups": st["zerocopy_groups"], "zerocopy_sweeps": st["zerocopy_sweeps"],
                      "overlap_computes": st["overlap_computes"], "device_plans": st["device_plans"],
+                     "hot_vertices": st["hot_vertices"],
                      "cache_slots": st["cache_slots"],
                      "index_on_device": bool(st["index_on_device"]), "step_s": spread(times[name]),
                      # where one run's time goes (last run): CUDA-event time of
@@ -683,6 +689,11 @@ def gb300_ooc(args, cfg):
         "learned_over_ablations": {n: {"steps_per_s": value / res[n]["value"],
                                        "bytes_per_step": L["bytes_per_step"] / res[n]["bytes_per_step"]}
                                    for n in ("batched", "frequency")},
+        # half the graph budget as a hot-vertex tier (built from the first
+        # run's counts): fewer host-link bytes per step, at this cost in steps/s
+        "hot_tier_50": {"steps_per_s": res["learned_tier50"]["value"] / value,
+                        "bytes_per_step": res["learned_tier50"]["bytes_per_step"] / L["bytes_per_step"],
+                        "hot_vertices": res["learned_tier50"]["hot_vertices"]},
         "serving_1000qps": serving,
         "parity": parity,
         "e2e": {"value": value, "unit": "steps/s", "h2d_bytes_per_step": s["h2d_graph_bytes"] + s["h2d_walker_bytes"],

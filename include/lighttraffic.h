@@ -119,6 +119,11 @@ typedef struct lt_engine_cfg {
     int bucket_items;                /* bucketing tile: 16 (0) = 4096 walkers, 8 = 2048 */
     int no_prefill;                  /* wave runs: 1 = leave a cold cache to fill as walkers arrive
                                         instead of loading the policy's forecast set at a run's start */
+    int hot_tier;                    /* wave runs with the device index: percent (0 = off, at most 90) of
+                                        the graph budget left by the index that holds a hot-vertex tier,
+                                        the adjacency of the vertices read most per byte outside the
+                                        cache, chosen from the counts of the engine's first run of a
+                                        walk and used by every later run (fewer partition slots) */
     int host_plan;                   /* out-of-core: 1 = the host plans every bucketing pass after
                                         reading the step kernel's histogram; 0 (default) = a device
                                         kernel plans it right behind the step kernel whenever the free
@@ -171,6 +176,8 @@ typedef struct lt_stats {
     double host_submit_ms;     /* work list, plan inputs and launches of each pass */
     double host_replay_ms;     /* queue bookkeeping after each histogram read-back */
     double host_observe_ms;    /* kernel timers and the policy's per-iteration update */
+    uint64_t hot_vertices;     /* vertices in the hot-vertex tier this run used (0: none) */
+    double tier_build_ms;      /* host time building the tier after this run (0: not built) */
 } lt_stats;
 
 const char *lt_strerror(lt_status s);

@@ -42,6 +42,13 @@ __device__ __forceinline__ uint32_t ld_nc_u32(const void *a, uint64_t pol)
     return v;
 }
 
+__device__ __forceinline__ uint2 ld_nc_u2(const void *a, uint64_t pol)
+{
+    uint2 v;
+    asm volatile("ld.global.nc.L2::cache_hint.v2.u32 {%0, %1}, [%2], %3;" : "=r"(v.x), "=r"(v.y) : "l"(a), "l"(pol));
+    return v;
+}
+
 // Read-only streaming load: not kept in L1, L2 policy as given.
 __device__ __forceinline__ uint32_t ld_nc_stream_u32(const void *a, uint64_t pol)
 {

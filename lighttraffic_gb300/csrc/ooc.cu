@@ -143,6 +143,24 @@ struct Ooc {
     // only col slices and zero-copy hops read rowptr here; null: the
     // reference's layout, rowptr slice then col slice in every slot
     uint32_t *d_index = nullptr;
+    // hot-vertex tier (cfg.hot_tier > 0): the adjacency of the vertices read
+    // most per byte in the partitions outside the cache, chosen from the
+    // counts of the engine's previous run of the same walk, in a device
+    // region paid from the -p budget (fewer slots):
+    //   uint2 words[ceil(V / 32)] | u32 rank -> pool offset[hot] | u32 pool
+    // packed on the host, copied in and marked in the vertex index at a
+    // run's start, unmarked when the cache is dropped
+    uint64_t tier_bytes = 0;  // device budget, 0 = no tier
+    uint8_t *d_tier = nullptr;
+    HostBuf h_tier;
+    uint64_t tier_words = 0;                 // ceil(V / 32)
+    uint64_t tier_hot = 0, tier_used = 0;    // current build: hot vertices, bytes in use
+    uint64_t tier_off_at = 0, tier_pool_at = 0;
+    bool tier_built = false, tier_loaded = false, tier_ready = false;
+    int tier_app = -1, tier_start = -1;
+    uint32_t tier_source = 0;
+    double tier_build_ms = 0;
+    cudaEvent_t ev_tier = nullptr;
     // zero-copy set of the next step kernel (wave runs)
     uint32_t zc_mask[kZcMaskWords] = {};
     bool zc_mask_any = false;
@@ -277,6 +295,149 @@ lt_status upload(Ooc &o, void *d_dst, const HostBuf &hb, uint8_t *hb_dev, const 
 }
 
 // waiting[] is kept current by refresh() wherever a queue changes.
+// ---- hot-vertex tier
+
+// Sets (set) or clears the tier mark (bit 31) in the vertex index entry of
+// every vertex the tier's words mark.
+__global__ void tier_mark_kernel(uint32_t *index, const uint2 *words, uint64_t n_words, uint32_t V, int set)
+{
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t w = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; w < n_words; w += stride) {
+        uint32_t m = words[w].x;
+        while (m) {
+            const uint32_t b = (uint32_t)__ffs(m) - 1;
+            m &= m - 1;
+            const uint64_t v = w * 32 + b;
+            if (v < V) index[v] = set ? (index[v] | kHotMark) : (index[v] & ~kHotMark);
+        }
+    }
+}
+
+lt_status tier_mark(Ooc &o, int set, cudaStream_t st)
+{
+    const uint64_t blocks = std::min<uint64_t>((o.tier_words + 255) / 256, 1024);
+    tier_mark_kernel<<<(unsigned)blocks, 256, 0, st>>>(o.d_index, (const uint2 *)o.d_tier, o.tier_words, o.g->V, set);
+    LT_CUDA_TRY(cudaGetLastError());
+    o.e->stats.kernel_launches++;
+    return LT_OK;
+}
+
+// Copies the built tier in and marks its vertices (copy stream); the step
+// kernels use it once the copy has landed (tier_ready, set by wave_step).
+lt_status tier_load(Ooc &o)
+{
+    lt_engine &e = *o.e;
+    if (!o.tier_built || o.tier_loaded) return LT_OK;
+    LT_CUDA_TRY(cudaMemcpyAsync(o.d_tier, o.h_tier.ptr, o.tier_used, cudaMemcpyHostToDevice, e.s_copy));
+    LT_TRY(tier_mark(o, 1, e.s_copy));
+    LT_CUDA_TRY(cudaEventRecord(o.ev_tier, e.s_copy));
+    e.stats.h2d_graph_bytes += o.tier_used;
+    o.tier_loaded = true;
+    o.tier_ready = false;
+    return LT_OK;
+}
+
+// Takes the tier out of use: unmarks the index (after every kernel that may
+// read it).
+lt_status tier_unload(Ooc &o)
+{
+    lt_engine &e = *o.e;
+    if (!o.tier_loaded) return LT_OK;
+    LT_CUDA_TRY(cudaStreamSynchronize(e.s_copy));
+    LT_CUDA_TRY(cudaStreamSynchronize(e.s_compute));
+    LT_TRY(tier_mark(o, 0, e.s_compute));
+    LT_CUDA_TRY(cudaStreamSynchronize(e.s_compute));
+    o.tier_loaded = o.tier_ready = false;
+    return LT_OK;
+}
+
+// Builds the tier for the next runs of the same walk from this run's
+// per-vertex counts (PPR endpoints, PageRank visits: proportional to the
+// reads of each vertex's adjacency).  Candidates are the vertices of the
+// partitions outside the cache at the end of the run; each is worth
+// counts / (4 deg + 4) (its adjacency and its pool offset), and the best go
+// in until the budget is spent: a histogram of the worths (the top 16 bits of
+// the float) finds the threshold.
+lt_status tier_build(Ooc &o, int app, int start, uint32_t source, const uint64_t *counts)
+{
+    lt_graph &g = *o.g;
+    const double t0 = now_ms();
+    LT_TRY(tier_unload(o));
+    o.tier_built = false;
+    const uint64_t *rowptr = g.rowptr();
+    const uint32_t *colp = g.col();
+    const uint64_t words_bytes = 8 * o.tier_words;
+    const uint64_t budget = o.tier_bytes - words_bytes - 16;
+    auto key_of = [&](uint32_t v, uint32_t p) -> int32_t {
+        if (o.slot_of[p] >= 0 || counts[v] == 0) return -1;
+        const uint64_t deg = rowptr[v + 1] - rowptr[v];
+        if (deg == 0) return -1;
+        const float worth = (float)counts[v] / (float)(4 * deg + 4);
+        uint32_t bits;
+        std::memcpy(&bits, &worth, 4);
+        return (int32_t)(bits >> 16);
+    };
+    // histogram of candidate bytes per worth key
+    std::vector<uint64_t> hist(1 << 16, 0);
+#pragma omp parallel
+    {
+        std::vector<uint64_t> mine(1 << 16, 0);
+#pragma omp for schedule(dynamic, 1)
+        for (int64_t p = 0; p < (int64_t)o.P; p++)
+            for (uint32_t v = g.node_off[p]; v < g.node_off[p + 1]; v++) {
+                const int32_t k = key_of(v, (uint32_t)p);
+                if (k >= 0) mine[k] += 4 * (rowptr[v + 1] - rowptr[v]) + 4;
+            }
+#pragma omp critical
+        for (size_t k = 0; k < mine.size(); k++) hist[k] += mine[k];
+    }
+    int32_t thr = (1 << 16) - 1;
+    uint64_t above = 0;
+    while (thr >= 0 && above + hist[thr] <= budget) above += hist[thr--];
+    // the vertices above the threshold key go in (a key spans under 1 % of
+    // worth: the threshold's own key is left out)
+    uint2 *words = (uint2 *)o.h_tier.ptr;
+    std::memset(words, 0, words_bytes);
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int64_t p = 0; p < (int64_t)o.P; p++)
+        for (uint32_t v = g.node_off[p]; v < g.node_off[p + 1]; v++)
+            if (key_of(v, (uint32_t)p) > thr) __atomic_fetch_or(&words[v >> 5].x, 1u << (v & 31), __ATOMIC_RELAXED);
+    // ranks, pool offsets and the pool
+    uint64_t hot = 0;
+    for (uint64_t w = 0; w < o.tier_words; w++) {
+        words[w].y = (uint32_t)hot;
+        hot += (uint64_t)__builtin_popcount(words[w].x);
+    }
+    o.tier_off_at = words_bytes;
+    o.tier_pool_at = (o.tier_off_at + 4 * hot + 15) & ~15ull;
+    uint32_t *off = (uint32_t *)((uint8_t *)o.h_tier.ptr + o.tier_off_at);
+    uint32_t *pool = (uint32_t *)((uint8_t *)o.h_tier.ptr + o.tier_pool_at);
+    uint64_t pw = 0;
+    for (uint64_t w = 0; w < o.tier_words; w++)
+        for (uint32_t m = words[w].x; m; m &= m - 1) {
+            const uint64_t v = w * 32 + (uint32_t)__builtin_ctz(m);
+            off[words[w].y + (uint32_t)__builtin_popcount(words[w].x & ((1u << (v & 31)) - 1u))] = (uint32_t)pw;
+            pw += rowptr[v + 1] - rowptr[v];
+        }
+    if (o.tier_pool_at + 4 * pw > o.tier_bytes || pw >= (1ull << 32))
+        return fail(LT_ERR_CAPACITY, "hot-vertex tier overflows its budget");
+#pragma omp parallel for schedule(dynamic, 256)
+    for (int64_t w = 0; w < (int64_t)o.tier_words; w++)
+        for (uint32_t m = words[w].x; m; m &= m - 1) {
+            const uint64_t v = (uint64_t)w * 32 + (uint32_t)__builtin_ctz(m);
+            const uint32_t r = words[w].y + (uint32_t)__builtin_popcount(words[w].x & ((1u << (v & 31)) - 1u));
+            std::memcpy(pool + off[r], colp + rowptr[v], 4 * (rowptr[v + 1] - rowptr[v]));
+        }
+    o.tier_hot = hot;
+    o.tier_used = o.tier_pool_at + 4 * pw;
+    o.tier_app = app;
+    o.tier_start = start;
+    o.tier_source = source;
+    o.tier_built = hot > 0;
+    o.tier_build_ms = now_ms() - t0;
+    return LT_OK;
+}
+
 void refresh(Ooc &o, uint32_t p)
 {
     o.waiting[p] = o.q[p].total();
@@ -711,6 +872,12 @@ lt_status step_and_bucket_parts(Ooc &o, const RunParams &rp, const std::vector<u
     a.zc_rp_base = o.zc_rp_base;
     a.rp32 = o.d_index != nullptr;
     a.zc_col_base = o.zc_col_base;
+    if (o.tier_ready) {
+        a.hot_on = 1;
+        a.hot_words = (const uint2 *)o.d_tier;
+        a.hot_off = (const uint32_t *)(o.d_tier + o.tier_off_at);
+        a.hot_pool = (const uint32_t *)(o.d_tier + o.tier_pool_at);
+    }
     if (o.zc_mask_any) std::memcpy(a.zc_mask, o.zc_mask, sizeof a.zc_mask);
     if (o.serve) serve_args(o, a);
     if (zero_copy) {
@@ -1118,6 +1285,15 @@ lt_status wave_step(Ooc &o, const RunParams &rp, WaveState &w, bool &done)
             }
             inflight.resize(keep);
         }
+        if (o.tier_loaded && !o.tier_ready) {
+            const cudaError_t q = cudaEventQuery(o.ev_tier);
+            if (q == cudaSuccess)
+                o.tier_ready = true;
+            else if (q != cudaErrorNotReady)
+                LT_CUDA_TRY(q);
+            else
+                cudaGetLastError();
+        }
         refresh_all(o);
         bool any = false;
         for (uint32_t p = 0; p < o.P && !any; p++) any = o.waiting[p] > 0;
@@ -1498,7 +1674,20 @@ lt_status ooc_create(lt_engine *e, Ooc **out)
     // none, the slots carry rowptr slices instead.
     if (o->d_index) {
         const uint64_t budget = (uint64_t)o->K * g.part_bytes, index_bytes = 4ull * ((uint64_t)g.V + 1);
-        const uint64_t fit = budget > index_bytes ? (budget - index_bytes) / o->slot_stride : 0;
+        uint64_t fit = budget > index_bytes ? (budget - index_bytes) / o->slot_stride : 0;
+        // the hot-vertex tier takes its share of what the index leaves
+        const bool wave = e->cfg.sched == LT_SCHED_LEARNED || e->cfg.sched == LT_SCHED_FREQUENCY ||
+                          e->cfg.sched == LT_SCHED_BATCHED;
+        if (e->cfg.hot_tier > 0 && wave && fit >= 2 && g.max_edges < (1ull << 31) && o->P <= kSmemPartMax) {
+            const uint64_t avail = budget - index_bytes;
+            const uint64_t want = (avail / 100 * std::min<uint64_t>((uint64_t)e->cfg.hot_tier, 90)) & ~255ull;
+            o->tier_words = ((uint64_t)g.V + 31) / 32;
+            const uint64_t left = (avail - want) / o->slot_stride;
+            if (want > 8 * o->tier_words + 4096 && left >= 1) {
+                o->tier_bytes = want;
+                fit = left;
+            }
+        }
         if (fit >= 1) {
             o->K = (uint32_t)std::min<uint64_t>(o->K, fit);
         } else {
@@ -1517,6 +1706,12 @@ lt_status ooc_create(lt_engine *e, Ooc **out)
     if (s == LT_OK) s = dalloc(&o->d_ctl, o->ctl_words);
     if (s == LT_OK) s = dalloc(&o->d_stats, 8);
     if (s == LT_OK) s = host_alloc(o->h_ctl, 4 * o->ctl_words, true);
+    if (s == LT_OK && o->tier_bytes) {
+        s = dalloc(&o->d_tier, o->tier_bytes);
+        if (s == LT_OK) s = host_alloc(o->h_tier, o->tier_bytes, true);
+        if (s == LT_OK && cudaEventCreateWithFlags(&o->ev_tier, cudaEventDisableTiming) != cudaSuccess)
+            s = fail(LT_ERR_CUDA, "event creation failed");
+    }
     if (s != LT_OK) return bail(s);
     if (cudaMemcpy(o->d_node_off, g.node_off.data(), 4ull * (o->P + 1), cudaMemcpyHostToDevice) != cudaSuccess ||
         cudaMemcpy(o->d_edge_off, g.edge_off.data(), 8ull * (o->P + 1), cudaMemcpyHostToDevice) != cudaSuccess ||
@@ -1560,6 +1755,7 @@ lt_status ooc_create(lt_engine *e, Ooc **out)
         o->zc_col_base = (unsigned long long)(uintptr_t)col_dev;
     } else {
         o->zc_threshold = 0;  // the graph is not in pinned memory: always load
+        o->tier_bytes = 0;    // (the tier's kernel path reads the index through zc_rp_base)
     }
     const size_t smem = part_smem(o->P);
     if (smem > 64 * 1024) return bail(fail(LT_ERR_UNSUPPORTED, "partition count %u needs %zu bytes of shared memory", o->P, smem));
@@ -1581,6 +1777,9 @@ void ooc_destroy(Ooc *o)
     host_free(o->h_plan);
     host_free(o->h_work);
     host_free(o->h_planin);
+    host_free(o->h_tier);
+    if (o->d_tier) cudaFree(o->d_tier);
+    if (o->ev_tier) cudaEventDestroy(o->ev_tier);
     if (o->ev_ctl) cudaEventDestroy(o->ev_ctl);
     for (cudaEvent_t ev : o->ev_free) cudaEventDestroy(ev);
     delete o;
@@ -1590,9 +1789,11 @@ void ooc_policy_stats(const Ooc *o, lt_policy_stats &s) { o->policy->stats(s); }
 
 // Autotuner of the out-of-core engine.  It times cold-cache PPR trial runs
 // (from the vertex with the most out-edges, as many walkers as the device
-// pool holds, at most 2^26) and walks the runtime knobs one at a time,
-// keeping each value that shortens the trial by 3 % or more (coordinate
-// descent; smaller differences are within run-to-run noise): the
+// pool holds, at most 2^26; the best of three per setting) and walks the
+// runtime knobs one at a time, keeping each value that shortens the trial by
+// 5 % or more (coordinate descent; with a 3 % margin it once kept 256 MiB
+// zero-copy groups that were 3.4 % faster on the trial and 5 % slower on the
+// c2 run): the
 // zero-copy group footprint and the load threshold factor of wave runs, the
 // step kernel's resident CTAs per SM and the bucketing tile.  Every knob
 // changes only the schedule, so results are unchanged.  The walker chunk
@@ -1613,7 +1814,7 @@ lt_status ooc_autotune(lt_engine *e, lt_ooc_tune *out)
     auto trial = [&](double &ms) -> lt_status {
         for (int app = 0; app < 3; app++) o.grid[app] = part_grid(app, 0, e->device, part_smem(o.P), e->cfg.ctas_per_sm);
         ms = 1e30;
-        for (int rep = 0; rep < 2; rep++) {
+        for (int rep = 0; rep < 3; rep++) {
             LT_TRY(ooc_drop_cache(&o));
             LT_TRY(ooc_run(e, kPPR, kStartSource, src, W, 0, 1, 0, 0.15f, nullptr, nullptr, nullptr));
             ms = std::min(ms, e->stats.running_ms);
@@ -1647,7 +1848,7 @@ lt_status ooc_autotune(lt_engine *e, lt_ooc_tune *out)
             double ms = 0;
             st = trial(ms);
             if (st != LT_OK) break;
-            if (ms < best * 0.97) {
+            if (ms < best * 0.95) {
                 best = ms;
                 pick = val;
             }
@@ -1688,6 +1889,7 @@ lt_status ooc_drop_cache(Ooc *o)
     lt_engine &e = *o->e;
     LT_CUDA_TRY(cudaStreamSynchronize(e.s_compute));
     LT_CUDA_TRY(cudaStreamSynchronize(e.s_copy));
+    LT_TRY(tier_unload(*o));
     for (uint32_t p = 0; p < o->P; p++)
         if (o->slot_of[p] >= 0) LT_TRY(evict_partition(*o, p));
     LT_CUDA_TRY(cudaStreamSynchronize(e.s_compute));
@@ -2012,6 +2214,9 @@ lt_status run_prepare(Ooc &o, const RunParams &rp)
 {
     lt_graph &g = *o.g;
     o.policy->run_start();
+    // the tier holds graph data: any walk may read it, whichever built it
+    if (o.tier_built && !o.serve) LT_TRY(tier_load(o));
+    o.e->stats.hot_vertices = o.tier_loaded ? o.tier_hot : 0;
     reset_queues(o);
     refresh_all(o);
     o.prev_computed = -1;
@@ -2142,6 +2347,21 @@ lt_status run_all(lt_engine *e, RunParams &rp, uint32_t runs, uint32_t run_base,
     e->stats.zerocopy_bytes = hs[3] * zc_bytes_per_hop(o);
     e->stats.handoffs = hs[4];
     e->stats.running_ms = now_ms() - t0;
+    // After the first run of a walk (PPR or PageRank, single source or any
+    // start), the hot-vertex tier is built from its counts for the runs that
+    // follow; outside the run's time.
+    if (o.tier_bytes && !o.serve && rp.counts && (rp.app == kPPR || rp.app == kPageRank) &&
+        !(o.tier_built && o.tier_app == rp.app && o.tier_start == rp.start && o.tier_source == rp.source)) {
+        std::vector<uint64_t> tmp;
+        const uint64_t *c = counts_out;
+        if (!c) {
+            tmp.resize(g.V);
+            LT_CUDA_TRY(cudaMemcpy(tmp.data(), rp.counts, 8ull * g.V, cudaMemcpyDeviceToHost));
+            c = tmp.data();
+        }
+        LT_TRY(tier_build(o, rp.app, rp.start, rp.source, c));
+        e->stats.tier_build_ms = o.tier_build_ms;
+    }
     return LT_OK;
 }
 

@@ -67,21 +67,50 @@ __device__ __forceinline__ uint32_t ld_u32(unsigned long long addr, uint64_t str
 // compact device-resident index (a.rp32), u32 offsets relative to the
 // partition's first edge; eb is then the partition's edge count, which ends
 // the last vertex's row.
+// hot: the vertex carries the tier mark (compact index only).
 __device__ __forceinline__ void row_at(bool rp32, unsigned long long rp, unsigned long long col, uint64_t eb,
                                        uint32_t cur, uint32_t nb, uint32_t ne, uint64_t keep,
-                                       unsigned long long &first_addr, uint64_t &deg)
+                                       unsigned long long &first_addr, uint64_t &deg, bool &hot)
 {
     const uint32_t rel = cur - nb;
     if (rp32) {
-        const uint32_t lo = ld_nc_u32(reinterpret_cast<const void *>(rp + 4ull * rel), keep);
-        const uint32_t hi =
-            cur + 1 < ne ? ld_nc_u32(reinterpret_cast<const void *>(rp + 4ull * (rel + 1)), keep) : (uint32_t)eb;
+        const uint32_t lo_m = ld_nc_u32(reinterpret_cast<const void *>(rp + 4ull * rel), keep);
+        const uint32_t hi = cur + 1 < ne
+                                ? ld_nc_u32(reinterpret_cast<const void *>(rp + 4ull * (rel + 1)), keep) & ~kHotMark
+                                : (uint32_t)eb;
+        const uint32_t lo = lo_m & ~kHotMark;
         first_addr = col + 4ull * lo;
         deg = hi - lo;
+        hot = (lo_m & kHotMark) != 0;
     } else {
+        hot = false;
         const uint64_t first = ld_u64(rp + 8ull * rel, keep);
         deg = ld_u64(rp + 8ull * (rel + 1), keep) - first;
         first_addr = col + 4ull * (first - eb);
+    }
+}
+
+// Address of the first column entry of marked vertex v in the tier.
+__device__ __forceinline__ unsigned long long hot_first(const StepArgs &a, uint32_t v, uint64_t keep)
+{
+    const uint2 w = ld_nc_u2(a.hot_words + (v >> 5), keep);
+    const uint32_t rank = w.y + __popc(w.x & ((1u << (v & 31)) - 1u));
+    return (unsigned long long)(a.hot_pool + ld_nc_u32(a.hot_off + rank, keep));
+}
+
+// Row of the next update in the lane's readable range; a marked vertex of a
+// zero-copy partition is read from the tier instead of host memory.
+template <bool HOT>
+__device__ __forceinline__ void row_of(const StepArgs &a, unsigned long long rp, unsigned long long col, uint64_t eb,
+                                       uint32_t cur, uint32_t nb, uint32_t ne, bool zc, uint64_t keep,
+                                       unsigned long long &first_addr, uint64_t &deg, bool &zc_read)
+{
+    bool marked;
+    row_at(a.rp32, rp, col, eb, cur, nb, ne, keep, first_addr, deg, marked);
+    zc_read = zc;
+    if (HOT && marked && zc) {
+        first_addr = hot_first(a, cur, keep);
+        zc_read = false;
     }
 }
 
@@ -119,7 +148,9 @@ __device__ __forceinline__ void ppr_count(const StepArgs &a, uint32_t qs, uint32
 template <int APP>
 constexpr int part_min_blocks() { return APP == kPPR ? 5 : 6; }
 
-template <int APP>
+// HOT: the hot-vertex tier is on (a.hot_on); a separate instance, so that
+// runs without the tier keep the registers of the kernel without it.
+template <int APP, bool HOT>
 __global__ void __launch_bounds__(kPartBlock, part_min_blocks<APP>()) walk_part_kernel(StepArgs a)
 {
     extern __shared__ uint32_t smem[];
@@ -256,7 +287,27 @@ __global__ void __launch_bounds__(kPartBlock, part_min_blocks<APP>()) walk_part_
                         col = a.zc_col_base + 4ull * a.t.edge_off[p];
                     }
                 }
-                if (rp == 0ull) {
+                bool hot = false;
+                if (HOT && rp == 0ull) {
+                    // unreadable partition: a marked vertex is read from the
+                    // tier, as a one-vertex readable range of the lane
+                    const uint32_t lo_m = ld_nc_u32(reinterpret_cast<const void *>(a.zc_rp_base + 4ull * cur), keep);
+                    if (lo_m & kHotMark) {
+                        const uint32_t lo = lo_m & ~kHotMark;
+                        cp_eb = cur + 1 < off[p + 1]
+                                    ? ld_nc_u32(reinterpret_cast<const void *>(a.zc_rp_base + 4ull * (cur + 1)), keep) &
+                                          ~kHotMark
+                                    : a.t.edge_off[p + 1] - a.t.edge_off[p];
+                        cp_nb = cur;
+                        cp_ne = cur + 1;
+                        cp_rp = a.zc_rp_base + 4ull * cur;
+                        cp_col = hot_first(a, cur, keep) - 4ull * lo;
+                        cp_zc = false;
+                        hot = true;
+                    }
+                }
+                if (hot) {
+                } else if (rp == 0ull) {
                     emit = true;
                     dest = p;
                     cp_nb = 1;
@@ -303,12 +354,13 @@ __global__ void __launch_bounds__(kPartBlock, part_min_blocks<APP>()) walk_part_
                 step = s - 1;
                 unsigned long long fa;
                 uint64_t deg;
-                row_at(a.rp32, cp_rp, cp_col, cp_eb, cur, cp_nb, cp_ne, keep, fa, deg);
+                bool zc_read;
+                row_of<HOT>(a, cp_rp, cp_col, cp_eb, cur, cp_nb, cp_ne, cp_zc, keep, fa, deg, zc_read);
                 if (deg > 0) {
                     const Rand4 q = walk_draw(seed, s, kTagStep, a.run, idx);
                     cur = ld_u32(fa + 4ull * mod_u64(r64_of(q), deg), stream);
                     n_mov++;
-                    n_zc += cp_zc;
+                    n_zc += zc_read;
                 } else {
                     ppr_count(a, qs, cur);
                     done = true;
@@ -326,11 +378,12 @@ __global__ void __launch_bounds__(kPartBlock, part_min_blocks<APP>()) walk_part_
                 if (!tele) {
                     unsigned long long fa;
                     uint64_t deg;
-                    row_at(a.rp32, cp_rp, cp_col, cp_eb, cur, cp_nb, cp_ne, keep, fa, deg);
+                    bool zc_read;
+                    row_of<HOT>(a, cp_rp, cp_col, cp_eb, cur, cp_nb, cp_ne, cp_zc, keep, fa, deg, zc_read);
                     if (deg > 0) {
                         cur = ld_u32(fa + 4ull * mod_u64(r64, deg), stream);
                         n_mov++;
-                        n_zc += cp_zc;
+                        n_zc += zc_read;
                     } else {
                         tele = true;
                     }
@@ -344,13 +397,14 @@ __global__ void __launch_bounds__(kPartBlock, part_min_blocks<APP>()) walk_part_
             // app/genericwalk.cu:22-32
             unsigned long long fa;
             uint64_t deg;
-            row_at(a.rp32, cp_rp, cp_col, cp_eb, cur, cp_nb, cp_ne, keep, fa, deg);
+            bool zc_read;
+            row_of<HOT>(a, cp_rp, cp_col, cp_eb, cur, cp_nb, cp_ne, cp_zc, keep, fa, deg, zc_read);
             uint32_t *path = a.paths ? a.paths + (uint64_t)idx * (a.length + 1) : nullptr;
             if (deg > 0) {
                 const Rand4 q = walk_draw(seed, s, kTagStep, a.run, idx);
                 cur = ld_u32(fa + 4ull * mod_u64(r64_of(q), deg), stream);
                 n_mov++;
-                n_zc += cp_zc;
+                n_zc += zc_read;
                 hop++;
                 if (path) path[hop] = cur;
                 step = s - 1;
@@ -694,10 +748,12 @@ __global__ void inject_kernel(InjectArgs a)
 template <int APP>
 int occ_part(size_t smem)
 {
-    if (smem > 48 * 1024)
-        cudaFuncSetAttribute(walk_part_kernel<APP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (smem > 48 * 1024) {
+        cudaFuncSetAttribute(walk_part_kernel<APP, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        cudaFuncSetAttribute(walk_part_kernel<APP, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    }
     int n = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, walk_part_kernel<APP>, kPartBlock, smem);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, walk_part_kernel<APP, false>, kPartBlock, smem);
     return n;
 }
 
@@ -719,9 +775,24 @@ cudaError_t launch_walk_part(const StepArgs &a, int app, int grid, cudaStream_t 
 {
     const size_t smem = part_smem(a.t.P);
     switch (app) {
-    case kPPR: walk_part_kernel<kPPR><<<grid, kPartBlock, smem, st>>>(a); break;
-    case kPageRank: walk_part_kernel<kPageRank><<<grid, kPartBlock, smem, st>>>(a); break;
-    default: walk_part_kernel<kWalk><<<grid, kPartBlock, smem, st>>>(a); break;
+    case kPPR:
+        if (a.hot_on)
+            walk_part_kernel<kPPR, true><<<grid, kPartBlock, smem, st>>>(a);
+        else
+            walk_part_kernel<kPPR, false><<<grid, kPartBlock, smem, st>>>(a);
+        break;
+    case kPageRank:
+        if (a.hot_on)
+            walk_part_kernel<kPageRank, true><<<grid, kPartBlock, smem, st>>>(a);
+        else
+            walk_part_kernel<kPageRank, false><<<grid, kPartBlock, smem, st>>>(a);
+        break;
+    default:
+        if (a.hot_on)
+            walk_part_kernel<kWalk, true><<<grid, kPartBlock, smem, st>>>(a);
+        else
+            walk_part_kernel<kWalk, false><<<grid, kPartBlock, smem, st>>>(a);
+        break;
     }
     return cudaGetLastError();
 }

@@ -79,6 +79,17 @@ struct StepArgs {
     // the partition's first edge (the compact device-resident vertex index);
     // 0: u64 global edge offsets
     int rp32;
+    // hot-vertex tier (hot_on, rp32 only): bit 31 of a vertex's entry in the
+    // device index marks it as held in the tier; hot_words[v / 32] = {the
+    // marks of vertices 32 (v / 32) .. + 31, tier rank of the first marked
+    // one}, hot_off[rank] = word offset of its adjacency in hot_pool.  A hop
+    // at a marked vertex of a partition outside the device cache reads its
+    // column entry from hot_pool instead of host memory (or of waiting for
+    // the partition).  Every reader of the index masks the mark.
+    int hot_on;
+    const uint2 *hot_words;
+    const uint32_t *hot_off;
+    const uint32_t *hot_pool;
     // query mode (serving many PPR queries): per query slot its key, table and
     // finished-walker counter; endpoints go to the query's table instead of
     // `counts`.  q_seed == null: single-run mode.
@@ -124,6 +135,7 @@ struct PlanArgs {
     unsigned int *err;           // bit 1 set when the stack or the plan buffer is too small
 };
 constexpr uint32_t kNoChunk = 0xFFFFFFFFu;
+constexpr uint32_t kHotMark = 0x80000000u;   // tier mark in a device index entry
 
 // Walkers of newly admitted queries: walker i of query slot q (i < n) goes to
 // position cursor + i of the chunk window, with PPR length from (seed, i).

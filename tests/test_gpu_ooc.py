@@ -268,3 +268,46 @@ def test_ooc_autotune_keeps_results(lt, require_gpu, g16, sched):
         g, e = _eng(lt, rp, col, 256 << 10, partitions=4, sched=sched, seed=3, bucket_items=items, ctas_per_sm=ctas,
                     load_factor=2, zc_group_bytes=1 << 20)
         assert (e.ppr(0, 200000, 0.15) == want).all()
+
+
+@pytest.mark.parametrize("sched", [2, 3, 4])
+def test_hot_tier_keeps_results(lt, require_gpu, g16, sched):
+    """The hot-vertex tier (built after the first run of a walk from its
+    counts, copied in and marked in the vertex index at every later run's
+    start, unmarked when the cache is dropped) changes where column entries
+    are read, never the result -- and, holding graph data, serves any walk."""
+    rp, col = g16
+    V = len(rp) - 1
+    g, e = _eng(lt, rp, col, 256 << 10, partitions=6, sched=sched, seed=9, hot_tier=50)
+    W = 300000
+    want, _, st = oracle.ppr(rp, col, 0, W, prob=0.15, seed=9)
+    for r in range(3):
+        assert (e.ppr(0, W, 0.15) == want).all()
+        s = e.stats()
+        assert s["moves"] == st[1]
+        if r == 0:
+            assert s["hot_vertices"] == 0 and s["tier_build_ms"] > 0
+        else:
+            assert s["hot_vertices"] > 0
+        if r == 1:
+            e.drop_cache()
+    pr_want, _ = oracle.pagerank(rp, col, 2 * V, length=8, runs=2, seed=9, start_mode=1)
+    assert (e.pagerank(2 * V, length=8, runs=2, start=1) == pr_want).all()
+    assert e.stats()["hot_vertices"] > 0
+
+
+def test_hot_tier_c2s(lt, require_gpu, c2s):
+    """c2s with a tier of half the budget: the second run reads hot vertices
+    from the tier and still gives the oracle's counts, with fewer zero-copy
+    bytes than the first."""
+    g, W, want, st = c2s
+    e = lt.Engine(g, partitions=16, batch=1 << 22, seed=1, sched=2, hot_tier=50)
+    first = e.ppr(0, W, 0.15)
+    s1 = e.stats()
+    e.drop_cache()
+    second = e.ppr(0, W, 0.15)
+    s2 = e.stats()
+    assert (first == want).all() and (second == want).all()
+    assert s1["hot_vertices"] == 0 and s2["hot_vertices"] > 0
+    assert s2["zerocopy_bytes"] < s1["zerocopy_bytes"]
+    e.close()
