@@ -475,6 +475,7 @@ def gb300_ooc(args, cfg):
              "frequency_noprefill": dict(sched=lt.SCHED_FREQUENCY, prefill=False),
              "learned_hostplan": dict(sched=lt.SCHED_LEARNED, host_plan=True),
              "learned_tile2k": dict(sched=lt.SCHED_LEARNED, bucket_items=8),
+             "learned_nosplit": dict(sched=lt.SCHED_LEARNED, split=False),
              "learned_tier25": dict(sched=lt.SCHED_LEARNED, hot_tier=25),
              "learned_tier75": dict(sched=lt.SCHED_LEARNED, hot_tier=75),
              "frequency_tier50": dict(sched=lt.SCHED_FREQUENCY, hot_tier=50)}
@@ -566,7 +567,7 @@ def gb300_ooc(args, cfg):
                      "refill_loads": st["refill_loads"], "prefill_loads": st["prefill_loads"],
                      "zerocopy_groups": st["zerocopy_groups"], "zerocopy_sweeps": st["zerocopy_sweeps"],
                      "overlap_computes": st["overlap_computes"], "device_plans": st["device_plans"],
-                     "hot_vertices": st["hot_vertices"],
+                     "hot_vertices": st["hot_vertices"], "split_launches": st["split_launches"],
                      "cache_slots": st["cache_slots"],
                      "index_on_device": bool(st["index_on_device"]), "step_s": spread(times[name]),
                      # where one run's time goes (last run): CUDA-event time of

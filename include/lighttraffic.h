@@ -124,6 +124,9 @@ typedef struct lt_engine_cfg {
                                         the adjacency of the vertices read most per byte outside the
                                         cache, chosen from the counts of the engine's first run of a
                                         walk and used by every later run (fewer partition slots) */
+    int no_split;                    /* wave runs: 1 = one step kernel per pass; 0 (default) = while a
+                                        zero-copy group is read, the walkers of cached queues and the ones
+                                        created in the pass run in a concurrent kernel on one CTA per SM */
     int host_plan;                   /* out-of-core: 1 = the host plans every bucketing pass after
                                         reading the step kernel's histogram; 0 (default) = a device
                                         kernel plans it right behind the step kernel whenever the free
@@ -176,6 +179,7 @@ typedef struct lt_stats {
     double host_submit_ms;     /* work list, plan inputs and launches of each pass */
     double host_replay_ms;     /* queue bookkeeping after each histogram read-back */
     double host_observe_ms;    /* kernel timers and the policy's per-iteration update */
+    uint64_t split_launches;   /* passes whose step ran as two concurrent kernels */
     uint64_t hot_vertices;     /* vertices in the hot-vertex tier this run used (0: none) */
     double tier_build_ms;      /* host time building the tier after this run (0: not built) */
 } lt_stats;

@@ -52,7 +52,8 @@ class EngineCfg(C.Structure):
                 ("zerocopy_threshold", C.c_uint64), ("seed", C.c_uint64), ("block_size", C.c_int),
                 ("ctas_per_sm", C.c_int), ("resident_index", C.c_int), ("zc_group_bytes", C.c_uint64),
                 ("sweep_walkers", C.c_uint64), ("load_factor", C.c_uint32), ("bucket_items", C.c_int),
-                ("no_prefill", C.c_int), ("hot_tier", C.c_int), ("host_plan", C.c_int)]
+                ("no_prefill", C.c_int), ("hot_tier", C.c_int), ("no_split", C.c_int),
+                ("host_plan", C.c_int)]
 
 
 class BatchTune(C.Structure):
@@ -95,7 +96,8 @@ class Stats(C.Structure):
                 ("prefill_loads", C.c_uint64),
                 ("bucket_ms", C.c_double), ("host_wait_ms", C.c_double), ("device_plans", C.c_uint64),
                 ("host_sched_ms", C.c_double), ("host_submit_ms", C.c_double), ("host_replay_ms", C.c_double),
-                ("host_observe_ms", C.c_double), ("hot_vertices", C.c_uint64), ("tier_build_ms", C.c_double)]
+                ("host_observe_ms", C.c_double), ("split_launches", C.c_uint64), ("hot_vertices", C.c_uint64),
+                ("tier_build_ms", C.c_double)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -436,7 +438,7 @@ class Engine:
                  sched: int = SCHED_PLAIN, pipeline: bool = True, zerocopy_threshold=None,
                  device: int = 0, ctas_per_sm: int = 0, resident_index: bool = True, zc_group_bytes: int = 0,
                  sweep_walkers: int = 0, load_factor: int = 0, bucket_items: int = 0, prefill: bool = True,
-                 host_plan: bool = False, hot_tier: int = 0):
+                 host_plan: bool = False, hot_tier: int = 0, split: bool = True):
         cfg = EngineCfg()
         lib.lt_engine_cfg_default(C.byref(cfg))
         cfg.device = device
@@ -456,6 +458,7 @@ class Engine:
         cfg.no_prefill = 0 if prefill else 1
         cfg.host_plan = int(host_plan)
         cfg.hot_tier = hot_tier
+        cfg.no_split = 0 if split else 1
         self.graph = graph
         self._h = C.c_void_p()
         check(lib.lt_engine_create(graph._h, C.byref(cfg), C.byref(self._h)))

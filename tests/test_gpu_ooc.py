@@ -200,10 +200,11 @@ def c2s(lt):
     return g, W, want, st
 
 
-@pytest.mark.parametrize("sched,pipeline,host_plan", [(2, True, False), (2, True, True), (4, True, False),
-                                                      (3, True, False), (0, True, False), (0, False, False),
-                                                      (1, True, False)])
-def test_c2s_scale_ooc(lt, require_gpu, c2s, sched, pipeline, host_plan):
+@pytest.mark.parametrize("sched,pipeline,host_plan,split", [(2, True, False, True), (2, True, True, True),
+                                                            (2, True, False, False), (4, True, False, True),
+                                                            (3, True, False, True), (0, True, False, True),
+                                                            (0, False, False, True), (1, True, False, True)])
+def test_c2s_scale_ooc(lt, require_gpu, c2s, sched, pipeline, host_plan, split):
     """16 of the graph's partitions cached, walker pool 2^22: every scheduler,
     with and without the load/compute overlap, gives the oracle's counts bit
     for bit, and wave runs read bounded zero-copy groups (the path that takes
@@ -212,10 +213,13 @@ def test_c2s_scale_ooc(lt, require_gpu, c2s, sched, pipeline, host_plan):
     cached partitions, so none keeps a queue (the reference stops walkers at
     each partition border, src/WalkManager.h:239, and computes the queues
     that builds up during loads).  Bucketing passes are planned by a device
-    kernel behind the step kernel, or (host_plan) by the host."""
+    kernel behind the step kernel, or (host_plan) by the host; wave runs
+    step the cached walkers and the zero-copy group in two concurrent
+    kernels (split) or in one."""
     g, W, want, st = c2s
     assert g.num_partitions > 16
-    e = lt.Engine(g, partitions=16, batch=1 << 22, seed=1, sched=sched, pipeline=pipeline, host_plan=host_plan)
+    e = lt.Engine(g, partitions=16, batch=1 << 22, seed=1, sched=sched, pipeline=pipeline, host_plan=host_plan,
+                  split=split)
     got = e.ppr(0, W, 0.15)
     assert (got == want).all()
     s = e.stats()
@@ -228,6 +232,10 @@ def test_c2s_scale_ooc(lt, require_gpu, c2s, sched, pipeline, host_plan):
         assert s["device_plans"] == 0
     else:
         assert s["device_plans"] > 0
+    if sched in (2, 3, 4):
+        assert (s["split_launches"] > 0) == split
+    else:
+        assert s["split_launches"] == 0
     e.close()
 
 
