@@ -35,7 +35,9 @@ namespace {
 constexpr unsigned kFull = 0xFFFFFFFFu;
 // idle lanes a warp waits for before refilling them (all lanes: always): the
 // refill sits on the warp's critical path and PPR's geometric walk lengths
-// would otherwise trigger one nearly every iteration
+// would otherwise trigger one nearly every iteration (also in zero-copy
+// launches, where refills are short beside host reads: on c2, thresholds 8
+// and 2 there made runs 4 % and 6 % slower)
 constexpr int kRefillMin = 24;
 
 __device__ __forceinline__ uint32_t find_part(const uint32_t *off, uint32_t P, uint32_t v)
