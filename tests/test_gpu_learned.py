@@ -13,7 +13,7 @@ up with the moving average (0.00196 vs 0.00158); at 16, 0.00017-0.00141 vs
 0.00129-0.00200.
 
 Against the plain scheduler it replaces (the reference policy, its fallback
-and judge) the learned one moves fewer host-link bytes per step in far
+and yardstick) the learned one moves fewer host-link bytes per step in far
 fewer iterations (measured: 9.2 vs 11.0 bytes/step, 97 vs 2048 iterations,
 18 vs 164 ms).  Against the LRU (batched) and moving-average (frequency)
 ablations the cache it keeps is no better on this graph (9.0-9.2 bytes/step
