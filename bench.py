@@ -476,6 +476,8 @@ def gb300_ooc(args, cfg):
              "learned_hostplan": dict(sched=lt.SCHED_LEARNED, host_plan=True),
              "learned_tile2k": dict(sched=lt.SCHED_LEARNED, bucket_items=8),
              "learned_nosplit": dict(sched=lt.SCHED_LEARNED, split=False),
+             "learned_nosweep": dict(sched=lt.SCHED_LEARNED, sweep_walkers=1),
+             "learned_sweep2m": dict(sched=lt.SCHED_LEARNED, sweep_walkers=1 << 21),
              "learned_tier25": dict(sched=lt.SCHED_LEARNED, hot_tier=25),
              "learned_tier75": dict(sched=lt.SCHED_LEARNED, hot_tier=75),
              "frequency_tier50": dict(sched=lt.SCHED_FREQUENCY, hot_tier=50)}

@@ -112,7 +112,7 @@ typedef struct lt_engine_cfg {
     uint64_t zc_group_bytes;         /* wave runs: estimated host bytes the partitions of one zero-copy
                                         group may touch (0 = 512 MiB; 128 MiB while serving) */
     uint64_t sweep_walkers;          /* wave runs: walkers left outside the cache at or below which one
-                                        kernel reads every uncached partition zero-copy (0 = 2^18) */
+                                        kernel reads every uncached partition zero-copy (0 = 2^14; 2^18 while serving) */
     uint32_t load_factor;            /* wave runs: a partition is loaded once its waiting walkers reach
                                         load_factor x zerocopy_threshold (0 = 256 / host bytes per
                                         zero-copy hop: 8 with the device index, 4 without) */

@@ -1254,7 +1254,14 @@ uint64_t wave_lazy_budget(Ooc &o, uint64_t chunks, uint64_t walkers, uint64_t le
     return std::min(g, left);
 }
 
-constexpr uint64_t kSweepWalkers = 1ull << 18;    // about one walker per resident lane
+// walkers left outside the cache at or below which one kernel reads every
+// uncached partition: few hops left, but each reads across the whole graph
+// (past the host-memory reach of fast zero-copy reads).  c2: 2^21 walkers
+// 1.06 s per run, 2^18 0.905 s, 1 (groups to the end) 0.895 s.  Serving
+// keeps 2^18: at light load every step is then one sweep that finishes the
+// admitted queries.
+constexpr uint64_t kSweepWalkers = 1ull << 14;
+constexpr uint64_t kSweepWalkersServe = 1ull << 18;
 constexpr double kRefillHorizon = 512.0;          // iterations a refill is credited with at most
 constexpr uint64_t kRefillHold = 128;             // iterations a partition stays before a refill may evict it
 constexpr int kRefillMax = 2;                     // refill swaps started per check
@@ -1321,7 +1328,8 @@ lt_status wave_step(Ooc &o, const RunParams &rp, WaveState &w, bool &done)
                                                                           : o.zc_threshold * load_factor;
     const uint64_t zc_group_bytes =
         e.cfg.zc_group_bytes ? e.cfg.zc_group_bytes : o.serve ? kZcGroupBytesServe : kZcGroupBytes;
-    const uint64_t sweep_walkers = e.cfg.sweep_walkers ? e.cfg.sweep_walkers : kSweepWalkers;
+    const uint64_t sweep_walkers =
+        e.cfg.sweep_walkers ? e.cfg.sweep_walkers : o.serve ? kSweepWalkersServe : kSweepWalkers;
     const uint64_t reserve = (uint64_t)o.P + 2;
     auto &inflight = w.inflight;
     auto &parts = w.parts;
