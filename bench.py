@@ -477,6 +477,10 @@ def gb300_ooc(args, cfg):
              "learned_tile2k": dict(sched=lt.SCHED_LEARNED, bucket_items=8),
              "learned_nosplit": dict(sched=lt.SCHED_LEARNED, split=False),
              "learned_nosweep": dict(sched=lt.SCHED_LEARNED, sweep_walkers=1),
+             "learned_zc256m": dict(sched=lt.SCHED_LEARNED, zc_group_bytes=256 << 20),
+             "learned_zc1g": dict(sched=lt.SCHED_LEARNED, zc_group_bytes=1 << 30),
+             "learned_lf4": dict(sched=lt.SCHED_LEARNED, load_factor=4),
+             "learned_lf16": dict(sched=lt.SCHED_LEARNED, load_factor=16),
              "learned_sweep2m": dict(sched=lt.SCHED_LEARNED, sweep_walkers=1 << 21),
              "learned_tier25": dict(sched=lt.SCHED_LEARNED, hot_tier=25),
              "learned_tier75": dict(sched=lt.SCHED_LEARNED, hot_tier=75),
