@@ -135,6 +135,9 @@ struct Ooc {
     // entered while it was cached, and step-kernel launches it was cached for
     std::vector<uint64_t> run_visits, run_cached_visits, run_cached_launches;
     std::vector<uint64_t> waiting, lazy_left, dev_waiting;
+    // 1 + the iteration since which a partition's queue has held walkers
+    // without a break (0: empty queue)
+    std::vector<uint64_t> wait_since;
 
     std::vector<Queue> q;
     std::unique_ptr<Policy> policy;
@@ -446,6 +449,10 @@ lt_status tier_build(Ooc &o, int app, int start, uint32_t source, const uint64_t
 void refresh(Ooc &o, uint32_t p)
 {
     o.waiting[p] = o.q[p].total();
+    if (o.waiting[p] == 0)
+        o.wait_since[p] = 0;
+    else if (o.wait_since[p] == 0)
+        o.wait_since[p] = o.iteration + 1;
     o.lazy_left[p] = o.q[p].lazy_left();
     o.dev_waiting[p] = o.q[p].dev_count();
 }
@@ -1594,7 +1601,11 @@ lt_status wave_step(Ooc &o, const RunParams &rp, WaveState &w, bool &done)
                 }
             const bool sweep = outside <= sweep_walkers && !lazy_left;
             if (!sweep) {
+                // serving: the partitions whose walkers have waited longest
+                // first (the latency tail of a query is its slowest walker),
+                // then the most waiting walkers
                 auto more = [&](uint32_t a, uint32_t b) {
+                    if (o.serve && o.wait_since[a] != o.wait_since[b]) return o.wait_since[a] < o.wait_since[b];
                     return o.waiting[a] != o.waiting[b] ? o.waiting[a] > o.waiting[b] : a < b;
                 };
                 // host bytes a partition's walkers touch: at most the partition,
@@ -1803,6 +1814,7 @@ lt_status ooc_create(lt_engine *e, Ooc **out)
     o->arrivals.assign(o->P, 0);
     o->visits.assign(o->P, 0);
     o->waiting.assign(o->P, 0);
+    o->wait_since.assign(o->P, 0);
     o->lazy_left.assign(o->P, 0);
     o->dev_waiting.assign(o->P, 0);
     o->run_visits.assign(o->P, 0);
