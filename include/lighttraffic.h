@@ -476,6 +476,16 @@ typedef struct lt_policy_stats {
  * counterpart in the reference. */
 lt_status lt_engine_policy_stats(const lt_engine *e, lt_policy_stats *out);
 
+/* ------------------------------------------------------------ ABI layout */
+
+/* Offset and size of a field of one of this header's structs, by name
+ * ("lt_engine_cfg", "num_device_walkers"), and the size of a struct, for
+ * bindings that mirror the structs (a cgo, JNI or ctypes layer can check its
+ * copy against the library it loads).  LT_ERR_INVALID / 0 for unknown
+ * names.  No GPU needed. */
+lt_status lt_abi_field(const char *type, const char *field, size_t *offset, size_t *size);
+size_t lt_abi_sizeof(const char *type);
+
 /* Per partition, over the engine's last out-of-core run: walkers that
  * entered it, those that entered while it was cached, and step-kernel
  * launches during which it was cached (P entries each; any may be NULL).

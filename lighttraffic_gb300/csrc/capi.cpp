@@ -1,5 +1,6 @@
 // capi.cpp -- extern "C" entry points declared in include/lighttraffic.h.
 #include <algorithm>
+#include <cstddef>
 #include <cstring>
 #include <new>
 
@@ -7,6 +8,127 @@
 #include "lt_core.cuh"
 
 using namespace lt;
+
+// ---- layout of the ABI structs, for bindings that mirror them (the Python
+// package checks its ctypes mirror against this table)
+
+namespace {
+struct AbiField {
+    const char *type, *field;
+    size_t offset, size;
+};
+#define LT_ABI_FIELD(T, F) {#T, #F, offsetof(T, F), sizeof(((T *)nullptr)->F)}
+const AbiField kAbiFields[] = {
+    LT_ABI_FIELD(lt_graph_info, num_nodes),
+    LT_ABI_FIELD(lt_graph_info, num_edges),
+    LT_ABI_FIELD(lt_graph_info, num_partitions),
+    LT_ABI_FIELD(lt_graph_info, partition_bytes),
+    LT_ABI_FIELD(lt_graph_info, max_nodes_in_partition),
+    LT_ABI_FIELD(lt_graph_info, max_edges_in_partition),
+    LT_ABI_FIELD(lt_engine_cfg, device),
+    LT_ABI_FIELD(lt_engine_cfg, num_device_partitions),
+    LT_ABI_FIELD(lt_engine_cfg, num_device_walkers),
+    LT_ABI_FIELD(lt_engine_cfg, sched),
+    LT_ABI_FIELD(lt_engine_cfg, pipeline),
+    LT_ABI_FIELD(lt_engine_cfg, zerocopy_threshold),
+    LT_ABI_FIELD(lt_engine_cfg, seed),
+    LT_ABI_FIELD(lt_engine_cfg, block_size),
+    LT_ABI_FIELD(lt_engine_cfg, ctas_per_sm),
+    LT_ABI_FIELD(lt_engine_cfg, resident_index),
+    LT_ABI_FIELD(lt_engine_cfg, zc_group_bytes),
+    LT_ABI_FIELD(lt_engine_cfg, sweep_walkers),
+    LT_ABI_FIELD(lt_engine_cfg, load_factor),
+    LT_ABI_FIELD(lt_engine_cfg, bucket_items),
+    LT_ABI_FIELD(lt_engine_cfg, no_prefill),
+    LT_ABI_FIELD(lt_engine_cfg, hot_tier),
+    LT_ABI_FIELD(lt_engine_cfg, no_split),
+    LT_ABI_FIELD(lt_engine_cfg, host_plan),
+    LT_ABI_FIELD(lt_stats, updates),
+    LT_ABI_FIELD(lt_stats, moves),
+    LT_ABI_FIELD(lt_stats, teleports),
+    LT_ABI_FIELD(lt_stats, iterations),
+    LT_ABI_FIELD(lt_stats, explicit_iterations),
+    LT_ABI_FIELD(lt_stats, h2d_graph_bytes),
+    LT_ABI_FIELD(lt_stats, h2d_walker_bytes),
+    LT_ABI_FIELD(lt_stats, d2h_walker_bytes),
+    LT_ABI_FIELD(lt_stats, zerocopy_bytes),
+    LT_ABI_FIELD(lt_stats, partition_loads),
+    LT_ABI_FIELD(lt_stats, kernel_launches),
+    LT_ABI_FIELD(lt_stats, running_ms),
+    LT_ABI_FIELD(lt_stats, graph_loading_ms),
+    LT_ABI_FIELD(lt_stats, computing_ms),
+    LT_ABI_FIELD(lt_stats, zerocopy_ms),
+    LT_ABI_FIELD(lt_stats, walker_loading_ms),
+    LT_ABI_FIELD(lt_stats, walker_evicting_ms),
+    LT_ABI_FIELD(lt_stats, graph_loading_calls),
+    LT_ABI_FIELD(lt_stats, computing_calls),
+    LT_ABI_FIELD(lt_stats, zerocopy_calls),
+    LT_ABI_FIELD(lt_stats, walker_loading_calls),
+    LT_ABI_FIELD(lt_stats, walker_evicting_calls),
+    LT_ABI_FIELD(lt_stats, step_kernel_ms),
+    LT_ABI_FIELD(lt_stats, handoffs),
+    LT_ABI_FIELD(lt_stats, overlap_computes),
+    LT_ABI_FIELD(lt_stats, zerocopy_groups),
+    LT_ABI_FIELD(lt_stats, zerocopy_sweeps),
+    LT_ABI_FIELD(lt_stats, cache_slots),
+    LT_ABI_FIELD(lt_stats, index_on_device),
+    LT_ABI_FIELD(lt_stats, refill_loads),
+    LT_ABI_FIELD(lt_stats, prefill_loads),
+    LT_ABI_FIELD(lt_stats, bucket_ms),
+    LT_ABI_FIELD(lt_stats, host_wait_ms),
+    LT_ABI_FIELD(lt_stats, device_plans),
+    LT_ABI_FIELD(lt_stats, host_sched_ms),
+    LT_ABI_FIELD(lt_stats, host_submit_ms),
+    LT_ABI_FIELD(lt_stats, host_replay_ms),
+    LT_ABI_FIELD(lt_stats, host_observe_ms),
+    LT_ABI_FIELD(lt_stats, split_launches),
+    LT_ABI_FIELD(lt_stats, hot_vertices),
+    LT_ABI_FIELD(lt_stats, tier_build_ms),
+    LT_ABI_FIELD(lt_checkpoint_info, app),
+    LT_ABI_FIELD(lt_checkpoint_info, start_mode),
+    LT_ABI_FIELD(lt_checkpoint_info, source),
+    LT_ABI_FIELD(lt_checkpoint_info, length),
+    LT_ABI_FIELD(lt_checkpoint_info, runs),
+    LT_ABI_FIELD(lt_checkpoint_info, run_index),
+    LT_ABI_FIELD(lt_checkpoint_info, num_walkers),
+    LT_ABI_FIELD(lt_checkpoint_info, num_nodes),
+    LT_ABI_FIELD(lt_checkpoint_info, has_endpoints),
+    LT_ABI_FIELD(lt_checkpoint_info, has_paths),
+    LT_ABI_FIELD(lt_checkpoint_info, iteration),
+    LT_ABI_FIELD(lt_batch_tune, block),
+    LT_ABI_FIELD(lt_batch_tune, ctas_per_sm),
+    LT_ABI_FIELD(lt_batch_tune, load_shift),
+    LT_ABI_FIELD(lt_batch_tune, tuned),
+    LT_ABI_FIELD(lt_ooc_tune, tuned),
+    LT_ABI_FIELD(lt_ooc_tune, trial_walkers),
+    LT_ABI_FIELD(lt_ooc_tune, zc_group_bytes),
+    LT_ABI_FIELD(lt_ooc_tune, load_factor),
+    LT_ABI_FIELD(lt_ooc_tune, ctas_per_sm),
+    LT_ABI_FIELD(lt_ooc_tune, bucket_items),
+    LT_ABI_FIELD(lt_ooc_tune, default_ms),
+    LT_ABI_FIELD(lt_ooc_tune, tuned_ms),
+    LT_ABI_FIELD(lt_policy_stats, name),
+    LT_ABI_FIELD(lt_policy_stats, train_steps),
+    LT_ABI_FIELD(lt_policy_stats, net_loss),
+    LT_ABI_FIELD(lt_policy_stats, baseline_loss),
+    LT_ABI_FIELD(lt_policy_stats, predictions),
+    LT_ABI_FIELD(lt_policy_stats, net_used),
+};
+#undef LT_ABI_FIELD
+const struct {
+    const char *type;
+    size_t size;
+} kAbiTypes[] = {
+    {"lt_graph_info", sizeof(lt_graph_info)},
+    {"lt_engine_cfg", sizeof(lt_engine_cfg)},
+    {"lt_stats", sizeof(lt_stats)},
+    {"lt_checkpoint_info", sizeof(lt_checkpoint_info)},
+    {"lt_batch_tune", sizeof(lt_batch_tune)},
+    {"lt_ooc_tune", sizeof(lt_ooc_tune)},
+    {"lt_policy_stats", sizeof(lt_policy_stats)},
+};
+}  // namespace
+
 
 extern "C" {
 
@@ -490,6 +612,26 @@ void lt_host_free(void *p)
 lt_status lt_rowptr_narrow(const uint64_t *d_rowptr, uint32_t *d_rowptr32, uint32_t num_nodes, void *stream)
 {
     return rowptr_narrow(d_rowptr, d_rowptr32, num_nodes, (cudaStream_t)stream);
+}
+
+lt_status lt_abi_field(const char *type, const char *field, size_t *offset, size_t *size)
+{
+    if (!type || !field || !offset || !size) return LT_ERR_INVALID;
+    for (const AbiField &f : kAbiFields)
+        if (std::strcmp(f.type, type) == 0 && std::strcmp(f.field, field) == 0) {
+            *offset = f.offset;
+            *size = f.size;
+            return LT_OK;
+        }
+    return LT_ERR_INVALID;
+}
+
+size_t lt_abi_sizeof(const char *type)
+{
+    if (!type) return 0;
+    for (const auto &t : kAbiTypes)
+        if (std::strcmp(t.type, type) == 0) return t.size;
+    return 0;
 }
 
 }  // extern "C"

@@ -134,3 +134,37 @@ def test_cli_accepts_host_index(lt):
     exe = os.path.join(lt.BIN_DIR, "ppr")
     r = subprocess.run([exe, "-f", "/nonexistent.bcsr", "--host-index"], capture_output=True, text=True)
     assert r.returncode == 1 and "cannot open" in r.stderr
+
+
+_MIRRORS = {"lt_graph_info": "GraphInfo", "lt_engine_cfg": "EngineCfg", "lt_stats": "Stats",
+            "lt_checkpoint_info": "CheckpointInfo", "lt_batch_tune": "BatchTune", "lt_ooc_tune": "OocTune",
+            "lt_policy_stats": "PolicyStats"}
+
+
+@pytest.mark.parametrize("ctype", sorted(_MIRRORS))
+def test_ctypes_mirror_matches_abi_layout(lt, ctype):
+    """Every field of the package's ctypes mirror sits at the offset, with the
+    size, the library reports for its C struct, and the structs are the same
+    size: a field added to the header in one place but not the other, or in
+    another order, fails here (no GPU needed)."""
+    lib = ctypes.CDLL(lt.LIB_PATH)
+    lib.lt_abi_field.argtypes = [ctypes.c_char_p, ctypes.c_char_p, ctypes.POINTER(ctypes.c_size_t),
+                                 ctypes.POINTER(ctypes.c_size_t)]
+    lib.lt_abi_field.restype = ctypes.c_int
+    lib.lt_abi_sizeof.argtypes = [ctypes.c_char_p]
+    lib.lt_abi_sizeof.restype = ctypes.c_size_t
+    mirror = getattr(lt, _MIRRORS[ctype])
+    assert lib.lt_abi_sizeof(ctype.encode()) == ctypes.sizeof(mirror)
+    for name, _ in mirror._fields_:
+        off, size = ctypes.c_size_t(), ctypes.c_size_t()
+        assert lib.lt_abi_field(ctype.encode(), name.encode(), ctypes.byref(off), ctypes.byref(size)) == 0, name
+        f = getattr(mirror, name)
+        assert (f.offset, f.size) == (off.value, size.value), f"{ctype}.{name}"
+
+
+def test_abi_layout_rejects_unknown_names(lt):
+    lib = ctypes.CDLL(lt.LIB_PATH)
+    lib.lt_abi_sizeof.restype = ctypes.c_size_t
+    off, size = ctypes.c_size_t(), ctypes.c_size_t()
+    assert lib.lt_abi_field(b"lt_engine_cfg", b"no_such_field", ctypes.byref(off), ctypes.byref(size)) == 1
+    assert lib.lt_abi_sizeof(b"lt_no_such_struct") == 0
